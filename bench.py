@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Benchmark: exact k-clique counting on one GB300, matches/s and GTEPS.
+
+Workload (the k-clique configuration): R-MAT scale 22 (4,194,304 vertices), edge factor
+16 (67,108,864 samples), (a,b,c,d) = (0.57,0.19,0.19,0.05), seed 2; symmetrised,
+deduplicated, self-loops removed, degree-oriented DAG (ties by id), int32 CSR.  Seeded
+synthetic data stands in for the reference's real-world graphs.
+
+A step is one exact count of the pattern (default 4-clique) over the whole graph through
+the engine: task generation (schedule) + the persistent counting launch, graph resident
+in HBM.  `value` is matches/s from CUDA-event device time; `e2e` is the same metric
+through the C ABI from host CSR buffers (pinned), host->device copy, GPU orientation,
+count and the 8-byte result read inside the timed region.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl engine|reference]
+                  [--pattern 4-clique|5-clique] [--policy learned|heuristic]
+
+--impl reference times the reference's CPU counting algorithm (oracle port of the
+G2Miner OpenMP path, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"graph": "rmat", "scale": 22, "edge_factor": 16, "abcd": [0.57, 0.19, 0.19, 0.05],
+            "seed": 2}
+PATTERN_KIND = {"4-clique": "clique4", "5-clique": "clique5", "triangle": "tc"}
+COSTMODEL = os.path.join(ROOT, "x-gminer_gb300", "costmodel.json")
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--pattern", default="4-clique", choices=list(PATTERN_KIND))
+    p.add_argument("--policy", default="learned", choices=["learned", "heuristic"])
+    p.add_argument("--scale", type=int, default=WORKLOAD["scale"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            backend = "nccl" if _cuda_ok() else "gloo"
+            td.init_process_group(backend)
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        dev = f"cuda:{self.local}" if _cuda_ok() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def _cuda_ok() -> bool:
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def _sync():
+    if _cuda_ok():
+        import torch
+
+        torch.cuda.synchronize()
+
+
+# ----------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------- helpers
+def load_engine():
+    return importlib.import_module("x-gminer_gb300")
+
+
+def load_model(xgm, ctx):
+    if not os.path.exists(COSTMODEL):
+        return None
+    with open(COSTMODEL) as f:
+        spec = json.load(f)
+    import numpy as np
+
+    m = xgm.Model(ctx)
+    m.set_params(np.asarray(spec["params"], dtype=np.float32))
+    return m
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic(pattern: str):
+    """dram bytes per launch of the counting kernel from the committed ncu summary."""
+    name = {"4-clique": "k_clique4", "5-clique": "k_clique5", "triangle": "k_clique3"}[pattern]
+    path = os.path.join(ROOT, "profiles", f"{name}_rmat_s22.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_sample(orc, kind: str, drow, dcol, budget_s: float):
+    """Times the oracle port on every `stride`-th top-level vertex (all host threads),
+    with the stride picked from a short calibration so the sample takes ~budget_s."""
+    nv = len(drow) - 1
+    cores = orc.threads()
+    stride = 1 << 12
+    t0 = time.perf_counter()
+    orc.count(kind, drow, dcol, 0, nv, stride)
+    t_cal = max(time.perf_counter() - t0, 1e-3)
+    est_full = t_cal * stride
+    stride = max(1, int(est_full / budget_s))
+    t0 = time.perf_counter()
+    c = orc.count(kind, drow, dcol, 0, nv, stride)
+    dt = time.perf_counter() - t0
+    return c, dt, stride, cores
+
+
+def gen_graph(xgm, scale):
+    a, b, c, _ = WORKLOAD["abcd"]
+    return xgm.gen_rmat(scale, WORKLOAD["edge_factor"], a, b, c, seed=WORKLOAD["seed"])
+
+
+# ------------------------------------------------------------------- engine arm
+def engine_arm(args, dist: Dist) -> None:
+    import numpy as np
+    import torch
+
+    xgm = load_engine()
+    torch.cuda.set_device(dist.local)
+    ctx = xgm.Context(dist.local)
+    nv, src, dst = gen_graph(xgm, args.scale)
+    g = ctx.graph_from_edges(nv, src, dst)
+    del src, dst
+    info = g.info()
+    model = load_model(xgm, ctx) if args.policy == "learned" else None
+    policy = xgm.SCHED_LEARNED if model is not None else xgm.SCHED_HEURISTIC
+    kw = {"policy": policy, "model": model}
+
+    def run(n, **k):
+        prep, kern, cnt = [], [], None
+        for _ in range(n):
+            cnt, st = ctx.count(g, args.pattern, with_stats=True, **k)
+            prep.append(st["prep_ms"])
+            kern.append(st["kernel_ms"])
+        return cnt, prep, kern
+
+    run(args.warmup, **kw)
+    dist.barrier()
+    _sync()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    t0 = time.perf_counter()
+    count, prep, kern = run(args.steps, **kw)
+    _sync()
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clk = clocks.stop()
+    step_ms = [p + k for p, k in zip(prep, kern)]
+    ms_per_step = dist.reduce(sum(step_ms) / args.steps, "max")
+    total_matches = dist.reduce(float(count), "sum")
+    value = total_matches / (ms_per_step / 1e3)
+    kern_ms = statistics.mean(kern)
+
+    # plain heuristic schedule on the same graph and steps (the learned schedule's judge)
+    plain = None
+    if policy == xgm.SCHED_LEARNED:
+        run(1, policy=xgm.SCHED_HEURISTIC)
+        c2, p2, k2 = run(args.steps, policy=xgm.SCHED_HEURISTIC)
+        assert c2 == count, "schedules disagree on the count"
+        pms = dist.reduce(sum(p + k for p, k in zip(p2, k2)) / args.steps, "max")
+        plain = {"matches_per_s": total_matches / (pms / 1e3), "ms_per_step": pms,
+                 "kernel_ms": statistics.mean(k2)}
+
+    launches = ctx.count_kernels(g, args.pattern, **kw)
+    peaks = measured_peaks()
+    algo = ctx.algo_bytes(g, args.pattern)
+    achieved = algo / (kern_ms / 1e3) / 1e9
+    traffic = profile_traffic(args.pattern)
+    line = {
+        "metric": "matches_per_sec",
+        "value": value,
+        "unit": "matches/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32 ids / uint64 counts",
+        "data": "synthetic (seeded R-MAT, engine host generator)",
+        "config": {"workload": f"{args.pattern} counting, R-MAT scale {args.scale} edge factor 16",
+                   "pattern": args.pattern, "graph": dict(WORKLOAD, scale=args.scale),
+                   "V": info["V"], "E_undirected_entries": info["E"], "E_dag": info["E_dag"],
+                   "max_degree": info["max_degree"], "max_out_degree": info["max_out_degree"],
+                   "schedule": "learned" if policy == xgm.SCHED_LEARNED else "heuristic",
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (adjacency %.0f MB > 129 MB)" % (info["E"] * 4 / 2**20)},
+        "count": count,
+        "gteps": info["E_dag"] / (ms_per_step / 1e3) / 1e9,
+        "kernel_ms": kern_ms,
+        "prep_ms": statistics.mean(prep),
+        "wall_ms_per_step": wall * 1e3 / args.steps,
+        "plain_heuristic": plain,
+        "gpu_launches": launches * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": traffic, "algo_bytes_per_launch": algo,
+                     "peak_source": peaks["source"]},
+        "clocks": clk,
+    }
+
+    # end to end through the C ABI from pinned host buffers
+    if not args.no_e2e:
+        rowptr, col = g.download()
+        rp = torch.empty(len(rowptr), dtype=torch.int64, pin_memory=True)
+        cp = torch.empty(len(col), dtype=torch.int32, pin_memory=True)
+        rp.numpy()[:] = rowptr
+        cp.numpy()[:] = col
+        del rowptr, col
+        g.close()
+        e2e_t = []
+        for i in range(args.warmup + args.steps):
+            _sync()
+            t0 = time.perf_counter()
+            ge = ctx.graph_from_csr(rp.numpy(), cp.numpy())
+            c3 = ctx.count(ge, args.pattern, **kw)
+            ge.close()
+            _sync()
+            if i >= args.warmup:
+                e2e_t.append(time.perf_counter() - t0)
+            assert c3 == count
+        e2e_s = dist.reduce(sum(e2e_t) / len(e2e_t), "max")
+        line["e2e"] = {"value": total_matches / e2e_s, "unit": "matches/s",
+                       "h2d_bytes_per_step": int(rp.numel() * 8 + cp.numel() * 4),
+                       "d2h_bytes_per_step": 8, "ms_per_step": e2e_s * 1e3}
+        g = None
+
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        import oracle
+
+        if g is None:
+            rowptr, col = rp.numpy(), cp.numpy()
+        else:
+            rowptr, col = g.download()
+        drow, dcol = oracle.orient(rowptr, col)
+        c, dt, stride, cores = cpu_sample(oracle, PATTERN_KIND[args.pattern], drow, dcol,
+                                          args.cpu_seconds)
+        line["cpu_baseline"] = {"value": c / dt, "unit": "matches/s", "cores": cores,
+                                "kind": "port",
+                                "sample": f"every {stride}-th top-level vertex of the same DAG "
+                                          f"({c} matches in {dt:.2f} s, OpenMP oracle port)"}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+# ---------------------------------------------------------------- reference arm
+def reference_arm(args, dist: Dist) -> None:
+    if dist.rank != 0:
+        return
+    import oracle
+
+    xgm = load_engine()  # host generator only (no GPU use)
+    nv, src, dst = gen_graph(xgm, args.scale)
+    rowptr, col = oracle.build_csr(nv, src, dst)
+    del src, dst
+    drow, dcol = oracle.orient(rowptr, col)
+    kind = PATTERN_KIND[args.pattern]
+    per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
+    c, dt, stride, cores = cpu_sample(oracle, kind, drow, dcol, per_step)
+    times, counts = [], []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ci = oracle.count(kind, drow, dcol, 0, nv, stride)
+        t = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(t)
+            counts.append(ci)
+    ms = statistics.mean(times) * 1e3
+    value = counts[-1] / (ms / 1e3)
+    sample = (f"every {stride}-th top-level vertex of the R-MAT s{args.scale} DAG "
+              f"({counts[-1]} matches per step); oracle port of the OpenMP path")
+    line = {"metric": "matches_per_sec", "value": value, "unit": "matches/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 ids / uint64 counts", "data": "synthetic (seeded R-MAT)",
+            "config": {"workload": f"{args.pattern} counting, R-MAT scale {args.scale} edge factor 16",
+                       "pattern": args.pattern, "graph": dict(WORKLOAD, scale=args.scale)},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "matches/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "matches/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            engine_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

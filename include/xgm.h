@@ -1,0 +1,253 @@
+/*
+ * xgm.h - C ABI of the GB300 pattern-counting engine.
+ *
+ * The engine takes a graph plus a pattern plan and returns exact uint64 counts.
+ * It replaces the counting call of X-GMiner / GLUMIN / G2Miner:
+ *
+ *   TCSolver(Graph&, uint64_t& total, int n_gpu, int chunk)
+ *       codes/GraphMiner/src/triangle/main.cc:5, impl gpu_base.cu:25-74
+ *   CliqueSolver(Graph&, int k, uint64_t& total, int, int)
+ *       codes/GraphMiner/src/clique/main.cc:6, impl clique/gpu_base.cu:16
+ *   ScSolver(Graph&, Pattern&, uint64_t& total, int, int)
+ *       codes/GraphMiner/src/count/main.cc:7, impl count/omp_base.cc:5-58
+ *   GLUMIN::CliqueSolver_[LUT_]on_G2Miner(Graph_V2&) writing total[0]
+ *       xgminer/include/glumin.h:82-86, xgminer/src/glumin/glumin_GM_solver.cu:1083-1235
+ *
+ * Conventions.
+ *  - Every call returns an xgm_status; nothing exits or aborts.  A device-side error
+ *    flag (bounds, bounded-wait timeout) is reported as XGM_ERR_DEVICE / XGM_ERR_TIMEOUT.
+ *  - Host buffers belong to the caller and are copied; device memory and the CUDA
+ *    stream belong to the context and are released by the matching *_destroy call.
+ *  - A context is used by one host thread at a time; contexts are independent.
+ *  - Vertex ids are int32 (vidType, codes/GraphMiner/include/common.h:36), row
+ *    pointers int64 (eidType, common.h:37), counts uint64 (AccType, common.h:40).
+ */
+#ifndef XGM_H_
+#define XGM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum {
+  XGM_OK = 0,
+  XGM_ERR_INVALID = 1,     /* bad argument */
+  XGM_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  XGM_ERR_OOM = 3,         /* device allocation failed */
+  XGM_ERR_DEVICE = 4,      /* a kernel raised its error flag (bounds check) */
+  XGM_ERR_TIMEOUT = 5,     /* a bounded device-side wait ran out */
+  XGM_ERR_UNSUPPORTED = 6, /* pattern / option not implemented */
+  XGM_ERR_IO = 7,          /* graph file missing or malformed */
+  XGM_ERR_GRAPH = 8,       /* CSR failed validation (unsorted, self-loop, id out of range) */
+  XGM_ERR_NO_DEVICE = 9    /* no CUDA device visible */
+} xgm_status;
+
+const char* xgm_status_string(xgm_status s);
+
+typedef struct xgm_ctx xgm_ctx;
+typedef struct xgm_graph xgm_graph;
+typedef struct xgm_plan xgm_plan;
+typedef struct xgm_batch xgm_batch;
+typedef struct xgm_model xgm_model;
+
+/* ----------------------------------------------------------------- context */
+typedef struct {
+  int device;        /* CUDA ordinal */
+  int reserved_flags;
+} xgm_config;
+
+/* Creates a context on cfg->device (NULL: device 0) with its own stream. */
+xgm_status xgm_create(xgm_ctx** out, const xgm_config* cfg);
+void xgm_destroy(xgm_ctx* ctx);
+/* Text of the last error raised on this context (never NULL). */
+const char* xgm_last_error(const xgm_ctx* ctx);
+/* The context's CUDA stream, as a void* cudaStream_t. */
+void* xgm_stream(xgm_ctx* ctx);
+
+/* ------------------------------------------------------------------- graph */
+/* Host CSR in the reference's binary layout: rowptr int64[V+1] (graph.vertex.bin),
+ * colidx int32[E] (graph.edge.bin); graph_v2.cpp:23-49, graph.cc:20-45. */
+typedef struct {
+  int64_t num_vertices;
+  int64_t num_edges;
+  const int64_t* rowptr;
+  const int32_t* colidx;
+} xgm_csr_host;
+
+enum {
+  XGM_BUILD_SYMMETRIZE = 1,  /* add (v,u) for every (u,v) */
+  XGM_BUILD_DEDUP = 2,       /* drop repeated edges */
+  XGM_BUILD_DROP_SELF = 4,   /* drop (v,v) */
+  XGM_BUILD_VALIDATE = 8,    /* upload only: reject unsorted/duplicate/self/out-of-range */
+  XGM_BUILD_CLEAN = 7        /* SYMMETRIZE|DEDUP|DROP_SELF */
+};
+
+typedef struct {
+  int64_t num_vertices;
+  int64_t num_edges;      /* undirected CSR entries (2 x undirected edges) */
+  int64_t num_dag_edges;  /* edges kept by the degree orientation */
+  int64_t max_degree;
+  int64_t max_out_degree; /* of the oriented DAG */
+  int64_t num_triangles_hint; /* reserved, 0 */
+} xgm_graph_info;
+
+/* Uploads an undirected CSR (as Graph_V2 loads it) and builds on the GPU the degree
+ * orientation (graph_v2.cpp:243-289), the vertex ranking used by the kernels and the
+ * task lists.  flags: XGM_BUILD_VALIDATE checks the input on the GPU; XGM_BUILD_CLEAN
+ * bits re-run the CSR build over the given entries. */
+xgm_status xgm_graph_upload(xgm_ctx* ctx, const xgm_csr_host* csr, int flags,
+                            xgm_graph** out);
+/* Builds the CSR on the GPU from raw edge samples (the offline step of
+ * scripts/graph_format_conversion.py:20-44 plus dedupe and self-loop removal),
+ * then the same as xgm_graph_upload.  Ids must lie in [0, num_vertices). */
+xgm_status xgm_graph_build_from_edges(xgm_ctx* ctx, int64_t num_vertices,
+                                      const int32_t* src, const int32_t* dst,
+                                      int64_t num_samples, int flags, xgm_graph** out);
+/* Loads <prefix>.meta.txt / .vertex.bin / .edge.bin (graph_v2.cpp:5-134). */
+xgm_status xgm_graph_load(xgm_ctx* ctx, const char* prefix, int flags, xgm_graph** out);
+xgm_status xgm_graph_info_get(const xgm_graph* g, xgm_graph_info* out);
+enum { XGM_VIEW_UNDIRECTED = 0, XGM_VIEW_DAG = 1 };
+/* Copies a CSR view back to host arrays sized from xgm_graph_info (original ids). */
+xgm_status xgm_graph_download(xgm_ctx* ctx, const xgm_graph* g, int view, int64_t* rowptr,
+                              int32_t* colidx);
+void xgm_graph_destroy(xgm_graph* g);
+
+/* Host-side file helpers in the reference layout. */
+xgm_status xgm_graph_write_files(const char* prefix, const xgm_csr_host* csr);
+
+/* -------------------------------------------------------------------- plan */
+/* Builtin patterns.  Cliques and the triangle run on the degree-oriented DAG
+ * (USE_DAG, codes/GraphMiner/include/defines.h:12); the other motifs are
+ * edge-induced counts on the undirected graph (count/omp_base.cc:5-58). */
+typedef enum {
+  XGM_PATTERN_TRIANGLE = 1,
+  XGM_PATTERN_CLIQUE4 = 2,
+  XGM_PATTERN_CLIQUE5 = 3,
+  XGM_PATTERN_DIAMOND = 4,          /* edge-induced, diamond.h */
+  XGM_PATTERN_CYCLE4 = 5,           /* edge-induced, rectangle.h */
+  XGM_PATTERN_TAILED_TRIANGLE = 6   /* edge-induced, tailedtriangle.h */
+} xgm_pattern;
+
+typedef struct {
+  int builtin;            /* xgm_pattern, or 0 to match `adj` */
+  int num_vertices;       /* pattern size when builtin == 0 (3..5) */
+  uint8_t adj[8][8];      /* pattern adjacency when builtin == 0 */
+  int induced;            /* 0: edge-induced (the only kind supported for motifs) */
+} xgm_plan_desc;
+
+xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* desc, xgm_plan** out);
+/* Plan for a reference pattern name ("triangle", "4-clique", "5-clique", "diamond",
+ * "rectangle", "4-cycle", "tailedtriangle"; Pattern(name), count/main.cc:17) */
+xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out);
+int xgm_plan_pattern(const xgm_plan* p);
+void xgm_plan_destroy(xgm_plan* p);
+
+/* ---------------------------------------------------------------- schedule */
+typedef enum {
+  XGM_SCHED_HEURISTIC = 0, /* degree-threshold split (common.h:114-116 analogue) */
+  XGM_SCHED_LEARNED = 1,   /* MLP cost model picks variant + order; needs a model */
+  XGM_SCHED_FIXED = 2      /* force `variant` for every task (tuning / logging) */
+} xgm_sched_policy;
+
+/* Kernel variants a task can run with. */
+typedef enum {
+  XGM_VAR_WARP = 0,   /* one warp per task, frontier bitmap in shared memory */
+  XGM_VAR_CTA = 1,    /* one CTA per task, frontier bitmap in shared memory */
+  XGM_VAR_SPLIT = 2,  /* task split into per-edge sub-tasks (hub vertices) */
+  XGM_NUM_VARIANTS = 3
+} xgm_variant;
+
+typedef struct {
+  int policy;             /* xgm_sched_policy */
+  int variant;            /* for XGM_SCHED_FIXED */
+  const xgm_model* model; /* for XGM_SCHED_LEARNED */
+  int warp_max;           /* heuristic: out-degree <= warp_max -> WARP (0: default) */
+  int cta_max;            /* heuristic: out-degree <= cta_max -> CTA, else SPLIT (0: default) */
+  int order_by_cost;      /* learned: 1 = heaviest predicted tasks first */
+} xgm_sched;
+
+typedef struct {
+  double kernel_ms;        /* device time of the counting launch(es) */
+  double prep_ms;          /* device time of task generation / scheduling */
+  int64_t tasks;           /* top-level tasks */
+  int64_t variant_tasks[XGM_NUM_VARIANTS];
+  uint64_t algo_bytes;     /* algorithmic adjacency bytes of the plan (0 unless requested) */
+  uint32_t device_error;   /* raw device error flag */
+  int launches;            /* kernels launched by the call */
+} xgm_stats;
+
+/* Counts `plan` on `g`.  out_count receives the exact uint64 total. */
+xgm_status xgm_count(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
+                     const xgm_sched* sched, uint64_t* out_count, xgm_stats* stats);
+
+/* Reference-shaped convenience entry points (same meaning as the solvers cited in the
+ * file header; n_gpu / chunk arguments are dropped: one GPU, persistent queue). */
+xgm_status xgm_tc_solver(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total);
+xgm_status xgm_clique_solver(xgm_ctx* ctx, const xgm_graph* g, int k, uint64_t* total);
+xgm_status xgm_sc_solver(xgm_ctx* ctx, const xgm_graph* g, const char* pattern,
+                         uint64_t* total);
+
+/* Number of kernels one xgm_count call with these arguments launches (the call's
+ * device work is captured once into a CUDA graph and its kernel nodes counted). */
+xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
+                             const xgm_sched* sched, int* n_kernels);
+
+/* Algorithmic adjacency bytes the plan reads on g (host pass over the downloaded
+ * graph; 4 B per int32 element + 8 B per task), used as the roofline numerator. */
+xgm_status xgm_algo_bytes(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
+                          uint64_t* bytes);
+
+/* -------------------------------------------------------------- cost model */
+/* Learned scheduler: a 12 -> 32 (ReLU) -> 1 MLP with fp16 weights and fp32
+ * accumulation that predicts log2(warp-cycles) of a task under a kernel variant.  It is
+ * trained by the engine's own forward/backward kernels on per-task timings the engine
+ * logs (xgm_model_collect), and used by XGM_SCHED_LEARNED to pick each task's variant
+ * and to order the queues heaviest-first.  It changes the schedule only, never a count.
+ * No counterpart in the reference (its schedule is the fixed heuristic of
+ * xgminer/include/glumin/common.h:114-116). */
+#define XGM_MODEL_FEATURES 12
+#define XGM_MODEL_HIDDEN 32
+#define XGM_MODEL_PARAMS (XGM_MODEL_HIDDEN * XGM_MODEL_FEATURES + 2 * XGM_MODEL_HIDDEN + 1)
+
+/* Parameter layout (fp32 view): W1[32][12] row-major, b1[32], w2[32], b2. */
+xgm_status xgm_model_create(xgm_ctx* ctx, uint64_t seed, xgm_model** out);
+void xgm_model_destroy(xgm_model* m);
+xgm_status xgm_model_set_params(xgm_model* m, const float* params);
+xgm_status xgm_model_get_params(const xgm_model* m, float* params);
+/* Runs `plan` on g with every task forced to `variant` (tasks the variant cannot hold
+ * fall back by capacity) and per-task timing on, and returns samples of the tasks that
+ * ran with `variant`: features X[n][12], targets y[n] = log2(cycles * warps used), for
+ * every `stride`-th such task, at most max_rows.  count_out (optional) gets the count. */
+xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan, int variant,
+                             int stride, float* X, float* y, int64_t max_rows, int64_t* n_rows,
+                             uint64_t* count_out);
+/* Adam on mean squared error, minibatches of `batch`, on the GPU. */
+xgm_status xgm_model_train(xgm_ctx* ctx, xgm_model* m, const float* X, const float* y, int64_t n,
+                           int epochs, int batch, float lr, uint64_t seed, float* final_loss);
+xgm_status xgm_model_predict(xgm_ctx* ctx, const xgm_model* m, const float* X, int64_t n,
+                             float* y);
+/* Mean squared error and its gradient with respect to the (fp16-rounded) parameters. */
+xgm_status xgm_model_loss_grad(xgm_ctx* ctx, const xgm_model* m, const float* X, const float* y,
+                               int64_t n, float* loss, float* grad);
+
+/* ------------------------------------------------------ generators (host) */
+/* Write `m` raw samples to caller arrays; with src == NULL return the sample count.
+ * Returns -1 on bad arguments. */
+int64_t xgm_gen_rmat(int scale, int edge_factor, double a, double b, double c,
+                     uint64_t seed, int32_t* src, int32_t* dst);
+int64_t xgm_gen_er(int64_t n, int64_t m, uint64_t seed, int32_t* src, int32_t* dst);
+int64_t xgm_gen_chung_lu(int64_t n, double gamma, double w_max, double avg_deg,
+                         uint64_t seed, int32_t* src, int32_t* dst);
+int64_t xgm_gen_ba(int64_t n, int m, uint64_t seed, int32_t* src, int32_t* dst);
+int64_t xgm_gen_ba_batch(int num_graphs, int64_t n_lo, int64_t n_hi, int m_lo, int m_hi,
+                         uint64_t seed, int64_t* vtx_off, int64_t* edge_off, int32_t* src,
+                         int32_t* dst);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XGM_H_ */

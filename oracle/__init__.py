@@ -1,0 +1,193 @@
+"""CPU oracle for the GB300 counting engine.
+
+TEST INFRASTRUCTURE ONLY.  Loaded by the tests, by __graft_entry__.smoke() and by the
+CPU-baseline leg of bench.py as the checker; the engine never imports or calls it.
+
+ - oracle.c: plain-C restatement of the reference's OpenMP counting path (each
+   function cites the reference lines it follows), built here into liborc.so.
+ - _ref/: the reference's own OpenMP binaries built from its sources by build_ref.sh
+   (only where the reference tree is present); run_ref() runs them on graph files.
+ - mlp_ref.py: numpy forward/backward of the cost model, the gradient checker.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import shutil
+import subprocess
+from typing import Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "oracle.c")
+LIB = os.path.join(HERE, "liborc.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+_lib = None
+
+
+def build() -> str:
+    """Compiles oracle.c (OpenMP when the compiler has it)."""
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler for the oracle")
+    tmp = LIB + ".tmp"
+    base = [cc, "-O3", "-std=c11", "-fPIC", "-shared", SRC, "-o", tmp]
+    r = subprocess.run(base[:2] + ["-fopenmp"] + base[2:], capture_output=True, text=True)
+    if r.returncode != 0:
+        r = subprocess.run(base, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_ref() -> bool:
+    """Builds the reference's own OpenMP binaries into _ref/ when the tree is present."""
+    r = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], capture_output=True,
+                       text=True)
+    return r.returncode == 0 and os.path.exists(os.path.join(REF_DIR, "tc_omp_base"))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        P, I64, U64 = C.c_void_p, C.c_int64, C.c_uint64
+        L.orc_max_threads.restype = C.c_int
+        L.orc_has_openmp.restype = C.c_int
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_free.argtypes = [P]
+        L.orc_build_csr.restype = C.c_int
+        L.orc_build_csr.argtypes = [I64, P, P, I64, C.c_int, C.POINTER(P), C.POINTER(P),
+                                    C.POINTER(I64)]
+        L.orc_orient.restype = C.c_int
+        L.orc_orient.argtypes = [I64, P, P, C.POINTER(P), C.POINTER(P), C.POINTER(I64)]
+        for name in ("orc_tc", "orc_diamond", "orc_cycle4", "orc_tailed_triangle"):
+            f = getattr(L, name)
+            f.restype = U64
+            f.argtypes = [I64, P, P, I64, I64, I64]
+        for name in ("orc_clique4", "orc_clique5"):
+            f = getattr(L, name)
+            f.restype = U64
+            f.argtypes = [I64, P, P, I64, I64, I64, I64]
+        L.orc_algo_bytes.restype = U64
+        L.orc_algo_bytes.argtypes = [C.c_int, I64, P, P, I64]
+        _lib = L
+    return _lib
+
+
+def _take(p, n, dtype):
+    arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dtype))),
+                                shape=(max(n, 1),))[:n].copy()
+    lib().orc_free(p)
+    return arr
+
+
+def threads(n: int = 0) -> int:
+    if n > 0:
+        lib().orc_set_threads(n)
+    return lib().orc_max_threads()
+
+
+def build_csr(nv: int, src: np.ndarray, dst: np.ndarray, flags: int = 7) -> Tuple[np.ndarray, np.ndarray]:
+    src = np.ascontiguousarray(src, dtype=np.int32)
+    dst = np.ascontiguousarray(dst, dtype=np.int32)
+    rp, cp, ne = C.c_void_p(), C.c_void_p(), C.c_int64()
+    st = lib().orc_build_csr(nv, src.ctypes.data, dst.ctypes.data, len(src), flags, C.byref(rp),
+                             C.byref(cp), C.byref(ne))
+    if st != 0:
+        raise ValueError(f"oracle CSR build failed ({st})")
+    return _take(rp, nv + 1, np.int64), _take(cp, ne.value, np.int32)
+
+
+def orient(rowptr: np.ndarray, col: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+    nv = len(rowptr) - 1
+    rp, cp, ne = C.c_void_p(), C.c_void_p(), C.c_int64()
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    if lib().orc_orient(nv, rowptr.ctypes.data, col.ctypes.data, C.byref(rp), C.byref(cp),
+                        C.byref(ne)) != 0:
+        raise MemoryError("oracle orientation failed")
+    return _take(rp, nv + 1, np.int64), _take(cp, ne.value, np.int32)
+
+
+def _args(rowptr, col):
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    return len(rowptr) - 1, rowptr, col
+
+
+def count(kind: str, rowptr: np.ndarray, col: np.ndarray, lo: int = 0, hi: int = -1,
+          stride: int = 1) -> int:
+    """kind: tc / clique4 / clique5 (on a DAG) or diamond / cycle4 / tailed (undirected)."""
+    nv, rowptr, col = _args(rowptr, col)
+    hi = nv if hi < 0 else hi
+    L = lib()
+    if kind in ("clique4", "clique5"):
+        md = int(np.max(np.diff(rowptr))) if nv else 0
+        f = L.orc_clique4 if kind == "clique4" else L.orc_clique5
+        return int(f(nv, rowptr.ctypes.data, col.ctypes.data, md, lo, hi, stride))
+    f = {"tc": L.orc_tc, "diamond": L.orc_diamond, "cycle4": L.orc_cycle4,
+         "tailed": L.orc_tailed_triangle}[kind]
+    return int(f(nv, rowptr.ctypes.data, col.ctypes.data, lo, hi, stride))
+
+
+ALGO_KIND = {"tc": 3, "clique4": 4, "clique5": 5, "diamond": 6, "cycle4": 7, "tailed": 8}
+
+
+def algo_bytes(kind: str, rowptr: np.ndarray, col: np.ndarray) -> int:
+    nv, rowptr, col = _args(rowptr, col)
+    md = int(np.max(np.diff(rowptr))) if nv else 0
+    return int(lib().orc_algo_bytes(ALGO_KIND[kind], nv, rowptr.ctypes.data, col.ctypes.data, md))
+
+
+# ------------------------------------------------------ reference binaries (_ref)
+def ref_available(name: str = "tc_omp_base") -> bool:
+    return os.access(os.path.join(REF_DIR, name), os.X_OK)
+
+
+def run_ref(kind: str, prefix: str, threads_: int = 0) -> Tuple[int, float]:
+    """Runs a reference binary on <prefix>.* graph files; returns (count, seconds)."""
+    env = dict(os.environ)
+    if threads_ > 0:
+        env["OMP_NUM_THREADS"] = str(threads_)
+    if kind == "tc":
+        cmd, pat = [os.path.join(REF_DIR, "tc_omp_base"), prefix], r"total_num_triangles = (\d+)"
+    elif kind in ("clique4", "clique5"):
+        cmd = [os.path.join(REF_DIR, "clique_omp_base"), prefix, kind[-1]]
+        pat = r"num_\d-cliques = (\d+)"
+    else:
+        name = {"diamond": "diamond", "cycle4": "rectangle", "tailed": "tailedtriangle"}[kind]
+        cmd, pat = [os.path.join(REF_DIR, "count_omp_base"), prefix, name], r"total_num = (\d+)"
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd[0]} failed: {r.stderr[-500:]}")
+    m = re.search(pat, r.stdout)
+    t = re.search(r"runtime[^=]*= ([0-9.eE+-]+)", r.stdout)
+    if not m:
+        raise RuntimeError("unexpected reference output:\n" + r.stdout[-800:])
+    return int(m.group(1)), float(t.group(1)) if t else float("nan")
+
+
+def write_graph(prefix: str, rowptr: np.ndarray, col: np.ndarray) -> None:
+    """Writes <prefix>.meta.txt/.vertex.bin/.edge.bin (scripts/graph_format_conversion.py:47-80)."""
+    nv = len(rowptr) - 1
+    maxd = int(np.max(np.diff(rowptr))) if nv else 0
+    with open(prefix + ".meta.txt", "w") as f:
+        f.write(f"{nv}\n{len(col)}\n4 8 1 2\n{maxd}\n0\n0\n0\n")
+    np.ascontiguousarray(rowptr, dtype="<i8").tofile(prefix + ".vertex.bin")
+    np.ascontiguousarray(col, dtype="<i4").tofile(prefix + ".edge.bin")
+
+
+def read_graph(prefix: str) -> Tuple[np.ndarray, np.ndarray]:
+    with open(prefix + ".meta.txt") as f:
+        nv, ne = int(f.readline()), int(f.readline())
+    rowptr = np.fromfile(prefix + ".vertex.bin", dtype="<i8", count=nv + 1)
+    col = np.fromfile(prefix + ".edge.bin", dtype="<i4", count=ne)
+    return rowptr, col

@@ -1,0 +1,386 @@
+/*
+ * oracle.c - CPU restatement of X-GMiner's (G2Miner's) OpenMP counting path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU engine: the tests,
+ * the smoke check and the CPU-baseline leg of bench.py load it.  The engine itself
+ * never links, loads or calls it, and nothing here is a fallback for the engine.
+ *
+ * Every function restates one function of the reference (cited file:line, paths
+ * inside the zlwu92/X-GMiner tree).  Parity of this restatement is pinned two ways
+ * by the tests: against the reference's published known answers on citeseer
+ * (codes/GraphMiner/src/triangle/README.md:53, src/motif/README.md:57,
+ * src/count/README.md:41) and against the reference's own OpenMP binaries built
+ * from source by oracle/build_ref.sh, run on the same graph files.
+ *
+ * Types follow codes/GraphMiner/include/common.h:36-40: vidType = int32,
+ * eidType = int64, counts uint64.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef int32_t vid_t;
+typedef int64_t eid_t;
+
+/* ---------------------------------------------------------------- threads */
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int orc_has_openmp(void) {
+#ifdef _OPENMP
+  return 1;
+#else
+  return 0;
+#endif
+}
+void orc_free(void* p) { free(p); }
+
+/* ------------------------------------------------------- set primitives */
+/* VertexSet::get_intersect_num, codes/GraphMiner/include/VertexSet.h:65-75 (merge). */
+static inline uint64_t isect_num(const vid_t* a, eid_t na, const vid_t* b, eid_t nb) {
+  uint64_t num = 0;
+  eid_t l = 0, r = 0;
+  while (l < na && r < nb) {
+    vid_t x = a[l], y = b[r];
+    if (x <= y) l++;
+    if (y <= x) r++;
+    if (x == y) num++;
+  }
+  return num;
+}
+/* VertexSet::intersect_ns (bounded count of common ids < up), VertexSet.h:110-123. */
+static inline uint64_t isect_num_bound(const vid_t* a, eid_t na, const vid_t* b, eid_t nb,
+                                       vid_t up) {
+  uint64_t num = 0;
+  eid_t l = 0, r = 0;
+  while (l < na && r < nb) {
+    vid_t x = a[l], y = b[r];
+    if (x >= up || y >= up) break;
+    if (x <= y) l++;
+    if (y <= x) r++;
+    if (x == y) num++;
+  }
+  return num;
+}
+/* VertexSet::operator& (set-producing merge), VertexSet.h:53-64. */
+static inline eid_t isect_set(const vid_t* a, eid_t na, const vid_t* b, eid_t nb, vid_t* out) {
+  eid_t n = 0, l = 0, r = 0;
+  while (l < na && r < nb) {
+    vid_t x = a[l], y = b[r];
+    if (x <= y) l++;
+    if (y <= x) r++;
+    if (x == y) out[n++] = x;
+  }
+  return n;
+}
+
+/* ------------------------------------------------------------ CSR build */
+/* LSD radix sort of 64-bit keys (16-bit digits) over the low `bits` bits. */
+static void radix_sort_u64(uint64_t* keys, eid_t n, int bits) {
+  uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1));
+  eid_t* cnt = (eid_t*)malloc(sizeof(eid_t) * 65536);
+  uint64_t *a = keys, *b = tmp;
+  for (int shift = 0; shift < bits; shift += 16) {
+    memset(cnt, 0, sizeof(eid_t) * 65536);
+    for (eid_t i = 0; i < n; i++) cnt[(a[i] >> shift) & 0xFFFF]++;
+    eid_t s = 0;
+    for (int d = 0; d < 65536; d++) { eid_t c = cnt[d]; cnt[d] = s; s += c; }
+    for (eid_t i = 0; i < n; i++) b[cnt[(a[i] >> shift) & 0xFFFF]++] = a[i];
+    uint64_t* t = a; a = b; b = t;
+  }
+  if (a != keys) memcpy(keys, a, sizeof(uint64_t) * (size_t)n);
+  free(tmp);
+  free(cnt);
+}
+
+/* Symmetrise + sort (scripts/graph_format_conversion.py:20-44), plus dedupe and
+ * self-loop removal (flags bit 2 / bit 4 as in xgm.h); bit 1 adds reverse edges.
+ * Returns 0 on success; *rowptr (nv+1) and *col are malloc'd. */
+int orc_build_csr(int64_t nv, const int32_t* src, const int32_t* dst, int64_t m, int flags,
+                  int64_t** rowptr_out, int32_t** col_out, int64_t* ne_out) {
+  const int sym = flags & 1, dedup = flags & 2, noself = flags & 4;
+  eid_t cap = sym ? 2 * m : m;
+  uint64_t* keys = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(cap > 0 ? cap : 1));
+  if (!keys) return 3;
+  eid_t n = 0;
+  for (eid_t i = 0; i < m; i++) {
+    uint32_t u = (uint32_t)src[i], v = (uint32_t)dst[i];
+    if ((int64_t)u >= nv || (int64_t)v >= nv) { free(keys); return 1; }
+    if (noself && u == v) continue;
+    keys[n++] = ((uint64_t)u << 32) | v;
+    if (sym) keys[n++] = ((uint64_t)v << 32) | u;
+  }
+  int vb = 1;
+  while (((int64_t)1 << vb) < nv) vb++;
+  /* the key (u<<32|v) sorts by u then v; sort on the used bits of both halves */
+  for (eid_t i = 0; i < n; i++) keys[i] = ((keys[i] >> 32) << vb) | (keys[i] & 0xFFFFFFFFull);
+  radix_sort_u64(keys, n, 2 * vb);
+  eid_t w = 0;
+  for (eid_t i = 0; i < n; i++) {
+    if (dedup && w > 0 && keys[w - 1] == keys[i]) continue;
+    keys[w++] = keys[i];
+  }
+  int64_t* rowptr = (int64_t*)calloc((size_t)nv + 1, sizeof(int64_t));
+  int32_t* col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(w > 0 ? w : 1));
+  const uint64_t vmask = (((uint64_t)1) << vb) - 1;
+  for (eid_t i = 0; i < w; i++) {
+    rowptr[(keys[i] >> vb) + 1]++;
+    col[i] = (int32_t)(keys[i] & vmask);
+  }
+  for (int64_t v = 0; v < nv; v++) rowptr[v + 1] += rowptr[v];
+  free(keys);
+  *rowptr_out = rowptr;
+  *col_out = col;
+  *ne_out = w;
+  return 0;
+}
+
+/* Graph::orientation, codes/GraphMiner/src/common/graph.cc:233-275 (identical to
+ * xgminer/src/graph_v2.cpp:243-289): keep src->dst iff deg(dst) > deg(src), or the
+ * degrees tie and dst > src; order within each row is preserved. */
+int orc_orient(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t** dag_rowptr_out,
+               int32_t** dag_col_out, int64_t* dag_ne_out) {
+  int64_t* nd = (int64_t*)calloc((size_t)nv + 1, sizeof(int64_t));
+  if (!nd) return 3;
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < nv; s++) {
+    int64_t ds = rowptr[s + 1] - rowptr[s], c = 0;
+    for (int64_t e = rowptr[s]; e < rowptr[s + 1]; e++) {
+      int32_t d = col[e];
+      int64_t dd = rowptr[d + 1] - rowptr[d];
+      if (dd > ds || (dd == ds && d > s)) c++;
+    }
+    nd[s + 1] = c;
+  }
+  for (int64_t v = 0; v < nv; v++) nd[v + 1] += nd[v];
+  int32_t* dc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nd[nv] > 0 ? nd[nv] : 1));
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < nv; s++) {
+    int64_t ds = rowptr[s + 1] - rowptr[s], o = nd[s];
+    for (int64_t e = rowptr[s]; e < rowptr[s + 1]; e++) {
+      int32_t d = col[e];
+      int64_t dd = rowptr[d + 1] - rowptr[d];
+      if (dd > ds || (dd == ds && d > s)) dc[o++] = d;
+    }
+  }
+  *dag_rowptr_out = nd;
+  *dag_col_out = dc;
+  *dag_ne_out = nd[nv];
+  return 0;
+}
+
+/* ------------------------------------------------------------- counting */
+/* All counting functions take the outer-loop range [lo, hi) with `stride`, so the
+ * CPU baseline can time a bounded sample; (0, V, 1) is the full count. */
+#define ROW(v) (col + rowptr[(v)]), (rowptr[(v) + 1] - rowptr[(v)])
+
+/* TCSolver, codes/GraphMiner/src/triangle/omp_base.cc:5-26 (on the DAG). */
+uint64_t orc_tc(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t lo, int64_t hi,
+                int64_t stride) {
+  (void)nv;
+  uint64_t counter = 0;
+#pragma omp parallel for reduction(+ : counter) schedule(dynamic, 1)
+  for (int64_t u = lo; u < hi; u += stride) {
+    for (int64_t e = rowptr[u]; e < rowptr[u + 1]; e++) {
+      int32_t v = col[e];
+      counter += isect_num(ROW(u), ROW(v));
+    }
+  }
+  return counter;
+}
+
+/* automine_4clique, codes/GraphMiner/src/clique/cpu_kernels/clique_base.h:53-68. */
+uint64_t orc_clique4(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t max_deg,
+                     int64_t lo, int64_t hi, int64_t stride) {
+  (void)nv;
+  uint64_t counter = 0;
+#pragma omp parallel reduction(+ : counter)
+  {
+    vid_t* y0y1 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t v0 = lo; v0 < hi; v0 += stride) {
+      uint64_t local = 0;
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+        int32_t v1 = col[e];
+        eid_t n = isect_set(ROW(v0), ROW(v1), y0y1);
+        for (eid_t i = 0; i < n; i++) local += isect_num(y0y1, n, ROW(y0y1[i]));
+      }
+      counter += local;
+    }
+    free(y0y1);
+  }
+  return counter;
+}
+
+/* automine_5clique, codes/GraphMiner/src/clique/cpu_kernels/automine_omp.h:138-157. */
+uint64_t orc_clique5(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t max_deg,
+                     int64_t lo, int64_t hi, int64_t stride) {
+  (void)nv;
+  uint64_t counter = 0;
+#pragma omp parallel reduction(+ : counter)
+  {
+    vid_t* y1y2 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
+    vid_t* y1y2y3 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t v1 = lo; v1 < hi; v1 += stride) {
+      uint64_t local = 0;
+      for (int64_t e = rowptr[v1]; e < rowptr[v1 + 1]; e++) {
+        int32_t v2 = col[e];
+        eid_t n12 = isect_set(ROW(v1), ROW(v2), y1y2);
+        for (eid_t i = 0; i < n12; i++) {
+          eid_t n123 = isect_set(y1y2, n12, ROW(y1y2[i]), y1y2y3);
+          for (eid_t j = 0; j < n123; j++) local += isect_num(y1y2y3, n123, ROW(y1y2y3[j]));
+        }
+      }
+      counter += local;
+    }
+    free(y1y2);
+    free(y1y2y3);
+  }
+  return counter;
+}
+
+/* Edge-induced diamond, codes/GraphMiner/src/count/cpu_kernels/diamond.h:1-8
+ * (undirected graph): sum over edges v1 < v0 of C(|N(v0) & N(v1)|, 2). */
+uint64_t orc_diamond(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t lo,
+                     int64_t hi, int64_t stride) {
+  (void)nv;
+  uint64_t counter = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : counter)
+  for (int64_t v0 = lo; v0 < hi; v0 += stride) {
+    for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+      int32_t v1 = col[e];
+      if (v1 >= v0) break;
+      uint64_t n = isect_num(ROW(v0), ROW(v1));
+      if (n > 1) counter += n * (n - 1) / 2;
+    }
+  }
+  return counter;
+}
+
+/* Edge-induced 4-cycle, codes/GraphMiner/src/count/cpu_kernels/rectangle.h:1-46:
+ * for each v0, wedges v0-v1-v2 with v1 < v0 and v2 < v0 are grouped by v2 and every
+ * group of n wedges closes C(n,2) cycles.  The reference groups by sorting the wedge
+ * list; this restatement groups with a dense per-thread counter (same groups). */
+uint64_t orc_cycle4(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t lo,
+                    int64_t hi, int64_t stride) {
+  uint64_t counter = 0;
+#pragma omp parallel reduction(+ : counter)
+  {
+    uint32_t* cnt = (uint32_t*)calloc((size_t)nv, sizeof(uint32_t));
+    vid_t* touched = (vid_t*)malloc(sizeof(vid_t) * (size_t)(nv > 0 ? nv : 1));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t v0 = lo; v0 < hi; v0 += stride) {
+      int64_t nt = 0;
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+        int32_t v1 = col[e];
+        if (v1 >= v0) break;
+        for (int64_t f = rowptr[v1]; f < rowptr[v1 + 1]; f++) {
+          int32_t v2 = col[f];
+          if (v2 >= v0) break;
+          if (cnt[v2]++ == 0) touched[nt++] = v2;
+        }
+      }
+      for (int64_t t = 0; t < nt; t++) {
+        uint64_t n = cnt[touched[t]];
+        counter += n * (n - 1) / 2;
+        cnt[touched[t]] = 0;
+      }
+    }
+    free(cnt);
+    free(touched);
+  }
+  return counter;
+}
+
+/* Edge-induced tailed triangle, codes/GraphMiner/src/count/cpu_kernels/tailedtriangle.h:1-12:
+ * for each v0 of degree > 2, t(v0) = sum over v1 in N(v0) of |N(v0) & N(v1)| bounded
+ * by v1, and the count grows by t(v0) * (deg(v0) - 2). */
+uint64_t orc_tailed_triangle(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t lo,
+                             int64_t hi, int64_t stride) {
+  (void)nv;
+  uint64_t counter = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : counter)
+  for (int64_t v0 = lo; v0 < hi; v0 += stride) {
+    int64_t deg = rowptr[v0 + 1] - rowptr[v0];
+    if (deg > 2) {
+      uint64_t tri = 0;
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+        int32_t v1 = col[e];
+        tri += isect_num_bound(ROW(v0), ROW(v1), v1);
+      }
+      counter += tri * (uint64_t)(deg - 2);
+    }
+  }
+  return counter;
+}
+
+/* ----------------------------------------------------- algorithmic bytes */
+/* Bytes of graph-resident adjacency data each plan reads: 4 B per int32 list element
+ * plus 8 B per task record.  The engine reports the same quantity as its roofline
+ * numerator; these loops are the checker for it.  kind: 3 = TC, 4 = 4-clique,
+ * 5 = 5-clique on the DAG; 6 = diamond, 7 = 4-cycle, 8 = tailed triangle on the
+ * undirected graph. */
+uint64_t orc_algo_bytes(int kind, int64_t nv, const int64_t* rowptr, const int32_t* col,
+                        int64_t max_deg) {
+  uint64_t bytes = 0;
+#define DEG(v) ((uint64_t)(rowptr[(v) + 1] - rowptr[(v)]))
+#pragma omp parallel reduction(+ : bytes)
+  {
+    vid_t* w = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
+    vid_t* w2 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t v0 = 0; v0 < nv; v0++) {
+      if (kind == 8) {
+        if (DEG(v0) > 2)
+          for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) bytes += 4 * (DEG(v0) + DEG(col[e]));
+        continue;
+      }
+      if (kind == 7) {
+        bytes += 4 * DEG(v0);
+        for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+          int32_t v1 = col[e];
+          if (v1 >= v0) break;
+          for (int64_t f = rowptr[v1]; f < rowptr[v1 + 1]; f++) {
+            if (col[f] >= v0) break;
+            bytes += 4;
+          }
+        }
+        continue;
+      }
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+        int32_t v1 = col[e];
+        if (kind == 6 && v1 >= v0) break;
+        bytes += 8 + 4 * (DEG(v0) + DEG(v1));
+        if (kind == 4 || kind == 5) {
+          eid_t n = isect_set(ROW(v0), ROW(v1), w);
+          for (eid_t i = 0; i < n; i++) {
+            bytes += 4 * DEG(w[i]);
+            if (kind == 5) {
+              eid_t n2 = isect_set(w, n, ROW(w[i]), w2);
+              for (eid_t j = 0; j < n2; j++) bytes += 4 * DEG(w2[j]);
+            }
+          }
+        }
+      }
+    }
+    free(w);
+    free(w2);
+  }
+#undef DEG
+  return bytes;
+}

@@ -1,0 +1,90 @@
+"""Generates tests/golden/golden_counts.json.
+
+For each seeded synthetic graph below, the edge samples come from the engine's host
+generators (integer-only, identical on x86-64 and aarch64), the CSR from the oracle's
+CSR build, and every count from the reference's OWN OpenMP binaries (oracle/_ref,
+built from the reference sources by oracle/build_ref.sh) run on the graph files.  The
+oracle restatement is cross-checked on the way.  A sha256 of the CSR bytes lets the
+GPU tests confirm they regenerated the same graph.
+
+Run from the repository root (needs the reference tree for oracle/_ref):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import importlib
+import json
+import os
+import sys
+import tempfile
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+xgm = importlib.import_module("x-gminer_gb300")
+
+CASES = [
+    {"name": "rmat_s10_ef16", "gen": "rmat", "args": [10, 16], "seed": 1},
+    {"name": "rmat_s12_ef8", "gen": "rmat", "args": [12, 8], "seed": 3},
+    {"name": "rmat_s14_ef16", "gen": "rmat", "args": [14, 16], "seed": 2},
+    {"name": "er_n4096_m40000", "gen": "er", "args": [4096, 40000], "seed": 3},
+    {"name": "ba_n3000_m5", "gen": "ba", "args": [3000, 5], "seed": 4},
+    {"name": "ba_n200_m8", "gen": "ba", "args": [200, 8], "seed": 9},
+]
+KINDS = ["tc", "clique4", "clique5", "diamond", "cycle4", "tailed"]
+
+
+def samples(case):
+    g, a, seed = case["gen"], case["args"], case["seed"]
+    if g == "rmat":
+        return xgm.gen_rmat(a[0], a[1], seed=seed)
+    if g == "er":
+        return xgm.gen_er(a[0], a[1], seed=seed)
+    if g == "ba":
+        return xgm.gen_ba(a[0], a[1], seed=seed)
+    raise ValueError(g)
+
+
+def csr_digest(rowptr, col) -> str:
+    h = hashlib.sha256()
+    h.update(rowptr.astype("<i8").tobytes())
+    h.update(col.astype("<i4").tobytes())
+    return h.hexdigest()
+
+
+def main() -> None:
+    if not oracle.build_ref():
+        raise SystemExit("reference binaries unavailable (needs the reference tree)")
+    out = []
+    tmp = tempfile.mkdtemp()
+    for case in CASES:
+        nv, src, dst = samples(case)
+        rowptr, col = oracle.build_csr(nv, src, dst)
+        drow, dcol = oracle.orient(rowptr, col)
+        prefix = os.path.join(tmp, case["name"])
+        oracle.write_graph(prefix, rowptr, col)
+        counts = {}
+        for k in KINDS:
+            ref, _ = oracle.run_ref(k, prefix)
+            mine = oracle.count(k, drow, dcol) if k in ("tc", "clique4", "clique5") else \
+                oracle.count(k, rowptr, col)
+            if ref != mine:
+                raise SystemExit(f"{case['name']} {k}: reference {ref} != oracle {mine}")
+            counts[k] = ref
+        rec = dict(case)
+        rec.update({"V": int(nv), "E": int(len(col)), "E_dag": int(len(dcol)),
+                    "csr_sha256": csr_digest(rowptr, col), "counts": counts,
+                    "source": "oracle/_ref reference OpenMP binaries"})
+        out.append(rec)
+        print(case["name"], counts)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_counts.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,93 @@
+"""The C-ABI library: loads without a GPU, exports what include/xgm.h declares."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "xgm.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(xgm_\w+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(xgm):
+    names = header_functions()
+    assert len(names) >= 30
+    so = ctypes.CDLL(xgm.LIB_PATH)
+    for n in names:
+        assert hasattr(so, n), n
+    assert sorted(xgm.EXPORTED) == names
+
+
+def test_generators_deterministic(xgm):
+    a = xgm.gen_rmat(12, 8, seed=11)
+    b = xgm.gen_rmat(12, 8, seed=11)
+    c = xgm.gen_rmat(12, 8, seed=12)
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert not np.array_equal(a[1], c[1])
+    assert a[1].min() >= 0 and a[1].max() < 4096
+    n, s, d = xgm.gen_er(1000, 5000, seed=3)
+    assert s.max() < 1000 and d.max() < 1000
+    n, s, d = xgm.gen_ba(500, 4, seed=3)
+    assert len(s) == 4 * (500 - 4)
+    assert np.all(s > d)  # each new vertex attaches to earlier ones
+    vo, eo, s, d = xgm.gen_ba_batch(16, 100, 300, 3, 8, seed=5)
+    for g in range(16):
+        lo, hi = vo[g], vo[g + 1]
+        es, ed = s[eo[g]:eo[g + 1]], d[eo[g]:eo[g + 1]]
+        assert es.min() >= lo and es.max() < hi and ed.min() >= lo and ed.max() < hi
+
+
+def test_chung_lu_degrees(xgm):
+    n, s, d = xgm.gen_chung_lu(1 << 14, 2.1, 2000.0, 16.0, seed=4)
+    deg = np.bincount(np.concatenate([s, d]), minlength=n)
+    assert abs(deg.mean() - 16.0) < 0.5
+    assert deg.max() > 1000  # power-law head near w_max
+
+
+def test_bad_generator_arguments(xgm):
+    lib = xgm.lib()
+    assert lib.xgm_gen_rmat(0, 16, 0.57, 0.19, 0.19, 1, None, None) == -1
+    assert lib.xgm_gen_rmat(10, 16, 0.7, 0.3, 0.3, 1, None, None) == -1
+    assert lib.xgm_gen_ba(3, 5, 1, None, None) == -1
+
+
+def test_status_strings(xgm):
+    for s in range(10):
+        assert xgm.lib().xgm_status_string(s)
+
+
+def test_no_device_is_an_error_not_a_fallback(xgm):
+    import subprocess
+    if subprocess.run(["sh", "-c", "command -v nvidia-smi && nvidia-smi -L"],
+                      capture_output=True).returncode == 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(xgm.XgmError) as e:
+        xgm.Context(0)
+    assert e.value.status == xgm.ERR_NO_DEVICE
+
+
+def test_mlp_reference_gradient_is_consistent():
+    import oracle.mlp_ref as M
+    rng = np.random.default_rng(0)
+    p = (rng.standard_normal(M.NPARAM) * 0.3).astype(np.float16).astype(np.float64)
+    X = rng.random((64, M.F))
+    y = rng.random(64) * 4
+    loss, g = M.loss_grad(p, X, y)
+    eps = 1e-6
+    for i in rng.choice(M.NPARAM, 25, replace=False):
+        q = p.copy()
+        q[i] += eps
+        w1, b1, w2, b2 = [a.astype(np.float64) for a in M.unpack(q)]
+        # finite difference in float64 without fp16 rounding of the perturbed weight
+        z = X @ (q[: M.H * M.F].reshape(M.H, M.F)).T + q[M.H * M.F: M.H * M.F + M.H]
+        yh = np.maximum(z, 0) @ q[M.H * M.F + M.H: M.H * M.F + 2 * M.H] + q[-1]
+        lp = np.mean((yh - y) ** 2)
+        assert abs((lp - loss) / eps - g[i]) < 1e-3 * max(1.0, abs(g[i]))

@@ -1,0 +1,78 @@
+// Internal definitions behind the C ABI.
+#pragma once
+#include <string>
+
+#include "clique.cuh"
+#include "graph.cuh"
+#include "sched.cuh"
+
+namespace xgm {
+
+// Small device-side scalars of one call, zeroed by one memset and read back by one copy.
+struct Scalars {
+  unsigned long long count;
+  unsigned long long aux;
+  uint32_t err;
+  uint32_t pad;
+  QueueHeads q;
+  unsigned long long c4heads[2];
+  int64_t n[4];  // task list sizes, copied back for the stats
+};
+
+struct Model;  // learned cost model (learned.cu)
+
+}  // namespace xgm
+
+struct xgm_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  xgm::Scalars* d_sc = nullptr;
+  xgm::Scalars* h_sc = nullptr;  // pinned
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  xgm::TaskBuf tb;
+  // motif buffers (grown on demand)
+  unsigned long long* vpart = nullptr;
+  int64_t vpart_cap = 0;
+  unsigned* epart = nullptr;
+  int64_t epart_cap = 0;
+  uint32_t* c4_scratch = nullptr;
+  int64_t c4_scratch_cap = 0;
+  long long* wedges = nullptr;
+  uint8_t* c4_flag_large = nullptr;
+  uint8_t* c4_flag_small = nullptr;
+  int64_t* c4_pos = nullptr;
+  int32_t* c4_large = nullptr;
+  int32_t* c4_small = nullptr;
+  int64_t* c4_n = nullptr;
+  int64_t c4_vcap = 0;
+  int clique_grid = 0;
+};
+
+struct xgm_graph {
+  xgm_ctx* ctx = nullptr;
+  xgm::DevGraph g;
+};
+
+struct xgm_plan {
+  int pattern = 0;
+};
+
+namespace xgm {
+
+xgm_status finish_status(xgm_ctx* ctx, xgm_status st);
+xgm_status check_device_flag(xgm_ctx* ctx, uint32_t flag);
+xgm_status ctx_sync_scalars(xgm_ctx* ctx);
+
+// count.cu
+xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
+                          uint64_t* out, xgm_stats& st);
+xgm_status algo_bytes_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, uint64_t* out);
+xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
+                         int* n_kernels);
+void motif_buffers_free(xgm_ctx* ctx);
+int match_pattern(const xgm_plan_desc* d);  // builtin id, 0 unsupported, -1 malformed
+int pattern_from_name(const char* name);
+
+}  // namespace xgm

@@ -1,0 +1,577 @@
+// Triangle and k-clique counting on the degree-oriented DAG, hand-written for sm_103a.
+//
+// Reference kernels this replaces (same counts, different schedule):
+//  - warp_edge (TC): codes/GraphMiner/src/triangle/gpu_kernels/bs_warp_edge.cuh:1-20
+//  - clique4_warp_edge / clique5_warp_edge:
+//      xgminer/src/gpu_kernels/glumin/gpu_GM_LUT_kernels/GM_kernels/clique{4,5}_warp_edge.cuh
+//  - LUT forms clique4_warp_vertex_subgraph / clique5_warp_edge_subgraph
+//      (GM_LUT_kernels/clique4_warp_vertex_subgraph.cuh:3-42,
+//       clique5_warp_edge_subgraph.cuh:3-51), which build a per-warp bitmap of the
+//      candidate set in global memory (BinaryEncode, binary_encode.h:8-515).
+//  - persistent atomic edge queue: clique5_warp_edge_taskallocate.cuh:76-79.
+//
+// Scheme.  Vertices are degree ranks, so N+(v) is sorted and every member is > v.  A
+// vertex task v0 takes its local set S = N+(v0) (|S| = s) and builds in shared memory
+// the bitmap adjacency of the DAG induced on S: row i holds bit j iff S[j] in N+(S[i]),
+// which implies j > i, so row i keeps only words floor(i/32)..W-1 (triangular layout).
+// Row construction streams each N+(S[i]) once, coalesced, and looks members up in an
+// open-addressing hash of S.  Then a k-clique rooted at v0 is a (k-1)-clique of the
+// local DAG:
+//    k = 3: number of local edges (no bitmap needed)
+//    k = 4: sum_i sum_{j in row i} popc(row_i & row_j)
+//    k = 5: sum_i sum_{j in row i} sum_{l in row_i & row_j} popc(row_i & row_j & row_l)
+// Hub vertices (s above the CTA capacity) are split into edge sub-tasks (v0, v1) whose
+// local set is N+(v0) & N+(v1) and which count (k-2)-cliques of it the same way.
+// One persistent kernel runs three queues in order: hub edge sub-tasks, CTA vertex
+// tasks, then warp vertex tasks (s <= 32, one-word rows), each fed by an atomic head.
+#include "clique.cuh"
+
+namespace xgm {
+
+namespace {
+
+// ---------------------------------------------------------------- smem layout
+// CTA region (bytes): lb[kCtaCap] i64 | S[kCtaCap] i32 | pre[kCtaCap+8] i32 |
+//                     hkey[kHashSize] i32 | hval[kHashSize] u16 | cnt[kCtaCap] u32 |
+//                     rows[tri_words(kCtaCap)] u32 | misc[16] i64
+constexpr int kOffLb = 0;
+constexpr int kOffS = kOffLb + 8 * kCtaCap;
+constexpr int kOffPre = kOffS + 4 * kCtaCap;
+constexpr int kOffHkey = kOffPre + 4 * (kCtaCap + 8);
+constexpr int kOffHval = kOffHkey + 4 * kHashSize;
+constexpr int kOffCnt = kOffHval + 2 * kHashSize;
+constexpr int kOffRows = kOffCnt + 4 * kCtaCap;
+constexpr int kRowsWords = 16896;  // tri_words(1024)
+constexpr int kOffMisc = kOffRows + 4 * kRowsWords;
+constexpr int kCtaSmem = kOffMisc + 8 * 16;
+
+// Warp region: one per warp, aliased over the CTA region once the CTA queues drain.
+struct WarpSmem {
+  long long lb[kWarpCap];
+  int32_t S[kWarpCap];
+  int32_t pre[kWarpCap + 2];
+  uint32_t rows[kWarpCap];
+  uint32_t cnt[kWarpCap];
+};
+static_assert(sizeof(WarpSmem) * kCtaWarps <= kCtaSmem, "warp region must fit");
+
+__device__ __forceinline__ uint32_t hash_slot(int32_t x) {
+  return ((uint32_t)x * 2654435761u) >> (32 - 11);  // kHashSize = 2^11
+}
+
+__device__ __forceinline__ int hash_find(const int32_t* hkey, const uint16_t* hval, int32_t x) {
+  uint32_t slot = hash_slot(x);
+#pragma unroll 1
+  for (int probe = 0; probe < kHashSize; ++probe) {
+    int32_t k = hkey[slot];
+    if (k == x) return hval[slot];
+    if (k == -1) return -1;
+    slot = (slot + 1) & (kHashSize - 1);
+  }
+  return -1;
+}
+
+// Block-wide exclusive scan of values v[i], i < n <= kCtaCap, into pre[0..n]; CTA-wide.
+__device__ void cta_scan_lengths(int32_t* pre, int n, int32_t* warp_tot) {
+  // each thread owns items [tid*2, tid*2+1] (kCtaCap = 2 * kCtaThreads)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int a = 2 * tid < n ? pre[2 * tid] : 0;
+  int b = 2 * tid + 1 < n ? pre[2 * tid + 1] : 0;
+  int s = a + b, inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < kCtaWarps ? warp_tot[lane] : 0, wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(kFull, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kCtaWarps) warp_tot[lane] = wi - w;
+  }
+  __syncthreads();
+  int ex = warp_tot[warp] + inc - s;
+  if (2 * tid < n) pre[2 * tid] = ex;
+  if (2 * tid + 1 < n) pre[2 * tid + 1] = ex + a;
+  if (2 * tid + 1 == n - 1 || 2 * tid == n - 1) pre[n] = ex + s;
+  __syncthreads();
+}
+
+// Kernel modes: plain count; triangle participation (per-vertex / per-edge triangle
+// counts for the motif plans); count weighted by the out-degree of each clique's
+// highest-ranked vertex (the plan's algorithmic-bytes term).
+enum { kModeCount = 0, kModePart = 1, kModeWeight = 2 };
+
+// Count of (q)-cliques in the local DAG held by the CTA (q >= 3 uses the bitmap).  WGT
+// (Q == 3 only) weights each clique by d+ of its top member, d+(S[l]) = pre[l+1]-pre[l].
+template <int Q, bool WGT>
+__device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, const int32_t* pre) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int W = (s + 31) >> 5;
+  uint64_t acc = 0;
+  for (int i = warp; i < s; i += kCtaWarps) {
+    const int qi = i >> 5, nwi = W - qi;
+    const uint32_t* Ri = rows + tri_row_off(i, W);
+    const uint32_t wi = lane < nwi ? Ri[lane] : 0u;
+    const int w = qi + lane;
+    unsigned nz = __ballot_sync(kFull, wi != 0u);
+    while (nz) {
+      const int src = __ffs(nz) - 1;
+      nz &= nz - 1;
+      uint32_t bits = __shfl_sync(kFull, wi, src);
+      while (bits) {
+        const int j = ((qi + src) << 5) + __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int qj = j >> 5;
+        const uint32_t* Rj = rows + tri_row_off(j, W);
+        const uint32_t m = (lane < nwi && w >= qj) ? (wi & Rj[w - qj]) : 0u;
+        if (Q == 3) {
+          if (WGT) {
+            uint32_t b3 = m;
+            while (b3) {
+              const int l = (w << 5) + __ffs(b3) - 1;
+              b3 &= b3 - 1;
+              acc += (uint64_t)(pre[l + 1] - pre[l]);
+            }
+          } else {
+            acc += __popc(m);
+          }
+        } else {
+          unsigned nz2 = __ballot_sync(kFull, m != 0u);
+          while (nz2) {
+            const int src2 = __ffs(nz2) - 1;
+            nz2 &= nz2 - 1;
+            uint32_t bits2 = __shfl_sync(kFull, m, src2);
+            while (bits2) {
+              const int l = ((qi + src2) << 5) + __ffs(bits2) - 1;
+              bits2 &= bits2 - 1;
+              const int ql = l >> 5;
+              const uint32_t* Rl = rows + tri_row_off(l, W);
+              if (w >= ql && m) acc += __popc(m & Rl[w - ql]);
+            }
+          }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// Participation counters of the triangle-participation mode.
+struct Part {
+  unsigned long long* v;  // per vertex (rank ids)
+  unsigned* e;            // per rank-space col entry
+};
+
+// The CTA has S[0..s) (sorted, local set) in shared memory.  Counts the Q-cliques of the
+// DAG induced on S, Q = 1..4.  PART (Q == 2 only, S = N+(root) starting at col entry
+// sbase): every local edge (i, j) is the triangle (root, S[i], S[j]); it is credited to
+// vertices S[i], S[j] and edges (root,S[i]), (root,S[j]), (S[i],S[j]).  The root's own
+// credit is the returned count.
+template <int Q, int MODE>
+__device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long long sbase) {
+  constexpr bool PART = MODE == kModePart;
+  constexpr bool WGT = MODE == kModeWeight;
+  int32_t* S = (int32_t*)(sm + kOffS);
+  if (Q == 1) {
+    if (!WGT) return (uint64_t)s;  // same value in every thread
+    uint64_t a = 0;                // per-thread partial sums
+    for (int i = threadIdx.x; i < s; i += kCtaThreads) {
+      const longlong2 d = ldg_ll2(g.dptr + S[i]);
+      a += (uint64_t)(d.y - d.x);
+    }
+    return a;
+  }
+  long long* lb = (long long*)(sm + kOffLb);
+  int32_t* pre = (int32_t*)(sm + kOffPre);
+  int32_t* hkey = (int32_t*)(sm + kOffHkey);
+  uint16_t* hval = (uint16_t*)(sm + kOffHval);
+  uint32_t* cnt = (uint32_t*)(sm + kOffCnt);
+  uint32_t* rows = (uint32_t*)(sm + kOffRows);
+  int32_t* wtot = (int32_t*)(sm + kOffMisc);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int W = (s + 31) >> 5;
+
+  for (int h = tid; h < kHashSize; h += kCtaThreads) hkey[h] = -1;
+  if (Q >= 3)
+    for (int x = tid; x < tri_words(s); x += kCtaThreads) rows[x] = 0u;
+  if (PART)
+    for (int i = tid; i < s; i += kCtaThreads) cnt[i] = 0u;
+  for (int i = tid; i < s; i += kCtaThreads) {
+    longlong2 d = ldg_ll2(g.dptr + S[i]);
+    lb[i] = d.x;
+    pre[i] = (int32_t)(d.y - d.x);
+  }
+  __syncthreads();
+  for (int i = tid; i < s; i += kCtaThreads) {
+    const int32_t x = S[i];
+    uint32_t slot = hash_slot(x);
+    while (atomicCAS(&hkey[slot], -1, x) != -1) slot = (slot + 1) & (kHashSize - 1);
+    hval[slot] = (uint16_t)i;
+  }
+  cta_scan_lengths(pre, s, wtot);  // ends with __syncthreads
+  const int total = pre[s];
+  const int32_t smax = S[s - 1];
+  uint64_t acc = 0;
+  // Flattened walk over all (i, element) pairs: warp chunks of 256 consecutive
+  // elements, lanes contiguous within a chunk so row reads are coalesced.
+  for (int c = warp; c * 256 < total; c += kCtaWarps) {
+    int k = c * 256 + lane;
+    int i;
+    {  // first segment: largest i with pre[i] <= k
+      int lo = 0, hi = s;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (pre[mid] <= k) lo = mid; else hi = mid;
+      }
+      i = lo;
+    }
+#pragma unroll 2
+    for (int t = 0; t < 8; ++t, k += 32) {
+      if (k >= total) break;
+      while (pre[i + 1] <= k) ++i;
+      const int32_t x = ldg_i32(g.col + lb[i] + (k - pre[i]));
+      if (x <= smax) {
+        const int j = hash_find(hkey, hval, x);
+        if (j >= 0) {
+          if (Q == 2) {
+            acc += WGT ? (uint64_t)(pre[j + 1] - pre[j]) : 1;
+            if (PART) {
+              atomicAdd(&cnt[i], 1u);
+              atomicAdd(&cnt[j], 1u);
+              atomicAdd(&part.e[lb[i] + (k - pre[i])], 1u);
+            }
+          } else {
+            atomicOr(&rows[tri_row_off(i, W) + (j >> 5) - (i >> 5)], 1u << (j & 31));
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (PART) {
+    for (int i = tid; i < s; i += kCtaThreads)
+      if (cnt[i]) {
+        atomicAdd(&part.v[S[i]], (unsigned long long)cnt[i]);
+        atomicAdd(&part.e[sbase + i], cnt[i]);
+      }
+  }
+  if (Q == 3) acc = cta_count_rows<3, WGT>(rows, s, pre);
+  if (Q == 4) acc = cta_count_rows<4, false>(rows, s, pre);
+  return acc;
+}
+
+// CTA-wide ordered intersection N+(v0) & N+(v1) into S; returns its size or -1 when it
+// exceeds kCtaCap.  Members of N+(v1) are binary-searched in N+(v0) (global, sorted).
+// PART credits the triangles (v0, v1, w): edges (v1, w) and (v0, w) and vertex w.
+template <bool PART>
+__device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_t v1, Part part) {
+  int32_t* S = (int32_t*)(sm + kOffS);
+  int32_t* wtot = (int32_t*)(sm + kOffMisc);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const longlong2 a = ldg_ll2(g.dptr + v0), b = ldg_ll2(g.dptr + v1);
+  int n = 0;
+  for (long long base = b.x; base < b.y; base += kCtaThreads) {
+    const long long e = base + tid;
+    bool found = false;
+    int32_t y = 0;
+    if (e < b.y) {
+      y = ldg_i32(g.col + e);
+      long long lo = a.x, hi = a.y;
+      while (lo < hi) {
+        long long mid = (lo + hi) >> 1;
+        if (ldg_i32(g.col + mid) < y) lo = mid + 1; else hi = mid;
+      }
+      found = lo < a.y && ldg_i32(g.col + lo) == y;
+      if (PART && found) {
+        atomicAdd(&part.e[e], 1u);
+        atomicAdd(&part.e[lo], 1u);
+        atomicAdd(&part.v[y], 1ull);
+      }
+    }
+    const unsigned bal = __ballot_sync(kFull, found);
+    if (lane == 0) wtot[warp] = __popc(bal);
+    __syncthreads();
+    int off = n;
+    for (int w = 0; w < warp; ++w) off += wtot[w];
+    int tot = 0;
+    for (int w = 0; w < kCtaWarps; ++w) tot += wtot[w];
+    const int pos = off + __popc(bal & lanemask_lt());
+    if (!PART && found && pos < kCtaCap) S[pos] = y;
+    n += tot;
+    __syncthreads();
+  }
+  return (PART || n <= kCtaCap) ? n : -1;
+}
+
+// --------------------------------------------------------------- warp tier
+__device__ __forceinline__ int warp_bsearch(const int32_t* S, int s, int32_t x) {
+  int lo = 0, hi = s;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (S[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return (lo < s && S[lo] == x) ? lo : -1;
+}
+
+// One warp, local set S = N+(v0) with s <= 32: Q-cliques of the local DAG.
+template <int Q, int MODE>
+__device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Part part) {
+  static_assert(Q >= 2, "warp tasks count at least local edges");
+  constexpr bool PART = MODE == kModePart;
+  constexpr bool WGT = MODE == kModeWeight;
+  const int lane = threadIdx.x & 31;
+  const longlong2 d0 = ldg_ll2(g.dptr + v0);
+  const int s = (int)(d0.y - d0.x);
+  int len = 0;
+  if (lane < s) {
+    const int32_t x = ldg_i32(g.col + d0.x + lane);
+    w.S[lane] = x;
+    const longlong2 d = ldg_ll2(g.dptr + x);
+    w.lb[lane] = d.x;
+    len = (int)(d.y - d.x);
+  }
+  int inc = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  w.pre[lane] = inc - len;
+  if (lane == 31) w.pre[32] = inc;
+  w.rows[lane] = 0u;
+  w.cnt[lane] = 0u;
+  __syncwarp();  // pre[s] is the total: lanes >= s contributed length 0
+  const int total = w.pre[s];
+  const int32_t smax = w.S[s - 1];
+  uint64_t acc = 0;
+  int i = 0;
+  for (int k = lane; k < total; k += 32) {
+    while (w.pre[i + 1] <= k) ++i;
+    const int32_t x = ldg_i32(g.col + w.lb[i] + (k - w.pre[i]));
+    if (x <= smax) {
+      const int j = warp_bsearch(w.S, s, x);
+      if (j >= 0) {
+        if (Q == 2) {
+          acc += WGT ? (uint64_t)(w.pre[j + 1] - w.pre[j]) : 1;
+          if (PART) {
+            atomicAdd(&w.cnt[i], 1u);
+            atomicAdd(&w.cnt[j], 1u);
+            atomicAdd(&part.e[w.lb[i] + (k - w.pre[i])], 1u);
+          }
+        } else {
+          atomicOr(&w.rows[i], 1u << j);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (PART && lane < s && w.cnt[lane]) {
+    atomicAdd(&part.v[w.S[lane]], (unsigned long long)w.cnt[lane]);
+    atomicAdd(&part.e[d0.x + lane], w.cnt[lane]);
+  }
+  if (Q >= 3 && lane < s) {
+    const uint32_t r = w.rows[lane];
+    uint32_t bits = r;
+    while (bits) {
+      const int j = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const uint32_t m = r & w.rows[j];
+      if (Q == 3) {
+        if (WGT) {
+          uint32_t b3 = m;
+          while (b3) {
+            const int l = __ffs(b3) - 1;
+            b3 &= b3 - 1;
+            acc += (uint64_t)(w.pre[l + 1] - w.pre[l]);
+          }
+        } else {
+          acc += __popc(m);
+        }
+      } else {
+        uint32_t b2 = m;
+        while (b2) {
+          const int l = __ffs(b2) - 1;
+          b2 &= b2 - 1;
+          acc += __popc(m & w.rows[l]);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  return acc;
+}
+
+// ------------------------------------------------------------ persistent kernel
+// K = clique size (3, 4, 5).  MODE kModePart (K == 3 only) credits triangle
+// participation to `part` instead of counting; kModeWeight (K <= 4) weights each clique
+// by the out-degree of its highest-ranked vertex.
+template <int K, int MODE>
+__global__ void __launch_bounds__(kCtaThreads, 2)
+    k_clique(GView g, TaskLists t, QueueHeads* q, unsigned long long* count, uint32_t* err,
+             Part part) {
+  constexpr bool PART = MODE == kModePart;
+  extern __shared__ __align__(16) char sm[];
+  __shared__ long long task_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long n_split = t.n[0], n_cta = t.n[1], n_warp = t.n[2], n_hubs = t.n[3];
+  uint64_t acc = 0;
+
+  // 1) hub edge sub-tasks: local set N+(v0) & N+(v1), (K-2)-cliques of it
+  for (;;) {
+    if (tid == 0) task_s = (long long)atomicAdd(&q->split, 1ull);
+    __syncthreads();
+    const long long ti = task_s;
+    __syncthreads();
+    if (ti >= n_split) break;
+    const long long c0 = t.log_split ? clock64() : 0;
+    long long lo = 0, hi = n_hubs;  // hub h with split_off[h] <= ti < split_off[h+1]
+    while (hi - lo > 1) {
+      long long mid = (lo + hi) >> 1;
+      if (t.split_off[mid] <= ti) lo = mid; else hi = mid;
+    }
+    const int32_t v0 = t.split_v[lo];
+    const longlong2 d0 = ldg_ll2(g.dptr + v0);
+    const long long e01 = d0.x + (ti - t.split_off[lo]);
+    const int32_t v1 = ldg_i32(g.col + e01);
+    const int n = cta_intersect_into_S<PART>(g, sm, v0, v1, part);
+    if (n < 0) {
+      if (tid == 0) atomicOr(err, ERR_CAPACITY);
+    } else if (PART) {
+      if (tid == 0 && n > 0) {
+        atomicAdd(&part.v[v0], (unsigned long long)n);
+        atomicAdd(&part.v[v1], (unsigned long long)n);
+        atomicAdd(&part.e[e01], (unsigned)n);
+      }
+    } else if (n > 0) {
+      uint64_t r = cta_local<K - 2, (PART ? kModeCount : MODE)>(g, sm, n, part, -1);
+      if (K - 2 == 1 && MODE != kModeWeight) {
+        if (tid == 0) acc += r;  // Q == 1 returns n from every thread; count it once
+      } else {
+        acc += r;
+      }
+    }
+    __syncthreads();
+    if (t.log_split && tid == 0) t.log_split[ti] = clock64() - c0;
+  }
+  // 2) CTA vertex tasks: local set N+(v0)
+  for (;;) {
+    if (tid == 0) task_s = (long long)atomicAdd(&q->cta, 1ull);
+    __syncthreads();
+    const long long ti = task_s;
+    __syncthreads();
+    if (ti >= n_cta) break;
+    const long long c0 = t.log_cta ? clock64() : 0;
+    const int32_t v0 = t.cta[ti];
+    const longlong2 d0 = ldg_ll2(g.dptr + v0);
+    const int s = (int)(d0.y - d0.x);
+    if (s > kCtaCap) {
+      if (tid == 0) atomicOr(err, ERR_CAPACITY);
+    } else if (s >= K - 1) {
+      int32_t* S = (int32_t*)(sm + kOffS);
+      for (int i = tid; i < s; i += kCtaThreads) S[i] = ldg_i32(g.col + d0.x + i);
+      __syncthreads();
+      uint64_t r = cta_local<K - 1, MODE>(g, sm, s, part, d0.x);
+      if (PART) {
+        // every local edge is a triangle containing v0
+        uint64_t tot = warp_sum_u64(r);
+        if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
+      } else {
+        acc += r;
+      }
+    }
+    __syncthreads();
+    if (t.log_cta && tid == 0) t.log_cta[ti] = clock64() - c0;
+  }
+  // 3) warp vertex tasks (s <= 32); the CTA region is reused per warp
+  WarpSmem& ws = ((WarpSmem*)sm)[warp];
+  for (;;) {
+    long long ti = 0;
+    if (lane == 0) ti = (long long)atomicAdd(&q->warp, 1ull);
+    ti = __shfl_sync(kFull, ti, 0);
+    if (ti >= n_warp) break;
+    const long long c0 = t.log_warp ? clock64() : 0;
+    const int32_t v0 = t.warp[ti];
+    const longlong2 d0 = ldg_ll2(g.dptr + v0);
+    const int s = (int)(d0.y - d0.x);
+    if (s > kWarpCap) {
+      if (lane == 0) atomicOr(err, ERR_CAPACITY);
+    } else if (s >= K - 1) {
+      uint64_t r = warp_vertex_task<K - 1, MODE>(g, ws, v0, part);
+      if (PART) {
+        uint64_t tot = warp_sum_u64(r);
+        if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
+      } else {
+        acc += r;
+      }
+    }
+    if (t.log_warp && lane == 0) t.log_warp[ti] = clock64() - c0;
+  }
+  if (!PART) {
+    acc = warp_sum_u64(acc);
+    if (lane == 0 && acc) atomicAdd(count, (unsigned long long)acc);
+  }
+}
+
+template <int K, int MODE>
+cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned long long* count,
+                     uint32_t* err, Part part, int grid, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_clique<K, MODE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kCtaSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  k_clique<K, MODE><<<grid, kCtaThreads, kCtaSmem, s>>>(g, t, q, count, err, part);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t clique_smem_bytes() { return kCtaSmem; }
+
+cudaError_t clique_occupancy(int* per_sm) {
+  cudaError_t e = cudaFuncSetAttribute(k_clique<4, kModeCount>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kCtaSmem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_clique<4, kModeCount>,
+                                                       kCtaThreads, kCtaSmem);
+}
+
+int clique_grid(int num_sms) { return 2 * num_sms; }
+
+cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads* q,
+                          unsigned long long* count, uint32_t* err, int grid, cudaStream_t s) {
+  const Part none{nullptr, nullptr};
+  switch (k) {
+    case 3: return launch_k<3, kModeCount>(g, t, q, count, err, none, grid, s);
+    case 4: return launch_k<4, kModeCount>(g, t, q, count, err, none, grid, s);
+    case 5: return launch_k<5, kModeCount>(g, t, q, count, err, none, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_clique_weighted(int k, const GView& g, const TaskLists& t, QueueHeads* q,
+                                   unsigned long long* sum, uint32_t* err, int grid,
+                                   cudaStream_t s) {
+  const Part none{nullptr, nullptr};
+  switch (k) {
+    case 3: return launch_k<3, kModeWeight>(g, t, q, sum, err, none, grid, s);
+    case 4: return launch_k<4, kModeWeight>(g, t, q, sum, err, none, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_triangle_participation(const GView& g, const TaskLists& t, QueueHeads* q,
+                                          unsigned long long* vpart, unsigned* epart,
+                                          uint32_t* err, int grid, cudaStream_t s) {
+  return launch_k<3, kModePart>(g, t, q, nullptr, err, Part{vpart, epart}, grid, s);
+}
+
+}  // namespace xgm

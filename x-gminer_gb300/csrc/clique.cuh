@@ -1,0 +1,60 @@
+// Clique / triangle counting on the degree-oriented DAG (clique.cu).
+#pragma once
+#include "common.cuh"
+
+namespace xgm {
+
+constexpr int kCtaThreads = 512;            // threads of the persistent counting CTA
+constexpr int kCtaWarps = kCtaThreads / 32;
+constexpr int kCtaCap = 1024;               // largest local set a CTA task holds
+constexpr int kHashSize = 2048;             // open-addressing table for the local set
+constexpr int kWarpCap = 32;                // largest local set a warp task holds
+
+// Task lists of one counting launch.  Sizes live on the device (`n`), so task
+// generation and counting run without a host round trip and can be graph-captured:
+//   n[0] = hub edge sub-tasks, n[1] = CTA vertex tasks, n[2] = warp vertex tasks,
+//   n[3] = hub vertices.
+// Hub sub-task t belongs to hub split_v[h] with split_off[h] <= t < split_off[h+1];
+// its second vertex is the (t - split_off[h])-th out-neighbour of the hub.
+// Per-task timing logs (clock64 cycles) are indexed like the lists; any may be null.
+struct TaskLists {
+  const int32_t* cta = nullptr;    // vertex tasks run by one CTA (out-degree <= kCtaCap)
+  const int32_t* warp = nullptr;   // vertex tasks run by one warp (out-degree <= kWarpCap)
+  const int32_t* split_v = nullptr;
+  const int64_t* split_off = nullptr;
+  const int64_t* n = nullptr;
+  long long* log_cta = nullptr;
+  long long* log_warp = nullptr;
+  long long* log_split = nullptr;
+};
+
+// Work-queue heads, zeroed before each launch.
+struct QueueHeads {
+  unsigned long long split, cta, warp, pad;
+};
+
+size_t clique_smem_bytes();
+// Resident counting CTAs per SM (dynamic shared memory bound).
+cudaError_t clique_occupancy(int* per_sm);
+
+// k in {3, 4, 5}: adds the k-clique count of g (DAG) over the listed tasks to *count.
+cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads* q,
+                          unsigned long long* count, uint32_t* err, int grid, cudaStream_t s);
+
+// Triangle participation from the same task lists run with k = 3: every triangle adds
+// 1 to vpart[] of its three vertices and 1 to epart[] of its three edges (edge = index
+// of the entry in the rank-space col array, stored on the lower endpoint).  Feeds the
+// tailed-triangle and diamond plans.
+cudaError_t launch_triangle_participation(const GView& g, const TaskLists& t, QueueHeads* q,
+                                          unsigned long long* vpart, unsigned* epart,
+                                          uint32_t* err, int grid, cudaStream_t s);
+
+// Sum over k-cliques (k in {3, 4}) of the out-degree of each clique's highest-ranked
+// vertex; gives the W-dependent terms of the plans' algorithmic bytes.
+cudaError_t launch_clique_weighted(int k, const GView& g, const TaskLists& t, QueueHeads* q,
+                                   unsigned long long* sum, uint32_t* err, int grid,
+                                   cudaStream_t s);
+
+int clique_grid(int num_sms);
+
+}  // namespace xgm

@@ -1,0 +1,317 @@
+// Count dispatch behind xgm_count: schedule -> persistent counting launch -> uint64.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "api_internal.h"
+#include "learned.cuh"
+#include "measure.cuh"
+#include "motif.cuh"
+#include "prim.cuh"
+
+namespace xgm {
+
+namespace {
+
+template <class T>
+cudaError_t grow(T** p, int64_t* cap, int64_t n, cudaStream_t s) {
+  if (*cap >= n && *p) return cudaSuccess;
+  if (*p) cudaFreeAsync(*p, s);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMallocAsync((void**)p, sizeof(T) * (size_t)(n > 0 ? n : 1), s);
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+int clique_kind(int pattern) {
+  switch (pattern) {
+    case XGM_PATTERN_TRIANGLE: return 3;
+    case XGM_PATTERN_CLIQUE4: return 4;
+    case XGM_PATTERN_CLIQUE5: return 5;
+    default: return 0;
+  }
+}
+
+int ensure_clique_grid(xgm_ctx* ctx) {
+  if (ctx->clique_grid == 0) {
+    int per_sm = 0;
+    if (clique_occupancy(&per_sm) != cudaSuccess || per_sm <= 0) per_sm = 1;
+    ctx->clique_grid = per_sm * ctx->num_sms;
+  }
+  return ctx->clique_grid;
+}
+
+// Fills tb from the schedule policy for a k-clique style launch.
+xgm_status schedule_tasks(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp) {
+  cudaStream_t s = ctx->stream;
+  bool order = false;
+  if (sp.policy == XGM_SCHED_LEARNED) {
+    if (!sp.model) {
+      set_thread_error("XGM_SCHED_LEARNED needs a trained model (xgm_sched.model)");
+      return XGM_ERR_INVALID;
+    }
+    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, ctx->tb, s));
+    order = sp.order_by_cost != 0;
+  } else {
+    int wmax = sp.warp_max > 0 ? sp.warp_max : kWarpCap;
+    int cmax = sp.cta_max > 0 ? sp.cta_max : kCtaCap;
+    if (sp.policy == XGM_SCHED_FIXED) {
+      switch (sp.variant) {
+        case XGM_VAR_WARP: wmax = kWarpCap; cmax = kCtaCap; break;
+        case XGM_VAR_CTA: wmax = 0; cmax = kCtaCap; break;
+        case XGM_VAR_SPLIT: wmax = 0; cmax = 0; break;
+        default:
+          set_thread_error("unknown variant for XGM_SCHED_FIXED");
+          return XGM_ERR_INVALID;
+      }
+    } else if (sp.policy != XGM_SCHED_HEURISTIC) {
+      set_thread_error("unknown schedule policy");
+      return XGM_ERR_INVALID;
+    }
+    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, cmax, ctx->tb, s));
+  }
+  XGM_CUDA_TRY(build_lists(g, ctx->tb, order, s));
+  return XGM_OK;
+}
+
+xgm_status ensure_c4(xgm_ctx* ctx, const DevGraph& g) {
+  cudaStream_t s = ctx->stream;
+  if (ctx->c4_vcap < g.nv || !ctx->wedges) {
+    void* ps[] = {ctx->wedges, ctx->c4_flag_large, ctx->c4_flag_small, ctx->c4_pos,
+                  ctx->c4_large, ctx->c4_small, ctx->c4_n};
+    for (void* p : ps)
+      if (p) cudaFreeAsync(p, s);
+    const int64_t c = g.nv > 0 ? g.nv : 1;
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->wedges, sizeof(long long) * c, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_flag_large, c, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_flag_small, c, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_pos, sizeof(int64_t) * c, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_large, sizeof(int32_t) * c, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_small, sizeof(int32_t) * c, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_n, sizeof(int64_t) * 2, s));
+    ctx->c4_vcap = c;
+  }
+  const int64_t need = (int64_t)cycle4_grid(ctx->num_sms) * (g.nv > 0 ? g.nv : 1);
+  if (ctx->c4_scratch_cap < need) {
+    XGM_CUDA_TRY(grow(&ctx->c4_scratch, &ctx->c4_scratch_cap, need, s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_scratch, 0, sizeof(uint32_t) * need, s));
+  }
+  return XGM_OK;
+}
+
+}  // namespace
+
+void motif_buffers_free(xgm_ctx* ctx) {
+  cudaStream_t s = ctx->stream;
+  void* ps[] = {ctx->vpart, ctx->epart, ctx->c4_scratch, ctx->wedges, ctx->c4_flag_large,
+                ctx->c4_flag_small, ctx->c4_pos, ctx->c4_large, ctx->c4_small, ctx->c4_n};
+  for (void* p : ps)
+    if (p) cudaFreeAsync(p, s);
+}
+
+xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
+                          uint64_t* out, xgm_stats& st) {
+  cudaStream_t s = ctx->stream;
+  XGM_CUDA_TRY(cudaSetDevice(ctx->device));
+  XGM_CUDA_TRY(taskbuf_reserve(ctx->tb, g.nv, s));
+  XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  const int k = clique_kind(pattern);
+  const GView view = g.view();
+  int launches = 0;
+  if (k) {
+    xgm_status r = schedule_tasks(ctx, g, k, sp);
+    if (r != XGM_OK) return r;
+    XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+    XGM_CUDA_TRY(launch_clique(k, view, ctx->tb.lists(false), &ctx->d_sc->q, &ctx->d_sc->count,
+                               &ctx->d_sc->err, ensure_clique_grid(ctx), s));
+    launches = 1;
+  } else if (pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_TAILED_TRIANGLE) {
+    xgm_sched tri = sp;
+    if (tri.policy == XGM_SCHED_LEARNED && !tri.model) tri.policy = XGM_SCHED_HEURISTIC;
+    xgm_status r = schedule_tasks(ctx, g, 3, tri);
+    if (r != XGM_OK) return r;
+    XGM_CUDA_TRY(grow(&ctx->vpart, &ctx->vpart_cap, g.nv, s));
+    XGM_CUDA_TRY(grow(&ctx->epart, &ctx->epart_cap, g.ne, s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->vpart, 0, sizeof(unsigned long long) * (g.nv > 0 ? g.nv : 1), s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->epart, 0, sizeof(unsigned) * (g.ne > 0 ? g.ne : 1), s));
+    XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+    XGM_CUDA_TRY(launch_triangle_participation(view, ctx->tb.lists(false), &ctx->d_sc->q,
+                                               ctx->vpart, ctx->epart, &ctx->d_sc->err,
+                                               ensure_clique_grid(ctx), s));
+    if (pattern == XGM_PATTERN_DIAMOND)
+      XGM_CUDA_TRY(launch_diamond_reduce(ctx->epart, g.ne, &ctx->d_sc->count, s));
+    else
+      XGM_CUDA_TRY(launch_tailed_reduce(ctx->vpart, g.rowptr, g.nv, &ctx->d_sc->count, s));
+    launches = 2;
+  } else if (pattern == XGM_PATTERN_CYCLE4) {
+    xgm_status r = ensure_c4(ctx, g);
+    if (r != XGM_OK) return r;
+    XGM_CUDA_TRY(launch_wedge_count(view, ctx->wedges, ctx->c4_flag_large, ctx->c4_flag_small, s));
+    XGM_CUDA_TRY(scan_excl(ctx->c4_flag_large, ctx->c4_pos, g.nv, ctx->c4_n + 0, s));
+    XGM_CUDA_TRY(launch_scatter_flags(ctx->c4_flag_large, ctx->c4_pos, g.nv, ctx->c4_large, s));
+    XGM_CUDA_TRY(scan_excl(ctx->c4_flag_small, ctx->c4_pos, g.nv, ctx->c4_n + 1, s));
+    XGM_CUDA_TRY(launch_scatter_flags(ctx->c4_flag_small, ctx->c4_pos, g.nv, ctx->c4_small, s));
+    XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+    XGM_CUDA_TRY(launch_cycle4(view, ctx->c4_large, ctx->c4_small, ctx->c4_n, ctx->d_sc->c4heads,
+                               ctx->c4_scratch, &ctx->d_sc->count, &ctx->d_sc->err,
+                               cycle4_grid(ctx->num_sms), s));
+    launches = 1;
+  } else {
+    set_thread_error("unknown pattern");
+    return XGM_ERR_INVALID;
+  }
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+  if (k || pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_TAILED_TRIANGLE)
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 4,
+                                 cudaMemcpyDeviceToDevice, s));
+  xgm_status r = ctx_sync_scalars(ctx);
+  if (r != XGM_OK) return r;
+  float prep = 0, kern = 0;
+  cudaEventElapsedTime(&prep, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&kern, ctx->ev[1], ctx->ev[2]);
+  st.prep_ms = prep;
+  st.kernel_ms = kern;
+  st.device_error = ctx->h_sc->err;
+  st.launches = launches;
+  st.variant_tasks[XGM_VAR_WARP] = ctx->h_sc->n[2];
+  st.variant_tasks[XGM_VAR_CTA] = ctx->h_sc->n[1];
+  st.variant_tasks[XGM_VAR_SPLIT] = ctx->h_sc->n[0];
+  st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3];
+  r = check_device_flag(ctx, ctx->h_sc->err);
+  if (r != XGM_OK) return r;
+  *out = ctx->h_sc->count;
+  return XGM_OK;
+}
+
+// Captures the device work of one count (schedule + counting kernels) on the context
+// stream into a CUDA graph and counts its kernel nodes.
+xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
+                         int* n_kernels) {
+  cudaStream_t s = ctx->stream;
+  XGM_CUDA_TRY(cudaSetDevice(ctx->device));
+  XGM_CUDA_TRY(taskbuf_reserve(ctx->tb, g.nv, s));
+  const int k = clique_kind(pattern);
+  if (!k) {
+    set_thread_error("kernel counting covers the triangle / clique plans");
+    return XGM_ERR_UNSUPPORTED;
+  }
+  ensure_clique_grid(ctx);
+  XGM_CUDA_TRY(cudaStreamSynchronize(s));
+  XGM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  xgm_status r = schedule_tasks(ctx, g, k, sp);
+  cudaError_t e = cudaSuccess;
+  if (r == XGM_OK)
+    e = launch_clique(k, g.view(), ctx->tb.lists(false), &ctx->d_sc->q, &ctx->d_sc->count,
+                      &ctx->d_sc->err, ensure_clique_grid(ctx), s);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+  if (r != XGM_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return r;
+  }
+  XGM_CUDA_TRY(e);
+  XGM_CUDA_TRY(e2);
+  size_t n = 0;
+  e = cudaGraphGetNodes(graph, nullptr, &n);
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (e == cudaSuccess && n) e = cudaGraphGetNodes(graph, nodes.data(), &n);
+  int kern = 0;
+  for (size_t i = 0; e == cudaSuccess && i < n; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kern;
+  }
+  cudaGraphDestroy(graph);
+  XGM_CUDA_TRY(e);
+  *n_kernels = kern;
+  return XGM_OK;
+}
+
+xgm_status algo_bytes_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, uint64_t* out) {
+  cudaStream_t s = ctx->stream;
+  XGM_CUDA_TRY(cudaSetDevice(ctx->device));
+  XGM_CUDA_TRY(taskbuf_reserve(ctx->tb, g.nv, s));
+  XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
+  const GView view = g.view();
+  unsigned long long* acc = &ctx->d_sc->count;
+  const int k = clique_kind(pattern);
+  xgm_sched heur;
+  std::memset(&heur, 0, sizeof(heur));
+  if (k) {
+    XGM_CUDA_TRY(launch_bytes_basic(view, 0, acc, s));
+    // W terms: 4 * sum over kk-cliques of d+(top member), kk = 3 .. k-1
+    for (int kk = 3; kk <= k - 1; ++kk) {
+      xgm_status r = schedule_tasks(ctx, g, kk, heur);
+      if (r != XGM_OK) return r;
+      XGM_CUDA_TRY(cudaMemsetAsync(&ctx->d_sc->q, 0, sizeof(QueueHeads), s));
+      XGM_CUDA_TRY(launch_clique_weighted(kk, view, ctx->tb.lists(false), &ctx->d_sc->q,
+                                          &ctx->d_sc->aux, &ctx->d_sc->err,
+                                          ensure_clique_grid(ctx), s));
+    }
+    xgm_status r = ctx_sync_scalars(ctx);
+    if (r != XGM_OK) return r;
+    *out = ctx->h_sc->count + 4ull * ctx->h_sc->aux;
+    return check_device_flag(ctx, ctx->h_sc->err);
+  } else if (pattern == XGM_PATTERN_DIAMOND) {
+    XGM_CUDA_TRY(launch_bytes_basic(view, 1, acc, s));
+  } else if (pattern == XGM_PATTERN_TAILED_TRIANGLE) {
+    XGM_CUDA_TRY(launch_bytes_basic(view, 2, acc, s));
+  } else if (pattern == XGM_PATTERN_CYCLE4) {
+    xgm_status r = ensure_c4(ctx, g);
+    if (r != XGM_OK) return r;
+    XGM_CUDA_TRY(launch_bytes_basic(view, 3, acc, s));
+    XGM_CUDA_TRY(launch_wedge_count(view, ctx->wedges, ctx->c4_flag_large, ctx->c4_flag_small, s));
+    XGM_CUDA_TRY(launch_sum_ll(ctx->wedges, g.nv, &ctx->d_sc->aux, s));
+    xgm_status r2 = ctx_sync_scalars(ctx);
+    if (r2 != XGM_OK) return r2;
+    *out = ctx->h_sc->count + 4ull * ctx->h_sc->aux;
+    return check_device_flag(ctx, ctx->h_sc->err);
+  } else {
+    return XGM_ERR_INVALID;
+  }
+  xgm_status r = ctx_sync_scalars(ctx);
+  if (r != XGM_OK) return r;
+  *out = ctx->h_sc->count;
+  return check_device_flag(ctx, ctx->h_sc->err);
+}
+
+// Pattern matching of a small adjacency matrix against the builtins (edge-induced).
+int match_pattern(const xgm_plan_desc* d) {
+  const int n = d->num_vertices;
+  if (n < 3 || n > 8) return -1;
+  int deg[8] = {0}, m = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const bool a = d->adj[i][j] != 0, b = d->adj[j][i] != 0;
+      if (a != b || (i == j && a)) return -1;
+      if (a && i < j) ++m, ++deg[i], ++deg[j];
+    }
+  int sorted[8];
+  for (int i = 0; i < n; ++i) sorted[i] = deg[i];
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j)
+      if (sorted[j] < sorted[i]) { int t = sorted[i]; sorted[i] = sorted[j]; sorted[j] = t; }
+  if (n == 3 && m == 3) return XGM_PATTERN_TRIANGLE;
+  if (n == 4 && m == 6) return XGM_PATTERN_CLIQUE4;
+  if (n == 5 && m == 10) return XGM_PATTERN_CLIQUE5;
+  if (n == 4 && m == 5) return XGM_PATTERN_DIAMOND;  // K4 minus one edge
+  if (n == 4 && m == 4 && sorted[0] == 2 && sorted[3] == 2) return XGM_PATTERN_CYCLE4;
+  if (n == 4 && m == 4 && sorted[0] == 1 && sorted[1] == 2 && sorted[2] == 2 && sorted[3] == 3)
+    return XGM_PATTERN_TAILED_TRIANGLE;
+  return 0;
+}
+
+int pattern_from_name(const char* name) {
+  const std::string s(name);
+  if (s == "triangle" || s == "3-clique" || s == "clique3" || s == "tc") return XGM_PATTERN_TRIANGLE;
+  if (s == "4-clique" || s == "clique4" || s == "k4") return XGM_PATTERN_CLIQUE4;
+  if (s == "5-clique" || s == "clique5" || s == "k5") return XGM_PATTERN_CLIQUE5;
+  if (s == "diamond") return XGM_PATTERN_DIAMOND;
+  if (s == "rectangle" || s == "4-cycle" || s == "cycle4") return XGM_PATTERN_CYCLE4;
+  if (s == "tailedtriangle" || s == "tailed-triangle" || s == "tailed_triangle")
+    return XGM_PATTERN_TAILED_TRIANGLE;
+  return 0;
+}
+
+}  // namespace xgm

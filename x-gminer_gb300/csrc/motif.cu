@@ -1,0 +1,274 @@
+// Edge-induced 4-vertex motif plans on the undirected graph (rank ids).
+//
+// Reference (CPU, the counting definitions): codes/GraphMiner/src/count/omp_base.cc:5-58
+// with cpu_kernels/diamond.h:1-8, rectangle.h:1-46 and tailedtriangle.h:1-12; GPU
+// analogues codes/GraphMiner/src/count/gpu_base.cu:1-104.
+//
+//  diamond        = sum over undirected edges e of C(n_e, 2), n_e = |N(u) & N(v)| =
+//                   number of triangles containing e.
+//  tailed triangle = sum over v with deg(v) > 2 of t(v) * (deg(v) - 2), t(v) = number
+//                   of triangles containing v.
+//  4-cycle        = for every v0, wedges v0-v1-v2 with v1 < v0 and v2 < v0 grouped by
+//                   v2; a group of c wedges closes C(c, 2) cycles.
+// n_e and t(v) come from one triangle-participation pass of the DAG kernels
+// (clique.cu); the 4-cycle plan has its own kernel below.  Any total order of the
+// vertices gives the same counts, so rank ids serve for the "v1 < v0" restrictions.
+#include "motif.cuh"
+
+namespace xgm {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__global__ void k_diamond_reduce(const unsigned* epart, int64_t ne, unsigned long long* out) {
+  unsigned long long acc = 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long n = epart[e];
+    acc += n * (n - (n > 0)) / 2;
+  }
+  acc = warp_sum_u64(acc);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+__global__ void k_tailed_reduce(const unsigned long long* vpart, const int64_t* rowptr, int64_t nv,
+                                unsigned long long* out) {
+  unsigned long long acc = 0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nv;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t d = rowptr[r + 1] - rowptr[r];
+    if (d > 2) acc += vpart[r] * (unsigned long long)(d - 2);
+  }
+  acc = warp_sum_u64(acc);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+// Entries of row v1 below v0: col[rowptr[v1] .. first index with col >= v0).
+__device__ __forceinline__ long long lower_end(const GView& g, int32_t v1, int32_t v0) {
+  long long lo = g.rowptr[v1], hi = g.dptr[v1].y;
+  while (lo < hi) {
+    long long mid = (lo + hi) >> 1;
+    if (ldg_i32(g.col + mid) < v0) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// wedges[r] = number of wedges r-v1-v2 with v1, v2 < r.  Warp per vertex.
+__global__ void k_wedge_count(GView g, long long* wedges, int hash_half, uint8_t* is_large,
+                              uint8_t* is_small) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < g.nv; r += warps) {
+    const long long a0 = g.rowptr[r], a1 = g.dptr[r].x;  // lower neighbours
+    long long w = 0;
+    for (long long e = a0 + lane; e < a1; e += 32) {
+      const int32_t v1 = ldg_i32(g.col + e);
+      w += lower_end(g, v1, (int32_t)r) - g.rowptr[v1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(kFull, w, o);
+    if (lane == 0) {
+      wedges[r] = w;
+      is_large[r] = w > hash_half;
+      is_small[r] = w > 1 && w <= hash_half;
+    }
+  }
+}
+
+__global__ void k_scatter_flags(const uint8_t* flag, const int64_t* pos, int64_t nv, int32_t* out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nv;
+       r += (int64_t)gridDim.x * blockDim.x)
+    if (flag[r]) out[pos[r]] = (int32_t)r;
+}
+
+// ------------------------------------------------------------ 4-cycle kernel
+constexpr int kC4Threads = 256;
+constexpr int kC4Chunk = 1024;           // lower neighbours handled per chunk
+constexpr int kC4Hash = 4096;            // smem hash slots (small tasks)
+
+struct C4Smem {
+  long long lb[kC4Chunk];
+  int32_t pre[kC4Chunk + 1];
+  int32_t hkey[kC4Hash];
+  uint32_t hcnt[kC4Hash];
+  int32_t wtot[kC4Threads / 32];
+  long long task;
+};
+
+__device__ __forceinline__ uint32_t c4_slot(int32_t x) {
+  return ((uint32_t)x * 2654435761u) >> (32 - 12);
+}
+
+// Loads chunk [c0, c0+n) of v0's lower neighbours: lb/pre (prefix of wedge lengths).
+__device__ int c4_load_chunk(const GView& g, C4Smem& sm, int32_t v0, long long c0, int n) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // kC4Chunk = 4 * kC4Threads: 4 items per thread
+  int len[4];
+  int s = 0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int i = tid * 4 + t;
+    len[t] = 0;
+    if (i < n) {
+      const int32_t v1 = ldg_i32(g.col + c0 + i);
+      const long long b = g.rowptr[v1];
+      sm.lb[i] = b;
+      len[t] = (int)(lower_end(g, v1, v0) - b);
+    }
+    s += len[t];
+  }
+  int inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) sm.wtot[warp] = inc;
+  __syncthreads();
+  int off = 0, tot = 0;
+  for (int w = 0; w < kC4Threads / 32; ++w) {
+    if (w < warp) off += sm.wtot[w];
+    tot += sm.wtot[w];
+  }
+  int ex = off + inc - s;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int i = tid * 4 + t;
+    if (i < n) sm.pre[i] = ex;
+    ex += len[t];
+  }
+  if (tid == 0) sm.pre[n] = tot;
+  __syncthreads();
+  return tot;
+}
+
+// Visits the v2 of every wedge of the loaded chunk (flattened, coalesced per row).
+template <class F>
+__device__ __forceinline__ void c4_walk(const GView& g, const C4Smem& sm, int n, int total, F f) {
+  const int tid = threadIdx.x;
+  for (int k = tid; k < total; k += kC4Threads) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (sm.pre[mid] <= k) lo = mid; else hi = mid;
+    }
+    f(ldg_i32(g.col + sm.lb[lo] + (k - sm.pre[lo])));
+  }
+}
+
+// Persistent CTA kernel.  Large tasks (more wedges than half the smem table) group
+// wedges in a per-CTA dense counter array in global memory (`scratch`, nv entries per
+// CTA, kept zeroed: each group is read back with atomicExch); small tasks use an
+// open-addressing table in shared memory.
+__global__ void __launch_bounds__(kC4Threads) k_cycle4(GView g, const int32_t* large,
+                                                       const int32_t* small, const int64_t* n,
+                                                       unsigned long long* heads,
+                                                       uint32_t* scratch,
+                                                       unsigned long long* out, uint32_t* err) {
+  __shared__ C4Smem sm;
+  const int tid = threadIdx.x;
+  uint32_t* cnt = scratch + (size_t)blockIdx.x * (size_t)g.nv;
+  unsigned long long acc = 0;
+  const long long n_large = n[0], n_small = n[1];
+  for (int phase = 0; phase < 2; ++phase) {
+    const int32_t* list = phase ? small : large;
+    const long long nt = phase ? n_small : n_large;
+    for (;;) {
+      if (tid == 0) sm.task = (long long)atomicAdd(&heads[phase], 1ull);
+      __syncthreads();
+      const long long ti = sm.task;
+      __syncthreads();
+      if (ti >= nt) break;
+      const int32_t v0 = list[ti];
+      const long long a0 = g.rowptr[v0], a1 = g.dptr[v0].x;
+      if (phase == 1)
+        for (int h = tid; h < kC4Hash; h += kC4Threads) sm.hkey[h] = -1, sm.hcnt[h] = 0;
+      __syncthreads();
+      for (int pass = 0; pass < (phase ? 1 : 2); ++pass) {
+        for (long long c0 = a0; c0 < a1; c0 += kC4Chunk) {
+          const int nc = (int)min((long long)kC4Chunk, a1 - c0);
+          const int total = c4_load_chunk(g, sm, v0, c0, nc);
+          if (phase == 0 && pass == 0) {
+            c4_walk(g, sm, nc, total, [&](int32_t v2) { atomicAdd(&cnt[v2], 1u); });
+          } else if (phase == 0) {
+            c4_walk(g, sm, nc, total, [&](int32_t v2) {
+              unsigned long long c = atomicExch(&cnt[v2], 0u);
+              acc += c * (c - (c > 0)) / 2;
+            });
+          } else {
+            c4_walk(g, sm, nc, total, [&](int32_t v2) {
+              uint32_t slot = c4_slot(v2);
+              for (int probe = 0; probe < kC4Hash; ++probe) {
+                int32_t k = atomicCAS(&sm.hkey[slot], -1, v2);
+                if (k == -1 || k == v2) {
+                  atomicAdd(&sm.hcnt[slot], 1u);
+                  return;
+                }
+                slot = (slot + 1) & (kC4Hash - 1);
+              }
+              atomicOr(err, ERR_CAPACITY);
+            });
+          }
+          __syncthreads();
+        }
+        __syncthreads();
+      }
+      if (phase == 1) {
+        for (int h = tid; h < kC4Hash; h += kC4Threads) {
+          unsigned long long c = sm.hcnt[h];
+          acc += c * (c - (c > 0)) / 2;
+        }
+        __syncthreads();
+      }
+    }
+  }
+  acc = warp_sum_u64(acc);
+  if ((tid & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+inline unsigned grid_for(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, int64_t(1) << 20));
+}
+
+}  // namespace
+
+cudaError_t launch_diamond_reduce(const unsigned* epart, int64_t ne, unsigned long long* out,
+                                  cudaStream_t s) {
+  k_diamond_reduce<<<grid_for(ne), kThreads, 0, s>>>(epart, ne, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tailed_reduce(const unsigned long long* vpart, const int64_t* rowptr, int64_t nv,
+                                 unsigned long long* out, cudaStream_t s) {
+  k_tailed_reduce<<<grid_for(nv), kThreads, 0, s>>>(vpart, rowptr, nv, out);
+  return cudaGetLastError();
+}
+
+int cycle4_grid(int num_sms) { return 4 * num_sms; }
+int cycle4_hash_half() { return kC4Hash / 2; }
+
+cudaError_t launch_wedge_count(const GView& g, long long* wedges, uint8_t* is_large,
+                               uint8_t* is_small, cudaStream_t s) {
+  if (g.nv == 0) return cudaSuccess;
+  k_wedge_count<<<grid_for(g.nv * 32), kThreads, 0, s>>>(g, wedges, kC4Hash / 2, is_large,
+                                                         is_small);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_flags(const uint8_t* flag, const int64_t* pos, int64_t nv, int32_t* out,
+                                 cudaStream_t s) {
+  if (nv == 0) return cudaSuccess;
+  k_scatter_flags<<<grid_for(nv), kThreads, 0, s>>>(flag, pos, nv, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cycle4(const GView& g, const int32_t* large, const int32_t* small,
+                          const int64_t* n, unsigned long long* heads, uint32_t* scratch,
+                          unsigned long long* out, uint32_t* err, int grid, cudaStream_t s) {
+  k_cycle4<<<grid, kC4Threads, 0, s>>>(g, large, small, n, heads, scratch, out, err);
+  return cudaGetLastError();
+}
+
+}  // namespace xgm

@@ -1,0 +1,27 @@
+// Edge-induced motif plans (motif.cu).
+#pragma once
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace xgm {
+
+cudaError_t launch_diamond_reduce(const unsigned* epart, int64_t ne, unsigned long long* out,
+                                  cudaStream_t s);
+cudaError_t launch_tailed_reduce(const unsigned long long* vpart, const int64_t* rowptr, int64_t nv,
+                                 unsigned long long* out, cudaStream_t s);
+
+// 4-cycle: wedge counts per vertex, then the persistent grouping kernel.
+int cycle4_grid(int num_sms);
+int cycle4_hash_half();
+cudaError_t launch_wedge_count(const GView& g, long long* wedges, uint8_t* is_large,
+                               uint8_t* is_small, cudaStream_t s);
+cudaError_t launch_scatter_flags(const uint8_t* flag, const int64_t* pos, int64_t nv, int32_t* out,
+                                 cudaStream_t s);
+// n[0] = large tasks, n[1] = small tasks; heads[0..1] zeroed; scratch = grid * nv
+// zeroed uint32 counters (left zeroed on return).
+cudaError_t launch_cycle4(const GView& g, const int32_t* large, const int32_t* small,
+                          const int64_t* n, unsigned long long* heads, uint32_t* scratch,
+                          unsigned long long* out, uint32_t* err, int grid, cudaStream_t s);
+
+}  // namespace xgm

@@ -1,0 +1,228 @@
+// Task generation for the clique kernels: variant per vertex -> ordered task lists.
+//
+// The reference sizes one grid per launch and grid-strides over the COO edge list
+// (clique4_warp_edge.cuh:14) or splits vertices by degree thresholds into warp / block
+// / per-hub launches (xgminer/src/glumin/glumin_GM_solver.cu:324-346, 490-503).  Here
+// one persistent launch consumes three device-built queues (clique.cu), and the
+// schedule is only the content and order of those queues; it never changes a count.
+#include "prim.cuh"
+#include "sched.cuh"
+
+namespace xgm {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kBins = 64;  // cost bins of the learned ordering
+
+inline unsigned grid_for(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  if (b < 1) b = 1;
+  if (b > (int64_t(1) << 20)) b = int64_t(1) << 20;
+  return (unsigned)b;
+}
+
+#define GRID_STRIDE(i, n)                                                   \
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); \
+       i += (int64_t)gridDim.x * blockDim.x)
+
+__global__ void k_classify_heur(const longlong2* dptr, int64_t nv, int kmin, int warp_max,
+                                int cta_max, uint8_t* var) {
+  GRID_STRIDE(r, nv) {
+    const longlong2 d = dptr[r];
+    const int64_t s = d.y - d.x;
+    uint8_t v;
+    if (s < kmin) v = VAR_SKIP;
+    else if (s <= warp_max) v = VAR_WARP;
+    else if (s <= cta_max) v = VAR_CTA;
+    else v = VAR_SPLIT;
+    var[r] = v;
+  }
+}
+
+__global__ void k_flag_eq(const uint8_t* var, int64_t nv, uint8_t x, uint8_t* flag) {
+  GRID_STRIDE(r, nv) flag[r] = var[r] == x;
+}
+
+__global__ void k_scatter(const uint8_t* flag, const int64_t* pos, int64_t nv, int32_t* out) {
+  GRID_STRIDE(r, nv) if (flag[r]) out[pos[r]] = (int32_t)r;
+}
+
+__global__ void k_hub_weights(const uint8_t* var, const longlong2* dptr, int64_t nv, int64_t* w) {
+  GRID_STRIDE(r, nv) {
+    const longlong2 d = dptr[r];
+    w[r] = var[r] == VAR_SPLIT ? (d.y - d.x) : 0;
+  }
+}
+
+__global__ void k_hub_offsets(const uint8_t* var, const int64_t* pos, const int64_t* w, int64_t nv,
+                              int64_t* split_off) {
+  GRID_STRIDE(r, nv) if (var[r] == VAR_SPLIT) split_off[pos[r]] = w[r];
+}
+
+__global__ void k_hub_tail(const int64_t* n, int64_t* split_off) {
+  split_off[n[3]] = n[0];
+}
+
+// ---- learned ordering: counting sort of each list by descending predicted cost
+__device__ __forceinline__ int cost_bin(float c) {
+  // predicted log2-cycles in [0, 32) -> 64 bins, bin 0 = most expensive
+  int b = (int)((32.0f - c) * 2.0f);
+  return b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+}
+
+__global__ void k_bin_hist(const uint8_t* var, const float* cost, int64_t nv,
+                           unsigned long long* hist /*[3][kBins]*/) {
+  __shared__ unsigned int h[3 * kBins];
+  for (int i = threadIdx.x; i < 3 * kBins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  GRID_STRIDE(r, nv) {
+    const uint8_t v = var[r];
+    if (v < 3) atomicAdd(&h[v * kBins + cost_bin(cost[r])], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * kBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], (unsigned long long)h[i]);
+}
+
+// One block: exclusive scan of each list's bins into cursors; list sizes into n[].
+__global__ void k_bin_scan(unsigned long long* hist, int64_t* n) {
+  if (threadIdx.x < 3) {
+    const int v = threadIdx.x;
+    unsigned long long run = 0;
+    for (int b = 0; b < kBins; ++b) {
+      unsigned long long c = hist[v * kBins + b];
+      hist[v * kBins + b] = run;
+      run += c;
+    }
+    // var code -> n[] slot: WARP -> n[2], CTA -> n[1], SPLIT -> n[3]
+    n[v == VAR_WARP ? 2 : (v == VAR_CTA ? 1 : 3)] = (int64_t)run;
+  }
+}
+
+__global__ void k_bin_scatter(const uint8_t* var, const float* cost, int64_t nv,
+                              unsigned long long* cursor, int32_t* warp_l, int32_t* cta_l,
+                              int32_t* hub_l) {
+  GRID_STRIDE(r, nv) {
+    const uint8_t v = var[r];
+    if (v < 3) {
+      const unsigned long long p = atomicAdd(&cursor[v * kBins + cost_bin(cost[r])], 1ull);
+      int32_t* out = v == VAR_WARP ? warp_l : (v == VAR_CTA ? cta_l : hub_l);
+      out[p] = (int32_t)r;
+    }
+  }
+}
+
+// Hub sub-task offsets in hub-list order.
+__global__ void k_hub_weights_list(const int32_t* hubs, const int64_t* n, const longlong2* dptr,
+                                   int64_t* w) {
+  const int64_t nh = n[3];
+  GRID_STRIDE(h, nh) {
+    const longlong2 d = dptr[hubs[h]];
+    w[h] = d.y - d.x;
+  }
+}
+
+template <class T>
+cudaError_t dalloc(T** p, int64_t n, cudaStream_t s) {
+  return cudaMallocAsync((void**)p, sizeof(T) * (size_t)(n > 0 ? n : 1), s);
+}
+
+#define TRY(x)                        \
+  do {                                \
+    cudaError_t _e = (x);             \
+    if (_e != cudaSuccess) return _e; \
+  } while (0)
+
+}  // namespace
+
+TaskLists TaskBuf::lists(bool with_log) const {
+  TaskLists t;
+  t.cta = cta;
+  t.warp = warp;
+  t.split_v = split_v;
+  t.split_off = split_off;
+  t.n = n;
+  if (with_log && log) {
+    t.log_cta = log;
+    t.log_warp = log + cap_v;
+    t.log_split = log + 2 * cap_v;
+  }
+  return t;
+}
+
+cudaError_t taskbuf_reserve(TaskBuf& tb, int64_t nv, cudaStream_t s) {
+  if (tb.cap_v >= nv && tb.cta) return cudaSuccess;
+  taskbuf_free(tb, s);
+  const int64_t c = nv > 0 ? nv : 1;
+  TRY(dalloc(&tb.cta, c, s));
+  TRY(dalloc(&tb.warp, c, s));
+  TRY(dalloc(&tb.split_v, c, s));
+  TRY(dalloc(&tb.split_off, c + 1, s));
+  TRY(dalloc(&tb.n, 4, s));
+  TRY(dalloc(&tb.var, c, s));
+  TRY(dalloc(&tb.flag, c, s));
+  TRY(dalloc(&tb.pos, c, s));
+  TRY(dalloc(&tb.w, c, s));
+  TRY(dalloc(&tb.cost, c, s));
+  TRY(dalloc(&tb.tmp, c, s));
+  tb.cap_v = c;
+  return cudaSuccess;
+}
+
+void taskbuf_free(TaskBuf& tb, cudaStream_t s) {
+  void* ps[] = {tb.cta, tb.warp, tb.split_v, tb.split_off, tb.n, tb.var, tb.flag,
+                tb.pos, tb.w,    tb.cost,    tb.tmp,       tb.log};
+  for (void* p : ps)
+    if (p) cudaFreeAsync(p, s);
+  tb = TaskBuf{};
+}
+
+cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int cta_max, TaskBuf& tb,
+                               cudaStream_t s) {
+  if (warp_max > kWarpCap) warp_max = kWarpCap;
+  if (cta_max > kCtaCap) cta_max = kCtaCap;
+  if (g.nv == 0) return cudaSuccess;
+  k_classify_heur<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, k - 1, warp_max, cta_max,
+                                                      tb.var);
+  return cudaGetLastError();
+}
+
+cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s) {
+  const int64_t nv = g.nv;
+  TRY(cudaMemsetAsync(tb.n, 0, 4 * sizeof(int64_t), s));
+  if (nv == 0) return cudaMemsetAsync(tb.split_off, 0, sizeof(int64_t), s);
+  if (!order) {
+    const uint8_t codes[3] = {VAR_CTA, VAR_WARP, VAR_SPLIT};
+    int32_t* outs[3] = {tb.cta, tb.warp, tb.split_v};
+    int64_t* cnts[3] = {tb.n + 1, tb.n + 2, tb.n + 3};
+    for (int x = 0; x < 3; ++x) {
+      k_flag_eq<<<grid_for(nv), kThreads, 0, s>>>(tb.var, nv, codes[x], tb.flag);
+      TRY(scan_excl(tb.flag, tb.pos, nv, cnts[x], s));
+      k_scatter<<<grid_for(nv), kThreads, 0, s>>>(tb.flag, tb.pos, nv, outs[x]);
+    }
+    // tb.pos still holds the hub positions (last pass)
+    k_hub_weights<<<grid_for(nv), kThreads, 0, s>>>(tb.var, g.dptr, nv, tb.w);
+    TRY(scan_excl(tb.w, tb.w, nv, tb.n + 0, s));
+    k_hub_offsets<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.pos, tb.w, nv, tb.split_off);
+  } else {
+    unsigned long long* hist = nullptr;
+    TRY(dalloc(&hist, 3 * kBins, s));
+    TRY(cudaMemsetAsync(hist, 0, 3 * kBins * sizeof(unsigned long long), s));
+    k_bin_hist<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.cost, nv, hist);
+    k_bin_scan<<<1, 32, 0, s>>>(hist, tb.n);
+    k_bin_scatter<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.cost, nv, hist, tb.warp, tb.cta,
+                                                    tb.split_v);
+    cudaFreeAsync(hist, s);
+    // hub offsets follow the ordered hub list (at most nv hubs; the unused tail of w
+    // is zero so the scan total is the number of hub sub-tasks)
+    TRY(cudaMemsetAsync(tb.w, 0, sizeof(int64_t) * nv, s));
+    k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, tb.w);
+    TRY(cudaGetLastError());
+    TRY(scan_excl(tb.w, tb.split_off, nv, tb.n + 0, s));
+  }
+  k_hub_tail<<<1, 1, 0, s>>>(tb.n, tb.split_off);
+  return cudaGetLastError();
+}
+
+}  // namespace xgm

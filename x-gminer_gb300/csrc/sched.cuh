@@ -1,0 +1,45 @@
+// Task generation and scheduling for the clique kernels (sched.cu).
+#pragma once
+#include "clique.cuh"
+#include "graph.cuh"
+
+namespace xgm {
+
+// Variant codes per vertex task (var[]).
+enum : uint8_t { VAR_WARP = 0, VAR_CTA = 1, VAR_SPLIT = 2, VAR_SKIP = 3 };
+
+// Device buffers of one schedule; sized for a graph's vertex count and reused.
+struct TaskBuf {
+  int64_t cap_v = 0;
+  int32_t* cta = nullptr;
+  int32_t* warp = nullptr;
+  int32_t* split_v = nullptr;
+  int64_t* split_off = nullptr;
+  int64_t* n = nullptr;       // [4] see TaskLists
+  uint8_t* var = nullptr;     // [cap_v] variant per vertex
+  uint8_t* flag = nullptr;    // [cap_v] scratch
+  int64_t* pos = nullptr;     // [cap_v] scratch
+  int64_t* w = nullptr;       // [cap_v] scratch
+  float* cost = nullptr;      // [cap_v] predicted log-cost (learned policy)
+  int32_t* tmp = nullptr;     // [cap_v] scratch for ordering
+  long long* log = nullptr;   // [3 * cap_v + split cap] per-task timing log (optional)
+  int64_t log_cap = 0;
+
+  TaskLists lists(bool with_log) const;
+};
+
+cudaError_t taskbuf_reserve(TaskBuf& tb, int64_t nv, cudaStream_t s);
+void taskbuf_free(TaskBuf& tb, cudaStream_t s);
+
+// Plain degree-threshold heuristic (the role of WARP_LIMIT / BLOCK_LIMIT,
+// xgminer/include/glumin/common.h:114-116, and the |W| <= 32 switch of
+// clique5_warp_edge_taskallocate.cuh:26): out-degree s < k-1 -> skip,
+// s <= warp_max -> WARP, s <= cta_max -> CTA, else SPLIT.  Lists keep vertex order.
+cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int cta_max, TaskBuf& tb,
+                               cudaStream_t s);
+
+// Compacts tb.var into the task lists.  With `order` (learned policy) each list is
+// ordered by descending tb.cost (binned), heaviest predicted tasks first.
+cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s);
+
+}  // namespace xgm
