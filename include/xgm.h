@@ -114,6 +114,7 @@ enum { XGM_VIEW_UNDIRECTED = 0, XGM_VIEW_DAG = 1 };
 /* Copies a CSR view back to host arrays sized from xgm_graph_info (original ids). */
 xgm_status xgm_graph_download(xgm_ctx* ctx, const xgm_graph* g, int view, int64_t* rowptr,
                               int32_t* colidx);
+/* Graphs (and models) must be destroyed before the context they were created on. */
 void xgm_graph_destroy(xgm_graph* g);
 
 /* Host-side file helpers in the reference layout. */

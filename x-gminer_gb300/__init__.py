@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from typing import Optional, Tuple
 
 import numpy as np
@@ -164,9 +165,18 @@ class Context:
         st = lib().xgm_create(C.byref(h), C.cast(cfg, C.c_void_p))
         _check(st)
         self._h = h
+        # graphs and models of this context; the C ABI requires them to be destroyed
+        # before the context, so close() releases them first
+        self._children: "weakref.WeakSet" = weakref.WeakSet()
+
+    def _adopt(self, obj):
+        self._children.add(obj)
+        return obj
 
     def close(self) -> None:
         if self._h:
+            for child in list(self._children):
+                child.close()
             lib().xgm_destroy(self._h)
             self._h = None
 
@@ -190,7 +200,7 @@ class Context:
         h = C.c_void_p()
         _check(lib().xgm_graph_build_from_edges(self._h, int(num_vertices), _ptr(src), _ptr(dst),
                                                  len(src), flags, C.byref(h)), self)
-        return Graph(self, h)
+        return self._adopt(Graph(self, h))
 
     def graph_from_csr(self, rowptr: np.ndarray, colidx: np.ndarray, flags: int = 0) -> "Graph":
         rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
@@ -198,12 +208,12 @@ class Context:
         csr = CsrHost(len(rowptr) - 1, len(colidx), _ptr(rowptr), _ptr(colidx) if len(colidx) else 0)
         h = C.c_void_p()
         _check(lib().xgm_graph_upload(self._h, C.byref(csr), flags, C.byref(h)), self)
-        return Graph(self, h)
+        return self._adopt(Graph(self, h))
 
     def load_graph(self, prefix: str, flags: int = 0) -> "Graph":
         h = C.c_void_p()
         _check(lib().xgm_graph_load(self._h, prefix.encode(), flags, C.byref(h)), self)
-        return Graph(self, h)
+        return self._adopt(Graph(self, h))
 
     # plans / counting -----------------------------------------------------
     def plan(self, pattern) -> "Plan":
@@ -295,9 +305,9 @@ class Graph:
         return rowptr, col[: int(rowptr[-1])]
 
     def close(self) -> None:
-        if self._h:
+        if self._h and self.ctx._h:
             lib().xgm_graph_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -314,6 +324,12 @@ class Model:
         h = C.c_void_p()
         _check(lib().xgm_model_create(ctx._h, seed, C.byref(h)), ctx)
         self._h = h
+        ctx._adopt(self)
+
+    def close(self) -> None:
+        if self._h and self.ctx._h:
+            lib().xgm_model_destroy(self._h)
+        self._h = None
 
     def params(self) -> np.ndarray:
         p = np.empty(MODEL_PARAMS, dtype=np.float32)
@@ -361,9 +377,7 @@ class Model:
 
     def __del__(self):
         try:
-            if self._h:
-                lib().xgm_model_destroy(self._h)
-                self._h = None
+            self.close()
         except Exception:
             pass
 

@@ -105,7 +105,9 @@ __device__ void cta_scan_lengths(int32_t* pre, int n, int32_t* warp_tot) {
 // Kernel modes: plain count; triangle participation (per-vertex / per-edge triangle
 // counts for the motif plans); count weighted by the out-degree of each clique's
 // highest-ranked vertex (the plan's algorithmic-bytes term).
-enum { kModeCount = 0, kModePart = 1, kModeWeight = 2 };
+// kModeMulti (K == 4, batched graphs) counts triangles and 4-cliques of every task in
+// one pass and credits triangle participation too.
+enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 
 // Count of (q)-cliques in the local DAG held by the CTA (q >= 3 uses the bitmap).  WGT
 // (Q == 3 only) weights each clique by d+ of its top member, d+(S[l]) = pre[l+1]-pre[l].
@@ -174,8 +176,10 @@ struct Part {
 // vertices S[i], S[j] and edges (root,S[i]), (root,S[j]), (S[i],S[j]).  The root's own
 // credit is the returned count.
 template <int Q, int MODE>
-__device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long long sbase) {
-  constexpr bool PART = MODE == kModePart;
+__device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long long sbase,
+                              uint64_t* q2out = nullptr) {
+  constexpr bool MULTI = MODE == kModeMulti;  // Q == 3: also local edges + participation
+  constexpr bool PART = MODE == kModePart || MULTI;
   constexpr bool WGT = MODE == kModeWeight;
   int32_t* S = (int32_t*)(sm + kOffS);
   if (Q == 1) {
@@ -217,7 +221,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   cta_scan_lengths(pre, s, wtot);  // ends with __syncthreads
   const int total = pre[s];
   const int32_t smax = S[s - 1];
-  uint64_t acc = 0;
+  uint64_t acc = 0, q2 = 0;
   // Flattened walk over all (i, element) pairs: warp chunks of 256 consecutive
   // elements, lanes contiguous within a chunk so row reads are coalesced.
   for (int c = warp; c * 256 < total; c += kCtaWarps) {
@@ -248,11 +252,18 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
             }
           } else {
             atomicOr(&rows[tri_row_off(i, W) + (j >> 5) - (i >> 5)], 1u << (j & 31));
+            if (MULTI) {
+              q2 += 1;
+              atomicAdd(&cnt[i], 1u);
+              atomicAdd(&cnt[j], 1u);
+              atomicAdd(&part.e[lb[i] + (k - pre[i])], 1u);
+            }
           }
         }
       }
     }
   }
+  if (MULTI) *q2out = q2;
   __syncthreads();
   if (PART) {
     for (int i = tid; i < s; i += kCtaThreads)
@@ -269,7 +280,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
 // CTA-wide ordered intersection N+(v0) & N+(v1) into S; returns its size or -1 when it
 // exceeds kCtaCap.  Members of N+(v1) are binary-searched in N+(v0) (global, sorted).
 // PART credits the triangles (v0, v1, w): edges (v1, w) and (v0, w) and vertex w.
-template <bool PART>
+template <bool PART, bool STORE>
 __device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_t v1, Part part) {
   int32_t* S = (int32_t*)(sm + kOffS);
   int32_t* wtot = (int32_t*)(sm + kOffMisc);
@@ -302,11 +313,11 @@ __device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_
     int tot = 0;
     for (int w = 0; w < kCtaWarps; ++w) tot += wtot[w];
     const int pos = off + __popc(bal & lanemask_lt());
-    if (!PART && found && pos < kCtaCap) S[pos] = y;
+    if (STORE && found && pos < kCtaCap) S[pos] = y;
     n += tot;
     __syncthreads();
   }
-  return (PART || n <= kCtaCap) ? n : -1;
+  return (!STORE || n <= kCtaCap) ? n : -1;
 }
 
 // --------------------------------------------------------------- warp tier
@@ -321,9 +332,11 @@ __device__ __forceinline__ int warp_bsearch(const int32_t* S, int s, int32_t x) 
 
 // One warp, local set S = N+(v0) with s <= 32: Q-cliques of the local DAG.
 template <int Q, int MODE>
-__device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Part part) {
+__device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Part part,
+                                     uint64_t* q2out = nullptr) {
   static_assert(Q >= 2, "warp tasks count at least local edges");
-  constexpr bool PART = MODE == kModePart;
+  constexpr bool MULTI = MODE == kModeMulti;
+  constexpr bool PART = MODE == kModePart || MULTI;
   constexpr bool WGT = MODE == kModeWeight;
   const int lane = threadIdx.x & 31;
   const longlong2 d0 = ldg_ll2(g.dptr + v0);
@@ -349,7 +362,7 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   __syncwarp();  // pre[s] is the total: lanes >= s contributed length 0
   const int total = w.pre[s];
   const int32_t smax = w.S[s - 1];
-  uint64_t acc = 0;
+  uint64_t acc = 0, q2 = 0;
   int i = 0;
   for (int k = lane; k < total; k += 32) {
     while (w.pre[i + 1] <= k) ++i;
@@ -366,10 +379,17 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
           }
         } else {
           atomicOr(&w.rows[i], 1u << j);
+          if (MULTI) {
+            q2 += 1;
+            atomicAdd(&w.cnt[i], 1u);
+            atomicAdd(&w.cnt[j], 1u);
+            atomicAdd(&part.e[w.lb[i] + (k - w.pre[i])], 1u);
+          }
         }
       }
     }
   }
+  if (MULTI) *q2out = q2;
   __syncwarp();
   if (PART && lane < s && w.cnt[lane]) {
     atomicAdd(&part.v[w.S[lane]], (unsigned long long)w.cnt[lane]);
@@ -408,14 +428,34 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
 }
 
 // ------------------------------------------------------------ persistent kernel
-// K = clique size (3, 4, 5).  MODE kModePart (K == 3 only) credits triangle
-// participation to `part` instead of counting; kModeWeight (K <= 4) weights each clique
-// by the out-degree of its highest-ranked vertex.
+// Per-task emission: one global total (gid == null) or per-graph totals
+// out[gid[v0] * stride + slot] (batched graphs).  Called by all 32 lanes of a warp.
+__device__ __forceinline__ void emit(const GOut& o, int32_t v0, uint64_t r, uint64_t r2,
+                                     uint64_t& acc) {
+  if (o.gid) {
+    const uint64_t a = warp_sum_u64(r), b = warp_sum_u64(r2);
+    if ((threadIdx.x & 31) == 0) {
+      const long long base = (long long)o.gid[v0] * o.stride;
+      if (a && o.slot >= 0) atomicAdd(&o.out[base + o.slot], (unsigned long long)a);
+      if (b && o.slot2 >= 0) atomicAdd(&o.out[base + o.slot2], (unsigned long long)b);
+    }
+  } else {
+    acc += r;
+  }
+}
+
+// K = clique size (3, 4, 5).  MODE kModePart (K == 3) credits triangle participation to
+// `part` instead of counting; kModeWeight (K <= 4) weights each clique by the out-degree
+// of its highest-ranked vertex; kModeMulti (K == 4) emits triangles to o.slot and
+// 4-cliques to o.slot2 and credits participation.
 template <int K, int MODE>
 __global__ void __launch_bounds__(kCtaThreads, 2)
     k_clique(GView g, TaskLists t, QueueHeads* q, unsigned long long* count, uint32_t* err,
-             Part part) {
-  constexpr bool PART = MODE == kModePart;
+             Part part, GOut o) {
+  constexpr bool MULTI = MODE == kModeMulti;
+  constexpr bool PART = MODE == kModePart || MULTI;
+  constexpr int kMinS = MULTI ? 2 : K - 1;  // smallest out-degree that can contribute
+  static_assert(!MULTI || K == 4, "multi mode runs the 4-clique machinery");
   extern __shared__ __align__(16) char sm[];
   __shared__ long long task_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -439,21 +479,23 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
     const longlong2 d0 = ldg_ll2(g.dptr + v0);
     const long long e01 = d0.x + (ti - t.split_off[lo]);
     const int32_t v1 = ldg_i32(g.col + e01);
-    const int n = cta_intersect_into_S<PART>(g, sm, v0, v1, part);
+    const int n = cta_intersect_into_S<PART, !(MODE == kModePart)>(g, sm, v0, v1, part);
     if (n < 0) {
       if (tid == 0) atomicOr(err, ERR_CAPACITY);
-    } else if (PART) {
-      if (tid == 0 && n > 0) {
+    } else {
+      if (PART && tid == 0 && n > 0) {
+        // triangles (v0, v1, w) for every w of the intersection
         atomicAdd(&part.v[v0], (unsigned long long)n);
         atomicAdd(&part.v[v1], (unsigned long long)n);
         atomicAdd(&part.e[e01], (unsigned)n);
       }
-    } else if (n > 0) {
-      uint64_t r = cta_local<K - 2, (PART ? kModeCount : MODE)>(g, sm, n, part, -1);
-      if (K - 2 == 1 && MODE != kModeWeight) {
-        if (tid == 0) acc += r;  // Q == 1 returns n from every thread; count it once
-      } else {
-        acc += r;
+      if (MULTI) {
+        const uint64_t k4 = n >= 2 ? cta_local<2, kModeCount>(g, sm, n, part, -1) : 0;
+        emit(o, v0, tid == 0 ? (uint64_t)n : 0, k4, acc);
+      } else if (!PART && n > 0) {
+        uint64_t r = cta_local<K - 2, MODE>(g, sm, n, part, -1);
+        if (K - 2 == 1 && MODE != kModeWeight) r = tid == 0 ? r : 0;  // same n in all threads
+        if (MODE == kModeWeight) acc += r; else emit(o, v0, r, 0, acc);
       }
     }
     __syncthreads();
@@ -472,18 +514,20 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
     const int s = (int)(d0.y - d0.x);
     if (s > kCtaCap) {
       if (tid == 0) atomicOr(err, ERR_CAPACITY);
-    } else if (s >= K - 1) {
+    } else if (s >= kMinS) {
       int32_t* S = (int32_t*)(sm + kOffS);
       for (int i = tid; i < s; i += kCtaThreads) S[i] = ldg_i32(g.col + d0.x + i);
       __syncthreads();
-      uint64_t r = cta_local<K - 1, MODE>(g, sm, s, part, d0.x);
+      uint64_t q2 = 0;
+      const uint64_t r = cta_local<K - 1, MODE>(g, sm, s, part, d0.x, &q2);
       if (PART) {
         // every local edge is a triangle containing v0
-        uint64_t tot = warp_sum_u64(r);
+        const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
         if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
-      } else {
-        acc += r;
       }
+      if (MULTI) emit(o, v0, q2, r, acc);
+      else if (MODE == kModeWeight) acc += r;
+      else if (!PART) emit(o, v0, r, 0, acc);
     }
     __syncthreads();
     if (t.log_cta && tid == 0) t.log_cta[ti] = clock64() - c0;
@@ -501,18 +545,20 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
     const int s = (int)(d0.y - d0.x);
     if (s > kWarpCap) {
       if (lane == 0) atomicOr(err, ERR_CAPACITY);
-    } else if (s >= K - 1) {
-      uint64_t r = warp_vertex_task<K - 1, MODE>(g, ws, v0, part);
+    } else if (s >= kMinS) {
+      uint64_t q2 = 0;
+      const uint64_t r = warp_vertex_task<K - 1, MODE>(g, ws, v0, part, &q2);
       if (PART) {
-        uint64_t tot = warp_sum_u64(r);
+        const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
         if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
-      } else {
-        acc += r;
       }
+      if (MULTI) emit(o, v0, q2, r, acc);
+      else if (MODE == kModeWeight) acc += r;
+      else if (!PART) emit(o, v0, r, 0, acc);
     }
     if (t.log_warp && lane == 0) t.log_warp[ti] = clock64() - c0;
   }
-  if (!PART) {
+  if (!PART && count) {
     acc = warp_sum_u64(acc);
     if (lane == 0 && acc) atomicAdd(count, (unsigned long long)acc);
   }
@@ -520,7 +566,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
 
 template <int K, int MODE>
 cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned long long* count,
-                     uint32_t* err, Part part, int grid, cudaStream_t s) {
+                     uint32_t* err, Part part, int grid, cudaStream_t s, GOut o = GOut{}) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(k_clique<K, MODE>,
@@ -528,7 +574,7 @@ cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_clique<K, MODE><<<grid, kCtaThreads, kCtaSmem, s>>>(g, t, q, count, err, part);
+  k_clique<K, MODE><<<grid, kCtaThreads, kCtaSmem, s>>>(g, t, q, count, err, part, o);
   return cudaGetLastError();
 }
 
@@ -547,14 +593,21 @@ cudaError_t clique_occupancy(int* per_sm) {
 int clique_grid(int num_sms) { return 2 * num_sms; }
 
 cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads* q,
-                          unsigned long long* count, uint32_t* err, int grid, cudaStream_t s) {
+                          unsigned long long* count, uint32_t* err, int grid, cudaStream_t s,
+                          const GOut& o) {
   const Part none{nullptr, nullptr};
   switch (k) {
-    case 3: return launch_k<3, kModeCount>(g, t, q, count, err, none, grid, s);
-    case 4: return launch_k<4, kModeCount>(g, t, q, count, err, none, grid, s);
-    case 5: return launch_k<5, kModeCount>(g, t, q, count, err, none, grid, s);
+    case 3: return launch_k<3, kModeCount>(g, t, q, count, err, none, grid, s, o);
+    case 4: return launch_k<4, kModeCount>(g, t, q, count, err, none, grid, s, o);
+    case 5: return launch_k<5, kModeCount>(g, t, q, count, err, none, grid, s, o);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_multi(const GView& g, const TaskLists& t, QueueHeads* q,
+                         unsigned long long* vpart, unsigned* epart, uint32_t* err, int grid,
+                         cudaStream_t s, const GOut& o) {
+  return launch_k<4, kModeMulti>(g, t, q, nullptr, err, Part{vpart, epart}, grid, s, o);
 }
 
 cudaError_t launch_clique_weighted(int k, const GView& g, const TaskLists& t, QueueHeads* q,

@@ -28,6 +28,16 @@ struct TaskLists {
   long long* log_split = nullptr;
 };
 
+// Per-graph outputs of batched launches: task totals go to out[gid[v0] * stride + slot]
+// (and slot2 in multi mode).  gid == null: one global total.
+struct GOut {
+  const int32_t* gid = nullptr;
+  unsigned long long* out = nullptr;
+  int stride = 0;
+  int slot = 0;
+  int slot2 = -1;
+};
+
 // Work-queue heads, zeroed before each launch.
 struct QueueHeads {
   unsigned long long split, cta, warp, pad;
@@ -39,7 +49,15 @@ cudaError_t clique_occupancy(int* per_sm);
 
 // k in {3, 4, 5}: adds the k-clique count of g (DAG) over the listed tasks to *count.
 cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads* q,
-                          unsigned long long* count, uint32_t* err, int grid, cudaStream_t s);
+                          unsigned long long* count, uint32_t* err, int grid, cudaStream_t s,
+                          const GOut& o = GOut{});
+
+// Batched multi-pattern launch (4-clique machinery): per task, triangles -> o.slot,
+// 4-cliques -> o.slot2 (-1: none), and triangle participation into vpart / epart.
+// Tasks must be classified with k = 3 so out-degree-2 roots are included.
+cudaError_t launch_multi(const GView& g, const TaskLists& t, QueueHeads* q,
+                         unsigned long long* vpart, unsigned* epart, uint32_t* err, int grid,
+                         cudaStream_t s, const GOut& o);
 
 // Triangle participation from the same task lists run with k = 3: every triangle adds
 // 1 to vpart[] of its three vertices and 1 to epart[] of its three edges (edge = index
