@@ -200,12 +200,17 @@ def cpu_sample(orc, kind: str, drow, dcol, budget_s: float):
     with the stride picked from a short calibration so the sample takes ~budget_s."""
     nv = len(drow) - 1
     cores = orc.threads()
-    stride = 1 << 12
-    t0 = time.perf_counter()
-    orc.count(kind, drow, dcol, 0, nv, stride)
-    t_cal = max(time.perf_counter() - t0, 1e-3)
-    est_full = t_cal * stride
-    stride = max(1, int(est_full / budget_s))
+    # shrink the stride until a sample takes an eighth of the budget, then scale it so
+    # the timed sample takes about budget_s (time grows ~ 1 / stride)
+    stride = 1 << 16
+    while True:
+        t0 = time.perf_counter()
+        orc.count(kind, drow, dcol, 0, nv, stride)
+        t_cal = time.perf_counter() - t0
+        if t_cal >= budget_s / 8 or stride == 1:
+            break
+        stride = max(1, stride // (4 if t_cal < budget_s / 64 else 2))
+    stride = max(1, int(round(stride * t_cal / budget_s)))
     t0 = time.perf_counter()
     c = orc.count(kind, drow, dcol, 0, nv, stride)
     dt = time.perf_counter() - t0

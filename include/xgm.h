@@ -151,7 +151,8 @@ void xgm_plan_destroy(xgm_plan* p);
 typedef enum {
   XGM_SCHED_HEURISTIC = 0, /* degree-threshold split (common.h:114-116 analogue) */
   XGM_SCHED_LEARNED = 1,   /* MLP cost model picks variant + order; needs a model */
-  XGM_SCHED_FIXED = 2      /* force `variant` for every task (tuning / logging) */
+  XGM_SCHED_FIXED = 2,     /* force `variant` for every task (tuning / logging) */
+  XGM_SCHED_TUNED = 3      /* per out-degree bucket variant table from xgm_autotune */
 } xgm_sched_policy;
 
 /* Kernel variants a task can run with. */
@@ -162,6 +163,14 @@ typedef enum {
   XGM_NUM_VARIANTS = 3
 } xgm_variant;
 
+/* Autotuned schedule: the variant for each out-degree bucket.  Bucket b holds
+ * out-degrees s with floor(log2(s)) == b - 1 (bucket 0: s == 0), the last bucket
+ * everything above.  A variant that cannot hold a task falls back by capacity. */
+#define XGM_TUNE_BUCKETS 16
+typedef struct {
+  uint8_t variant[XGM_TUNE_BUCKETS];
+} xgm_tune_table;
+
 typedef struct {
   int policy;             /* xgm_sched_policy */
   int variant;            /* for XGM_SCHED_FIXED */
@@ -169,7 +178,11 @@ typedef struct {
   int warp_max;           /* heuristic: out-degree <= warp_max -> WARP (0: default) */
   int cta_max;            /* heuristic: out-degree <= cta_max -> CTA, else SPLIT (0: default) */
   int order_by_cost;      /* learned: 1 = heaviest predicted tasks first */
+  const xgm_tune_table* table; /* for XGM_SCHED_TUNED */
+  int flags;              /* XGM_SCHED_NO_GRAPH: batched calls launch directly, no CUDA graph */
 } xgm_sched;
+
+enum { XGM_SCHED_NO_GRAPH = 1 };
 
 typedef struct {
   double kernel_ms;        /* device time of the counting launch(es) */
@@ -201,6 +214,44 @@ xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
  * graph; 4 B per int32 element + 8 B per task), used as the roofline numerator. */
 xgm_status xgm_algo_bytes(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
                           uint64_t* bytes);
+
+/* ----------------------------------------------------------------- autotuner */
+/* Empirical search of the per-bucket variant table for `plan` on g (or on a batch when
+ * g is NULL and b is set): coordinate descent over buckets, each candidate timed as
+ * the median of `reps` counts; the counts are checked equal to the first.  `best_ms` /
+ * `heuristic_ms` report the tuned and plain per-call times.  No counterpart in the
+ * reference (its thresholds are compile-time constants, common.h:114-116). */
+typedef struct {
+  xgm_tune_table table;
+  double best_ms;
+  double heuristic_ms;
+  int trials;
+} xgm_tune_result;
+xgm_status xgm_autotune(xgm_ctx* ctx, const xgm_graph* g, xgm_batch* b, const xgm_plan* const* plans,
+                        int n_plans, int reps, xgm_tune_result* out);
+
+/* ------------------------------------------------------------------- batches */
+/* Many small graphs counted together.  Graph i owns vertices [vtx_off[i], vtx_off[i+1])
+ * of one packed id space; edge samples (or CSR entries) use those global ids and never
+ * cross graphs.  The reference counts one graph per process run (GLUMIN::run,
+ * xgminer/include/glumin.h:56); this is the batched form of that call. */
+xgm_status xgm_batch_build_from_edges(xgm_ctx* ctx, int num_graphs, const int64_t* vtx_off,
+                                      const int32_t* src, const int32_t* dst,
+                                      int64_t num_samples, int flags, xgm_batch** out);
+xgm_status xgm_batch_upload(xgm_ctx* ctx, int num_graphs, const int64_t* vtx_off,
+                            const xgm_csr_host* csr, int flags, xgm_batch** out);
+int xgm_batch_num_graphs(const xgm_batch* b);
+/* The batch's packed graph (for xgm_graph_download / xgm_graph_info_get); owned by b. */
+const xgm_graph* xgm_batch_graph(const xgm_batch* b);
+/* Counts every plan on every graph of the batch: out[i * n_plans + p].  Triangle,
+ * 4-clique, diamond and tailed-triangle plans run in one persistent launch (plus a
+ * per-graph reduction); 5-clique and 4-cycle add one launch each.  The device work is
+ * captured into a CUDA graph on the first call for a (plan set, schedule) and replayed
+ * afterwards, unless sched->flags has XGM_SCHED_NO_GRAPH. */
+xgm_status xgm_count_batched(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const* plans,
+                             int n_plans, const xgm_sched* sched, uint64_t* out,
+                             xgm_stats* stats);
+void xgm_batch_destroy(xgm_batch* b);
 
 /* -------------------------------------------------------------- cost model */
 /* Learned scheduler: a 12 -> 32 (ReLU) -> 1 MLP with fp16 weights and fp32

@@ -39,7 +39,9 @@ PATTERN_NAMES = {"triangle": TRIANGLE, "4-clique": CLIQUE4, "5-clique": CLIQUE5,
                  "diamond": DIAMOND, "rectangle": CYCLE4, "4-cycle": CYCLE4,
                  "tailedtriangle": TAILED_TRIANGLE}
 
-SCHED_HEURISTIC, SCHED_LEARNED, SCHED_FIXED = 0, 1, 2
+SCHED_HEURISTIC, SCHED_LEARNED, SCHED_FIXED, SCHED_TUNED = 0, 1, 2, 3
+SCHED_NO_GRAPH = 1
+TUNE_BUCKETS = 16
 VAR_WARP, VAR_CTA, VAR_SPLIT = 0, 1, 2
 
 MODEL_FEATURES, MODEL_HIDDEN = 12, 32
@@ -69,9 +71,19 @@ class PlanDesc(C.Structure):
                 ("adj", (C.c_uint8 * 8) * 8), ("induced", C.c_int)]
 
 
+class TuneTable(C.Structure):
+    _fields_ = [("variant", C.c_uint8 * 16)]
+
+
 class Sched(C.Structure):
     _fields_ = [("policy", C.c_int), ("variant", C.c_int), ("model", C.c_void_p),
-                ("warp_max", C.c_int), ("cta_max", C.c_int), ("order_by_cost", C.c_int)]
+                ("warp_max", C.c_int), ("cta_max", C.c_int), ("order_by_cost", C.c_int),
+                ("table", C.c_void_p), ("flags", C.c_int)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("table", TuneTable), ("best_ms", C.c_double), ("heuristic_ms", C.c_double),
+                ("trials", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -110,6 +122,13 @@ _SIGS = [
     ("xgm_clique_solver", _I, [_P, _P, _I, C.POINTER(_U64)]),
     ("xgm_sc_solver", _I, [_P, _P, C.c_char_p, C.POINTER(_U64)]),
     ("xgm_algo_bytes", _I, [_P, _P, _P, C.POINTER(_U64)]),
+    ("xgm_autotune", _I, [_P, _P, _P, _P, _I, _I, C.POINTER(TuneResult)]),
+    ("xgm_batch_build_from_edges", _I, [_P, _I, _P, _P, _P, _I64, _I, C.POINTER(_P)]),
+    ("xgm_batch_upload", _I, [_P, _I, _P, C.POINTER(CsrHost), _I, C.POINTER(_P)]),
+    ("xgm_batch_num_graphs", _I, [_P]),
+    ("xgm_batch_graph", _P, [_P]),
+    ("xgm_count_batched", _I, [_P, _P, _P, _I, C.POINTER(Sched), _P, C.POINTER(Stats)]),
+    ("xgm_batch_destroy", None, [_P]),
     ("xgm_model_create", _I, [_P, _U64, C.POINTER(_P)]),
     ("xgm_model_destroy", None, [_P]),
     ("xgm_model_set_params", _I, [_P, _P]),
@@ -235,12 +254,21 @@ class Context:
             _check(lib().xgm_plan_compile(self._h, C.byref(d), C.byref(h)), self)
         return Plan(h)
 
+    @staticmethod
+    def _sched(policy=SCHED_HEURISTIC, variant=0, model=None, warp_max=0, cta_max=0,
+               order_by_cost=1, table=None, flags=0):
+        sp = Sched(policy, variant, model._h if model is not None else None, warp_max, cta_max,
+                   order_by_cost, C.cast(C.pointer(table), C.c_void_p) if table is not None
+                   else None, flags)
+        sp._keep = table  # keep the table alive with the struct
+        return sp
+
     def count(self, graph: "Graph", pattern, policy: int = SCHED_HEURISTIC, variant: int = 0,
               model: Optional["Model"] = None, warp_max: int = 0, cta_max: int = 0,
-              order_by_cost: int = 1, with_stats: bool = False):
+              order_by_cost: int = 1, table: Optional[TuneTable] = None,
+              with_stats: bool = False):
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
-        sp = Sched(policy, variant, model._h if model is not None else None, warp_max, cta_max,
-                   order_by_cost)
+        sp = self._sched(policy, variant, model, warp_max, cta_max, order_by_cost, table)
         out = C.c_uint64()
         st = Stats()
         _check(lib().xgm_count(self._h, graph._h, plan._h, C.byref(sp), C.byref(out),
@@ -250,10 +278,63 @@ class Context:
     def count_kernels(self, graph: "Graph", pattern, policy: int = SCHED_HEURISTIC,
                       model: Optional["Model"] = None, order_by_cost: int = 1) -> int:
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
-        sp = Sched(policy, 0, model._h if model is not None else None, 0, 0, order_by_cost)
+        sp = self._sched(policy, 0, model, 0, 0, order_by_cost)
         n = C.c_int()
         _check(lib().xgm_count_kernels(self._h, graph._h, plan._h, C.byref(sp), C.byref(n)), self)
         return int(n.value)
+
+    # batches --------------------------------------------------------------
+    def batch_from_edges(self, vtx_off: np.ndarray, src: np.ndarray, dst: np.ndarray,
+                         flags: int = BUILD_CLEAN) -> "Batch":
+        vtx_off = np.ascontiguousarray(vtx_off, dtype=np.int64)
+        src = np.ascontiguousarray(src, dtype=np.int32)
+        dst = np.ascontiguousarray(dst, dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().xgm_batch_build_from_edges(self._h, len(vtx_off) - 1, _ptr(vtx_off),
+                                                 _ptr(src), _ptr(dst), len(src), flags,
+                                                 C.byref(h)), self)
+        return self._adopt(Batch(self, h))
+
+    def batch_from_csr(self, vtx_off: np.ndarray, rowptr: np.ndarray, colidx: np.ndarray,
+                       flags: int = 0) -> "Batch":
+        vtx_off = np.ascontiguousarray(vtx_off, dtype=np.int64)
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        colidx = np.ascontiguousarray(colidx, dtype=np.int32)
+        csr = CsrHost(len(rowptr) - 1, len(colidx), _ptr(rowptr), _ptr(colidx) if len(colidx) else 0)
+        h = C.c_void_p()
+        _check(lib().xgm_batch_upload(self._h, len(vtx_off) - 1, _ptr(vtx_off), C.byref(csr),
+                                      flags, C.byref(h)), self)
+        return self._adopt(Batch(self, h))
+
+    def count_batched(self, batch: "Batch", patterns, policy: int = SCHED_HEURISTIC,
+                      model: Optional["Model"] = None, table: Optional[TuneTable] = None,
+                      use_graph: bool = True, order_by_cost: int = 1, with_stats: bool = False):
+        plans = [p if isinstance(p, Plan) else self.plan(p) for p in patterns]
+        arr = (C.c_void_p * len(plans))(*[p._h.value for p in plans])
+        sp = self._sched(policy, 0, model, 0, 0, order_by_cost, table,
+                         0 if use_graph else SCHED_NO_GRAPH)
+        out = np.empty(batch.num_graphs * len(plans), dtype=np.uint64)
+        st = Stats()
+        _check(lib().xgm_count_batched(self._h, batch._h, C.cast(arr, C.c_void_p), len(plans),
+                                       C.byref(sp), _ptr(out), C.byref(st)), self)
+        res = out.reshape(batch.num_graphs, len(plans))
+        return (res, st.as_dict()) if with_stats else res
+
+    def autotune(self, target, patterns, reps: int = 3) -> dict:
+        """Per out-degree bucket variant table for a graph (one pattern) or a batch."""
+        if isinstance(patterns, (str, int, Plan)):
+            patterns = [patterns]
+        plans = [p if isinstance(p, Plan) else self.plan(p) for p in patterns]
+        arr = (C.c_void_p * len(plans))(*[p._h.value for p in plans])
+        res = TuneResult()
+        g = target._h if isinstance(target, Graph) else None
+        b = target._h if isinstance(target, Batch) else None
+        _check(lib().xgm_autotune(self._h, g, b, C.cast(arr, C.c_void_p), len(plans), reps,
+                                  C.byref(res)), self)
+        table = TuneTable()
+        C.memmove(C.byref(table), C.byref(res.table), C.sizeof(TuneTable))
+        return {"table": table, "variants": list(res.table.variant), "best_ms": res.best_ms,
+                "heuristic_ms": res.heuristic_ms, "trials": res.trials}
 
     def algo_bytes(self, graph: "Graph", pattern) -> int:
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
@@ -307,6 +388,36 @@ class Graph:
     def close(self) -> None:
         if self._h and self.ctx._h:
             lib().xgm_graph_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many small graphs in one packed id space (graph i owns [vtx_off[i], vtx_off[i+1]))."""
+
+    def __init__(self, ctx: Context, h):
+        self.ctx = ctx
+        self._h = h
+        self.num_graphs = lib().xgm_batch_num_graphs(h)
+
+    def download(self):
+        """Packed undirected CSR (global ids)."""
+        gh = lib().xgm_batch_graph(self._h)
+        view = Graph.__new__(Graph)
+        view.ctx, view._h = self.ctx, C.c_void_p(gh)
+        try:
+            return view.download()
+        finally:
+            view._h = None  # owned by the batch
+
+    def close(self) -> None:
+        if self._h and self.ctx._h:
+            lib().xgm_batch_destroy(self._h)
         self._h = None
 
     def __del__(self):

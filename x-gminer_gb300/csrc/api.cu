@@ -70,7 +70,7 @@ xgm_status ctx_sync_scalars(xgm_ctx* ctx) {
 }
 
 xgm_status graph_finish_common(xgm_ctx* ctx, DevGraph& g) {
-  XGM_CUDA_TRY(finish_graph(g, nullptr, ctx->stream));
+  XGM_CUDA_TRY(finish_graph(g, nullptr, 0, ctx->stream));
   XGM_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return XGM_OK;
 }

@@ -72,6 +72,9 @@ xgm_status algo_bytes_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, uin
 xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
                          int* n_kernels);
 void motif_buffers_free(xgm_ctx* ctx);
+xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
+                         cudaStream_t s);
+int ensure_clique_grid(xgm_ctx* ctx);
 int match_pattern(const xgm_plan_desc* d);  // builtin id, 0 unsupported, -1 malformed
 int pattern_from_name(const char* name);
 

@@ -44,6 +44,7 @@ constexpr int kOffRows = kOffCnt + 4 * kCtaCap;
 constexpr int kRowsWords = 16896;  // tri_words(1024)
 constexpr int kOffMisc = kOffRows + 4 * kRowsWords;
 constexpr int kCtaSmem = kOffMisc + 8 * 16;
+constexpr int kClipMin = 96;  // lists longer than this are clipped at max(S)
 
 // Warp region: one per warp, aliased over the CTA region once the CTA queues drain.
 struct WarpSmem {
@@ -206,10 +207,21 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
     for (int x = tid; x < tri_words(s); x += kCtaThreads) rows[x] = 0u;
   if (PART)
     for (int i = tid; i < s; i += kCtaThreads) cnt[i] = 0u;
+  // Only members <= max(S) can hit: clip long lists at max(S) (binary search in the
+  // sorted global row) so the walk streams no element that cannot match.
+  const int32_t smax0 = S[s - 1];
   for (int i = tid; i < s; i += kCtaThreads) {
-    longlong2 d = ldg_ll2(g.dptr + S[i]);
+    const longlong2 d = ldg_ll2(g.dptr + S[i]);
+    long long hi = d.y;
+    if (d.y - d.x > kClipMin && ldg_i32(g.col + d.y - 1) > smax0) {
+      long long lo = d.x;
+      while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (ldg_i32(g.col + mid) <= smax0) lo = mid + 1; else hi = mid;
+      }
+    }
     lb[i] = d.x;
-    pre[i] = (int32_t)(d.y - d.x);
+    pre[i] = (int32_t)(hi - d.x);
   }
   __syncthreads();
   for (int i = tid; i < s; i += kCtaThreads) {

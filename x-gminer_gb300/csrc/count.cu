@@ -33,6 +33,8 @@ int clique_kind(int pattern) {
   }
 }
 
+}  // namespace
+
 int ensure_clique_grid(xgm_ctx* ctx) {
   if (ctx->clique_grid == 0) {
     int per_sm = 0;
@@ -42,17 +44,24 @@ int ensure_clique_grid(xgm_ctx* ctx) {
   return ctx->clique_grid;
 }
 
-// Fills tb from the schedule policy for a k-clique style launch.
-xgm_status schedule_tasks(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp) {
-  cudaStream_t s = ctx->stream;
+// Fills tb from the schedule policy for a k-clique style launch (k = 3 for the
+// participation and multi-pattern launches).
+xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
+                         cudaStream_t s) {
   bool order = false;
   if (sp.policy == XGM_SCHED_LEARNED) {
     if (!sp.model) {
       set_thread_error("XGM_SCHED_LEARNED needs a trained model (xgm_sched.model)");
       return XGM_ERR_INVALID;
     }
-    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, ctx->tb, s));
+    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, s));
     order = sp.order_by_cost != 0;
+  } else if (sp.policy == XGM_SCHED_TUNED) {
+    if (!sp.table) {
+      set_thread_error("XGM_SCHED_TUNED needs a variant table (xgm_sched.table)");
+      return XGM_ERR_INVALID;
+    }
+    XGM_CUDA_TRY(classify_table(g, k - 1, *sp.table, tb, s));
   } else {
     int wmax = sp.warp_max > 0 ? sp.warp_max : kWarpCap;
     int cmax = sp.cta_max > 0 ? sp.cta_max : kCtaCap;
@@ -69,10 +78,16 @@ xgm_status schedule_tasks(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sche
       set_thread_error("unknown schedule policy");
       return XGM_ERR_INVALID;
     }
-    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, cmax, ctx->tb, s));
+    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, cmax, tb, s));
   }
-  XGM_CUDA_TRY(build_lists(g, ctx->tb, order, s));
+  XGM_CUDA_TRY(build_lists(g, tb, order, s));
   return XGM_OK;
+}
+
+namespace {
+
+xgm_status schedule_tasks(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp) {
+  return schedule_into(ctx->tb, g, k, sp, ctx->stream);
 }
 
 xgm_status ensure_c4(xgm_ctx* ctx, const DevGraph& g) {

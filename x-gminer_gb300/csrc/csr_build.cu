@@ -326,7 +326,7 @@ cudaError_t validate_csr(const DevGraph& g, uint32_t* err, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t finish_graph(DevGraph& g, const int32_t* group, cudaStream_t s) {
+cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cudaStream_t s) {
   const int64_t nv = g.nv, ne = g.ne;
   const int vb = bits_for(nv);
   int32_t *deg = nullptr, *degp = nullptr;
@@ -344,8 +344,7 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, cudaStream_t s) {
   TRY(cudaStreamSynchronize(s));
   g.max_deg = (int64_t)h[0];
   const int db = bits_for(g.max_deg + 1);
-  int gb = 0;
-  if (group) gb = 31;  // group ids are int32
+  const int gb = group ? bits_for(num_groups) : 0;
   if (vb + db + gb > 64) return cudaErrorInvalidValue;
 
   uint64_t *keys = nullptr, *tmp = nullptr;

@@ -40,9 +40,10 @@ cudaError_t build_csr_from_samples(int64_t nv, const int32_t* src, const int32_t
 cudaError_t validate_csr(const DevGraph& g, uint32_t* err, cudaStream_t s);
 
 // From g.rowptr_o/col_o: degrees, ranks, the rank-space CSR, out-neighbour pointers
-// and the size statistics.  `group` (optional, [nv] original ids) keeps vertices of
-// one group contiguous in rank order (batched graphs) and fills g.gid.
-cudaError_t finish_graph(DevGraph& g, const int32_t* group, cudaStream_t s);
+// and the size statistics.  `group` (optional, [nv] original ids, values below
+// num_groups) keeps vertices of one group contiguous in rank order (batched graphs)
+// and fills g.gid.
+cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cudaStream_t s);
 
 // The oriented DAG in original ids (graph.cc:233-275 output), device arrays
 // allocated here; caller frees.

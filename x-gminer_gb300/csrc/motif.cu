@@ -13,6 +13,7 @@
 // n_e and t(v) come from one triangle-participation pass of the DAG kernels
 // (clique.cu); the 4-cycle plan has its own kernel below.  Any total order of the
 // vertices gives the same counts, so rank ids serve for the "v1 < v0" restrictions.
+#include "clique.cuh"
 #include "motif.cuh"
 
 namespace xgm {
@@ -165,7 +166,8 @@ __global__ void __launch_bounds__(kC4Threads) k_cycle4(GView g, const int32_t* l
                                                        const int32_t* small, const int64_t* n,
                                                        unsigned long long* heads,
                                                        uint32_t* scratch,
-                                                       unsigned long long* out, uint32_t* err) {
+                                                       unsigned long long* out, uint32_t* err,
+                                                       GOut o) {
   __shared__ C4Smem sm;
   const int tid = threadIdx.x;
   uint32_t* cnt = scratch + (size_t)blockIdx.x * (size_t)g.nv;
@@ -182,6 +184,7 @@ __global__ void __launch_bounds__(kC4Threads) k_cycle4(GView g, const int32_t* l
       if (ti >= nt) break;
       const int32_t v0 = list[ti];
       const long long a0 = g.rowptr[v0], a1 = g.dptr[v0].x;
+      unsigned long long tacc = 0;
       if (phase == 1)
         for (int h = tid; h < kC4Hash; h += kC4Threads) sm.hkey[h] = -1, sm.hcnt[h] = 0;
       __syncthreads();
@@ -194,7 +197,7 @@ __global__ void __launch_bounds__(kC4Threads) k_cycle4(GView g, const int32_t* l
           } else if (phase == 0) {
             c4_walk(g, sm, nc, total, [&](int32_t v2) {
               unsigned long long c = atomicExch(&cnt[v2], 0u);
-              acc += c * (c - (c > 0)) / 2;
+              tacc += c * (c - (c > 0)) / 2;
             });
           } else {
             c4_walk(g, sm, nc, total, [&](int32_t v2) {
@@ -217,14 +220,58 @@ __global__ void __launch_bounds__(kC4Threads) k_cycle4(GView g, const int32_t* l
       if (phase == 1) {
         for (int h = tid; h < kC4Hash; h += kC4Threads) {
           unsigned long long c = sm.hcnt[h];
-          acc += c * (c - (c > 0)) / 2;
+          tacc += c * (c - (c > 0)) / 2;
         }
         __syncthreads();
+      }
+      if (o.gid) {
+        const unsigned long long w = warp_sum_u64(tacc);
+        if ((tid & 31) == 0 && w)
+          atomicAdd(&o.out[(long long)o.gid[v0] * o.stride + o.slot], w);
+      } else {
+        acc += tacc;
       }
     }
   }
   acc = warp_sum_u64(acc);
-  if ((tid & 31) == 0 && acc) atomicAdd(out, acc);
+  if ((tid & 31) == 0 && acc && out) atomicAdd(out, acc);
+}
+
+// Per-graph diamond / tailed-triangle totals from the participation counters: block
+// of consecutive rank ids (graphs are contiguous in rank order), shared-memory
+// aggregation by graph id, then one atomic per (block, graph).
+__global__ void k_part_reduce_graphs(GView g, const int32_t* gid,
+                                     const unsigned long long* vpart, const unsigned* epart,
+                                     unsigned long long* out, int stride, int slot_d, int slot_t) {
+  __shared__ unsigned long long sd[kThreads], st[kThreads];
+  __shared__ int32_t gfirst;
+  for (int64_t base = (int64_t)blockIdx.x * kThreads; base < g.nv;
+       base += (int64_t)gridDim.x * kThreads) {
+    sd[threadIdx.x] = 0;
+    st[threadIdx.x] = 0;
+    if (threadIdx.x == 0) gfirst = gid[base];
+    __syncthreads();
+    const int64_t r = base + threadIdx.x;
+    if (r < g.nv) {
+      const longlong2 d = g.dptr[r];
+      const long long deg = d.y - g.rowptr[r];
+      unsigned long long dia = 0;
+      if (slot_d >= 0)
+        for (long long e = d.x; e < d.y; ++e) {
+          const unsigned long long c = epart[e];
+          dia += c * (c - (c > 0)) / 2;
+        }
+      const unsigned long long tt = (slot_t >= 0 && deg > 2) ? vpart[r] * (unsigned long long)(deg - 2) : 0;
+      const int k = gid[r] - gfirst;  // < kThreads: ids are non-decreasing in rank order
+      if (dia) atomicAdd(&sd[k], dia);
+      if (tt) atomicAdd(&st[k], tt);
+    }
+    __syncthreads();
+    const long long gg = (long long)gfirst + threadIdx.x;
+    if (slot_d >= 0 && sd[threadIdx.x]) atomicAdd(&out[gg * stride + slot_d], sd[threadIdx.x]);
+    if (slot_t >= 0 && st[threadIdx.x]) atomicAdd(&out[gg * stride + slot_t], st[threadIdx.x]);
+    __syncthreads();
+  }
 }
 
 inline unsigned grid_for(int64_t n) {
@@ -266,8 +313,19 @@ cudaError_t launch_scatter_flags(const uint8_t* flag, const int64_t* pos, int64_
 
 cudaError_t launch_cycle4(const GView& g, const int32_t* large, const int32_t* small,
                           const int64_t* n, unsigned long long* heads, uint32_t* scratch,
-                          unsigned long long* out, uint32_t* err, int grid, cudaStream_t s) {
-  k_cycle4<<<grid, kC4Threads, 0, s>>>(g, large, small, n, heads, scratch, out, err);
+                          unsigned long long* out, uint32_t* err, int grid, cudaStream_t s,
+                          const GOut& o) {
+  k_cycle4<<<grid, kC4Threads, 0, s>>>(g, large, small, n, heads, scratch, out, err, o);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_part_reduce_graphs(const GView& g, const int32_t* gid,
+                                      const unsigned long long* vpart, const unsigned* epart,
+                                      unsigned long long* out, int stride, int slot_d, int slot_t,
+                                      cudaStream_t s) {
+  if (g.nv == 0) return cudaSuccess;
+  k_part_reduce_graphs<<<grid_for(g.nv), kThreads, 0, s>>>(g, gid, vpart, epart, out, stride,
+                                                           slot_d, slot_t);
   return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <algorithm>
 
+#include "clique.cuh"
 #include "common.cuh"
 
 namespace xgm {
@@ -22,6 +23,13 @@ cudaError_t launch_scatter_flags(const uint8_t* flag, const int64_t* pos, int64_
 // zeroed uint32 counters (left zeroed on return).
 cudaError_t launch_cycle4(const GView& g, const int32_t* large, const int32_t* small,
                           const int64_t* n, unsigned long long* heads, uint32_t* scratch,
-                          unsigned long long* out, uint32_t* err, int grid, cudaStream_t s);
+                          unsigned long long* out, uint32_t* err, int grid, cudaStream_t s,
+                          const GOut& o = GOut{});
+// Batched graphs: per-graph diamond (slot_d) and tailed-triangle (slot_t) totals from the
+// participation counters; a slot < 0 is skipped.
+cudaError_t launch_part_reduce_graphs(const GView& g, const int32_t* gid,
+                                      const unsigned long long* vpart, const unsigned* epart,
+                                      unsigned long long* out, int stride, int slot_d, int slot_t,
+                                      cudaStream_t s);
 
 }  // namespace xgm

@@ -40,6 +40,29 @@ __global__ void k_classify_heur(const longlong2* dptr, int64_t nv, int kmin, int
   }
 }
 
+// Bucket b of out-degree s: 0 for s == 0, else floor(log2(s)) + 1, capped.
+__device__ __forceinline__ int degree_bucket(int64_t s) {
+  if (s <= 0) return 0;
+  const int b = 64 - __clzll((unsigned long long)s);
+  return b < XGM_TUNE_BUCKETS ? b : XGM_TUNE_BUCKETS - 1;
+}
+
+__global__ void k_classify_table(const longlong2* dptr, int64_t nv, int kmin, xgm_tune_table tab,
+                                 uint8_t* var) {
+  GRID_STRIDE(r, nv) {
+    const longlong2 d = dptr[r];
+    const int64_t s = d.y - d.x;
+    uint8_t v = VAR_SKIP;
+    if (s >= kmin) {
+      v = tab.variant[degree_bucket(s)];
+      if (v == VAR_WARP && s > kWarpCap) v = VAR_CTA;
+      if (v == VAR_CTA && s > kCtaCap) v = VAR_SPLIT;
+      if (v > VAR_SPLIT) v = VAR_SPLIT;
+    }
+    var[r] = v;
+  }
+}
+
 __global__ void k_flag_eq(const uint8_t* var, int64_t nv, uint8_t x, uint8_t* flag) {
   GRID_STRIDE(r, nv) flag[r] = var[r] == x;
 }
@@ -181,10 +204,18 @@ void taskbuf_free(TaskBuf& tb, cudaStream_t s) {
 cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int cta_max, TaskBuf& tb,
                                cudaStream_t s) {
   if (warp_max > kWarpCap) warp_max = kWarpCap;
+  if (k < 2) k = 2;
   if (cta_max > kCtaCap) cta_max = kCtaCap;
   if (g.nv == 0) return cudaSuccess;
   k_classify_heur<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, k - 1, warp_max, cta_max,
                                                       tb.var);
+  return cudaGetLastError();
+}
+
+cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& tab, TaskBuf& tb,
+                           cudaStream_t s) {
+  if (g.nv == 0) return cudaSuccess;
+  k_classify_table<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, kmin, tab, tb.var);
   return cudaGetLastError();
 }
 

@@ -38,6 +38,10 @@ void taskbuf_free(TaskBuf& tb, cudaStream_t s);
 cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int cta_max, TaskBuf& tb,
                                cudaStream_t s);
 
+// Variant per out-degree bucket (XGM_SCHED_TUNED); roots with out-degree < kmin skip.
+cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& tab, TaskBuf& tb,
+                           cudaStream_t s);
+
 // Compacts tb.var into the task lists.  With `order` (learned policy) each list is
 // ordered by descending tb.cost (binned), heaviest predicted tasks first.
 cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s);
