@@ -113,6 +113,20 @@ def test_complete_graphs(xgm, ctx, n):
     assert gpu_counts(ctx, g) == _closed_form(n)
 
 
+def test_dense_hub_split_tasks(xgm, ctx):
+    # K_1100: the lowest-ranked vertices have out-degree > 1024, so their tasks are split
+    # into edge sub-tasks whose intersections exceed the shared-memory capacity; plans
+    # that only need the intersection size or participation must still be exact
+    n = 1100
+    iu = np.triu_indices(n, 1)
+    g = ctx.graph_from_edges(n, iu[0].astype(np.int32), iu[1].astype(np.int32))
+    want = _closed_form(n)
+    assert ctx.count(g, "triangle") == want["tc"]
+    assert ctx.count(g, "diamond") == want["diamond"]
+    assert ctx.count(g, "tailedtriangle") == want["tailed"]
+    assert ctx.count(g, "rectangle") == want["cycle4"]
+
+
 def test_edge_cases(xgm, ctx, orc):
     # no edges at all
     g = ctx.graph_from_edges(10, np.zeros(0, np.int32), np.zeros(0, np.int32))

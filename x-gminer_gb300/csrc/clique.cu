@@ -292,8 +292,11 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
 // CTA-wide ordered intersection N+(v0) & N+(v1) into S; returns its size or -1 when it
 // exceeds kCtaCap.  Members of N+(v1) are binary-searched in N+(v0) (global, sorted).
 // PART credits the triangles (v0, v1, w): edges (v1, w) and (v0, w) and vertex w.
-template <bool PART, bool STORE>
-__device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_t v1, Part part) {
+// Without STORE only the size is produced (no capacity limit); WSUM adds d+(w) of every
+// member to *wsum (per thread).
+template <bool PART, bool STORE, bool WSUM = false>
+__device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_t v1, Part part,
+                                    uint64_t* wsum = nullptr) {
   int32_t* S = (int32_t*)(sm + kOffS);
   int32_t* wtot = (int32_t*)(sm + kOffMisc);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -315,6 +318,10 @@ __device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_
         atomicAdd(&part.e[e], 1u);
         atomicAdd(&part.e[lo], 1u);
         atomicAdd(&part.v[y], 1ull);
+      }
+      if (WSUM && found) {
+        const longlong2 dy = ldg_ll2(g.dptr + y);
+        *wsum += (uint64_t)(dy.y - dy.x);
       }
     }
     const unsigned bal = __ballot_sync(kFull, found);
@@ -491,7 +498,11 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
     const longlong2 d0 = ldg_ll2(g.dptr + v0);
     const long long e01 = d0.x + (ti - t.split_off[lo]);
     const int32_t v1 = ldg_i32(g.col + e01);
-    const int n = cta_intersect_into_S<PART, !(MODE == kModePart)>(g, sm, v0, v1, part);
+    // the local set is stored only when (K-2)-cliques of it have to be counted
+    constexpr bool kStore = MULTI || (MODE != kModePart && K - 2 >= 2);
+    constexpr bool kWsum = MODE == kModeWeight && K == 3;
+    uint64_t wsum = 0;
+    const int n = cta_intersect_into_S<PART, kStore, kWsum>(g, sm, v0, v1, part, &wsum);
     if (n < 0) {
       if (tid == 0) atomicOr(err, ERR_CAPACITY);
     } else {
@@ -505,8 +516,9 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
         const uint64_t k4 = n >= 2 ? cta_local<2, kModeCount>(g, sm, n, part, -1) : 0;
         emit(o, v0, tid == 0 ? (uint64_t)n : 0, k4, acc);
       } else if (!PART && n > 0) {
-        uint64_t r = cta_local<K - 2, MODE>(g, sm, n, part, -1);
-        if (K - 2 == 1 && MODE != kModeWeight) r = tid == 0 ? r : 0;  // same n in all threads
+        uint64_t r;
+        if (K - 2 == 1) r = kWsum ? wsum : (tid == 0 ? (uint64_t)n : 0);  // |L| once per CTA
+        else r = cta_local<K - 2, MODE>(g, sm, n, part, -1);
         if (MODE == kModeWeight) acc += r; else emit(o, v0, r, 0, acc);
       }
     }
