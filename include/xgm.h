@@ -210,6 +210,16 @@ xgm_status xgm_sc_solver(xgm_ctx* ctx, const xgm_graph* g, const char* pattern,
 xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
                              const xgm_sched* sched, int* n_kernels);
 
+/* Triangle count that allocates no device memory.  No counterpart in the reference.
+ * For callers that cannot allocate while they count (a stream under CUDA-graph capture,
+ * a host framework that owns all device memory, an allocation-free hot loop): the
+ * task lists and counters live in a 48 MiB file-scope device array instead of memory
+ * allocated per call, so graphs of up to 2^21 vertices are accepted (larger:
+ * XGM_ERR_UNSUPPORTED).  Same result as xgm_tc_solver.  All calls share the array, so
+ * calls whose GPU work overlaps race; the first call on a device resolves the array's
+ * address and should come before any stream capture. */
+xgm_status xgm_tc_solver_static(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total);
+
 /* Algorithmic adjacency bytes the plan reads on g (host pass over the downloaded
  * graph; 4 B per int32 element + 8 B per task), used as the roofline numerator. */
 xgm_status xgm_algo_bytes(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,

@@ -119,6 +119,7 @@ _SIGS = [
     ("xgm_count", _I, [_P, _P, _P, C.POINTER(Sched), C.POINTER(_U64), C.POINTER(Stats)]),
     ("xgm_count_kernels", _I, [_P, _P, _P, C.POINTER(Sched), C.POINTER(_I)]),
     ("xgm_tc_solver", _I, [_P, _P, C.POINTER(_U64)]),
+    ("xgm_tc_solver_static", _I, [_P, _P, C.POINTER(_U64)]),
     ("xgm_clique_solver", _I, [_P, _P, _I, C.POINTER(_U64)]),
     ("xgm_sc_solver", _I, [_P, _P, C.c_char_p, C.POINTER(_U64)]),
     ("xgm_algo_bytes", _I, [_P, _P, _P, C.POINTER(_U64)]),
