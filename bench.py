@@ -200,21 +200,16 @@ def cpu_sample(orc, kind: str, drow, dcol, budget_s: float):
     with the stride picked from a short calibration so the sample takes ~budget_s."""
     nv = len(drow) - 1
     cores = orc.threads()
-    # shrink the stride until a sample takes an eighth of the budget, then scale it so
-    # the timed sample takes about budget_s (time grows ~ 1 / stride)
-    stride = 1 << 16
+    # halve a power-of-two stride (nested samples: every 2^k-th vertex) until the sample
+    # takes at least half the budget; that sample is the measurement
+    stride = 1 << 20
     while True:
         t0 = time.perf_counter()
-        orc.count(kind, drow, dcol, 0, nv, stride)
-        t_cal = time.perf_counter() - t0
-        if t_cal >= budget_s / 8 or stride == 1:
-            break
-        stride = max(1, stride // (4 if t_cal < budget_s / 64 else 2))
-    stride = max(1, int(round(stride * t_cal / budget_s)))
-    t0 = time.perf_counter()
-    c = orc.count(kind, drow, dcol, 0, nv, stride)
-    dt = time.perf_counter() - t0
-    return c, dt, stride, cores
+        c = orc.count(kind, drow, dcol, 0, nv, stride)
+        dt = time.perf_counter() - t0
+        if dt >= budget_s / 2 or stride == 1:
+            return c, dt, stride, cores
+        stride //= 2
 
 
 def gen_graph(xgm, scale):

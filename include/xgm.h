@@ -160,7 +160,8 @@ typedef enum {
   XGM_VAR_WARP = 0,   /* one warp per task, frontier bitmap in shared memory */
   XGM_VAR_CTA = 1,    /* one CTA per task, frontier bitmap in shared memory */
   XGM_VAR_SPLIT = 2,  /* task split into per-edge sub-tasks (hub vertices) */
-  XGM_NUM_VARIANTS = 3
+  XGM_VAR_WIDE = 3,   /* one warp per task, 4-word frontier bitmap rows (out-degree <= 128) */
+  XGM_NUM_VARIANTS = 4
 } xgm_variant;
 
 /* Autotuned schedule: the variant for each out-degree bucket.  Bucket b holds
@@ -175,11 +176,12 @@ typedef struct {
   int policy;             /* xgm_sched_policy */
   int variant;            /* for XGM_SCHED_FIXED */
   const xgm_model* model; /* for XGM_SCHED_LEARNED */
-  int warp_max;           /* heuristic: out-degree <= warp_max -> WARP (0: default) */
-  int cta_max;            /* heuristic: out-degree <= cta_max -> CTA, else SPLIT (0: default) */
+  int warp_max;           /* heuristic: out-degree <= warp_max -> WARP (0: default 32) */
+  int cta_max;            /* heuristic: out-degree <= cta_max -> CTA, else SPLIT (0: default 1024) */
   int order_by_cost;      /* learned: 1 = heaviest predicted tasks first */
   const xgm_tune_table* table; /* for XGM_SCHED_TUNED */
   int flags;              /* XGM_SCHED_NO_GRAPH: batched calls launch directly, no CUDA graph */
+  int wide_max;           /* heuristic: out-degree <= wide_max -> WIDE (0: default 128; -1: none) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };

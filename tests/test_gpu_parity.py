@@ -63,10 +63,11 @@ def test_schedules_never_change_counts(xgm, ctx):
     g = ctx.graph_from_edges(nv, s, d)
     for pat in ("triangle", "4-clique", "5-clique", "diamond", "tailedtriangle"):
         base = ctx.count(g, pat)
-        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT):
+        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE):
             assert ctx.count(g, pat, policy=xgm.SCHED_FIXED, variant=var) == base, (pat, var)
-        for wmax, cmax in ((8, 64), (32, 128), (1, 1), (16, 2048)):
-            assert ctx.count(g, pat, warp_max=wmax, cta_max=cmax) == base, (pat, wmax, cmax)
+        for wmax, dmax, cmax in ((8, 0, 64), (32, 64, 128), (1, -1, 1), (16, 100, 2048)):
+            assert ctx.count(g, pat, warp_max=wmax, wide_max=dmax, cta_max=cmax) == base, \
+                (pat, wmax, dmax, cmax)
 
 
 def test_upload_paths_agree(xgm, ctx, orc):

@@ -482,7 +482,10 @@ xgm_status xgm_autotune(xgm_ctx* ctx, const xgm_graph* g, xgm_batch* b, const xg
   xgm_tune_table tab;
   for (int k = 0; k < XGM_TUNE_BUCKETS; ++k) {
     const int64_t smax = k == 0 ? 0 : (int64_t(1) << k) - 1;
-    tab.variant[k] = smax <= kWarpCap ? XGM_VAR_WARP : (smax <= kCtaCap ? XGM_VAR_CTA : XGM_VAR_SPLIT);
+    tab.variant[k] = smax <= kWarpCap   ? XGM_VAR_WARP
+                     : smax <= kWideCap ? XGM_VAR_WIDE
+                     : smax <= kCtaCap  ? XGM_VAR_CTA
+                                        : XGM_VAR_SPLIT;
   }
   xgm_sched ts = heur;
   ts.policy = XGM_SCHED_TUNED;
@@ -500,9 +503,10 @@ xgm_status xgm_autotune(xgm_ctx* ctx, const xgm_graph* g, xgm_batch* b, const xg
       const int64_t smin = int64_t(1) << (k - 1);
       const uint8_t keep = tab.variant[k];
       uint8_t bestv = keep;
-      for (uint8_t v = 0; v < 3; ++v) {
+      for (uint8_t v = 0; v < XGM_NUM_VARIANTS; ++v) {
         if (v == keep) continue;
         if (v == XGM_VAR_WARP && smin > kWarpCap) continue;
+        if (v == XGM_VAR_WIDE && smin > kWideCap) continue;
         if (v == XGM_VAR_CTA && smin > kCtaCap) continue;
         tab.variant[k] = v;
         double ms = 0;

@@ -42,22 +42,45 @@ constexpr int kOffHval = kOffHkey + 4 * kHashSize;
 constexpr int kOffCnt = kOffHval + 2 * kHashSize;
 constexpr int kOffRows = kOffCnt + 4 * kCtaCap;
 constexpr int kRowsWords = 16896;  // tri_words(1024)
-constexpr int kOffMisc = kOffRows + 4 * kRowsWords;
+constexpr int kBloomWords = 512;  // 16 Kbit membership pre-filter of the local set
+constexpr int kOffBloom = kOffRows + 4 * kRowsWords;
+constexpr int kOffMisc = kOffBloom + 4 * kBloomWords;
 constexpr int kCtaSmem = kOffMisc + 8 * 16;
 constexpr int kClipMin = 96;  // lists longer than this are clipped at max(S)
 
-// Warp region: one per warp, aliased over the CTA region once the CTA queues drain.
+// Wide-warp region (one warp, s <= kWideCap, 4-word rows), aliased over the CTA region
+// once the CTA queues drain; the warp regions follow all wide regions so a warp in the
+// last phase never overlaps a warp still in the wide phase.
+struct WideSmem {
+  uint32_t bloom[16];  // 512-bit membership pre-filter of S
+  long long lb[kWideCap];
+  int32_t S[kWideCap];
+  int32_t pre[kWideCap + 4];
+  uint32_t rows[kWideCap * kWideWords];  // full rows, word w of row i at [i*4 + w]
+  uint32_t cnt[kWideCap];
+};
+constexpr int kOffWarpRegion = kCtaWarps * (int)sizeof(WideSmem);
+
+// Warp region: one per warp (s <= 32, one-word rows).
 struct WarpSmem {
+  uint32_t bloom[8];  // 256-bit membership pre-filter of S
   long long lb[kWarpCap];
   int32_t S[kWarpCap];
   int32_t pre[kWarpCap + 2];
   uint32_t rows[kWarpCap];
   uint32_t cnt[kWarpCap];
 };
-static_assert(sizeof(WarpSmem) * kCtaWarps <= kCtaSmem, "warp region must fit");
+static_assert(kOffWarpRegion + sizeof(WarpSmem) * kCtaWarps <= kCtaSmem, "warp regions fit");
+static_assert(sizeof(WideSmem) % 16 == 0, "wide regions stay 16-byte aligned");
 
 __device__ __forceinline__ uint32_t hash_slot(int32_t x) {
   return ((uint32_t)x * 2654435761u) >> (32 - 11);  // kHashSize = 2^11
+}
+
+// Bloom bit of x (independent of hash_slot's multiplier): 14 bits for the CTA filter,
+// the top 8 of them for the warp filter.
+__device__ __forceinline__ uint32_t bloom_bit(int32_t x) {
+  return ((uint32_t)x * 0x85EBCA6Bu) >> 18;
 }
 
 __device__ __forceinline__ int hash_find(const int32_t* hkey, const uint16_t* hval, int32_t x) {
@@ -112,6 +135,45 @@ enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 
 // Count of (q)-cliques in the local DAG held by the CTA (q >= 3 uses the bitmap).  WGT
 // (Q == 3 only) weights each clique by d+ of its top member, d+(S[l]) = pre[l+1]-pre[l].
+//
+// A warp owns row i (words qi..W-1, nwi of them).  It splits into groups of
+// G = next_pow2(nwi) lanes; lane p of a group holds word qi+p, so each group can take a
+// different set bit j of row i per round: the group finds the rank-n bit with a
+// group-local prefix of popcounts, a ballot and __fns.  For Q == 4 each group then
+// walks the bits l of m = row_i & row_j the same way.  Short rows (most rows of small
+// tasks and the second half of every task) thus process 32/G bits at a time.
+__device__ __forceinline__ int group_width(int nwi) {
+  return nwi <= 1 ? 1 : nwi <= 2 ? 2 : nwi <= 4 ? 4 : nwi <= 8 ? 8 : nwi <= 16 ? 16 : 32;
+}
+
+// Rank-n set bit of the group's distributed word (lane p holds word qi+p; incl/excl are
+// group-local inclusive/exclusive popcount prefixes).  Returns the local bit index
+// (relative to word qi) or -1 when n is out of range; called by all 32 lanes.
+__device__ __forceinline__ int group_nth_bit(uint32_t word, int incl, int excl, int n, bool act,
+                                             int g, int G) {
+  const unsigned bal = __ballot_sync(kFull, act && incl <= n);
+  const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << (g * G));
+  const int pstar = __popc(bal & gmask);
+  const int src = g * G + (pstar < G ? pstar : G - 1);
+  const uint32_t wsrc = __shfl_sync(kFull, word, src);
+  const int ex = __shfl_sync(kFull, excl, src);
+  if (!act) return -1;
+  return (pstar << 5) + (int)__fns(wsrc, 0, n - ex + 1);
+}
+
+__device__ __forceinline__ void group_prefix(uint32_t word, int p, int G, int& incl, int& excl) {
+  const int c = __popc(word);
+  int v = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    if (o >= G) break;
+    const int y = __shfl_up_sync(kFull, v, o, G);
+    if (p >= o) v += y;
+  }
+  incl = v;
+  excl = v - c;
+}
+
 template <int Q, bool WGT>
 __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, const int32_t* pre) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -119,44 +181,48 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
   uint64_t acc = 0;
   for (int i = warp; i < s; i += kCtaWarps) {
     const int qi = i >> 5, nwi = W - qi;
+    const int G = group_width(nwi), NG = 32 / G;
+    const int g = lane / G, p = lane - g * G;
     const uint32_t* Ri = rows + tri_row_off(i, W);
-    const uint32_t wi = lane < nwi ? Ri[lane] : 0u;
-    const int w = qi + lane;
-    unsigned nz = __ballot_sync(kFull, wi != 0u);
-    while (nz) {
-      const int src = __ffs(nz) - 1;
-      nz &= nz - 1;
-      uint32_t bits = __shfl_sync(kFull, wi, src);
-      while (bits) {
-        const int j = ((qi + src) << 5) + __ffs(bits) - 1;
-        bits &= bits - 1;
-        const int qj = j >> 5;
-        const uint32_t* Rj = rows + tri_row_off(j, W);
-        const uint32_t m = (lane < nwi && w >= qj) ? (wi & Rj[w - qj]) : 0u;
-        if (Q == 3) {
-          if (WGT) {
-            uint32_t b3 = m;
-            while (b3) {
-              const int l = (w << 5) + __ffs(b3) - 1;
-              b3 &= b3 - 1;
-              acc += (uint64_t)(pre[l + 1] - pre[l]);
-            }
-          } else {
-            acc += __popc(m);
+    const uint32_t wi = p < nwi ? Ri[p] : 0u;
+    const int w = qi + p;  // absolute word of this lane
+    int incl, excl;
+    group_prefix(wi, p, G, incl, excl);
+    const int T = __shfl_sync(kFull, incl, g * G + G - 1);  // bits in row i
+    for (int base = 0; base < T; base += NG) {
+      const int n = base + g;
+      const int jl = group_nth_bit(wi, incl, excl, n, n < T, g, G);
+      const int j = (qi << 5) + jl;
+      const int qj = j >> 5;
+      const uint32_t* Rj = rows + tri_row_off(j, W);
+      const uint32_t m = (jl >= 0 && p < nwi && w >= qj) ? (wi & Rj[w - qj]) : 0u;
+      if (Q == 3) {
+        if (WGT) {
+          uint32_t b3 = m;
+          while (b3) {
+            const int l = (w << 5) + __ffs(b3) - 1;
+            b3 &= b3 - 1;
+            acc += (uint64_t)(pre[l + 1] - pre[l]);
           }
         } else {
-          unsigned nz2 = __ballot_sync(kFull, m != 0u);
-          while (nz2) {
-            const int src2 = __ffs(nz2) - 1;
-            nz2 &= nz2 - 1;
-            uint32_t bits2 = __shfl_sync(kFull, m, src2);
-            while (bits2) {
-              const int l = ((qi + src2) << 5) + __ffs(bits2) - 1;
-              bits2 &= bits2 - 1;
-              const int ql = l >> 5;
-              const uint32_t* Rl = rows + tri_row_off(l, W);
-              if (w >= ql && m) acc += __popc(m & Rl[w - ql]);
-            }
+          acc += __popc(m);
+        }
+      } else {
+        int incl2, excl2;
+        group_prefix(m, p, G, incl2, excl2);
+        const int T2 = __shfl_sync(kFull, incl2, g * G + G - 1);
+        int T2max = T2;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const int y = __shfl_xor_sync(kFull, T2max, o);
+          T2max = y > T2max ? y : T2max;
+        }
+        for (int n2 = 0; n2 < T2max; ++n2) {
+          const int ll = group_nth_bit(m, incl2, excl2, n2, n2 < T2, g, G);
+          if (ll >= 0) {
+            const int l = (qi << 5) + ll;
+            const int ql = l >> 5;
+            if (p < nwi && w >= ql && m) acc += __popc(m & rows[tri_row_off(l, W) + (w - ql)]);
           }
         }
       }
@@ -202,7 +268,9 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = (s + 31) >> 5;
 
+  uint32_t* bloom = (uint32_t*)(sm + kOffBloom);
   for (int h = tid; h < kHashSize; h += kCtaThreads) hkey[h] = -1;
+  for (int h = tid; h < kBloomWords; h += kCtaThreads) bloom[h] = 0u;
   if (Q >= 3)
     for (int x = tid; x < tri_words(s); x += kCtaThreads) rows[x] = 0u;
   if (PART)
@@ -229,47 +297,75 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
     uint32_t slot = hash_slot(x);
     while (atomicCAS(&hkey[slot], -1, x) != -1) slot = (slot + 1) & (kHashSize - 1);
     hval[slot] = (uint16_t)i;
+    const uint32_t b = bloom_bit(x);
+    atomicOr(&bloom[b >> 5], 1u << (b & 31));
   }
   cta_scan_lengths(pre, s, wtot);  // ends with __syncthreads
   const int total = pre[s];
   const int32_t smax = S[s - 1];
   uint64_t acc = 0, q2 = 0;
   // Flattened walk over all (i, element) pairs: warp chunks of 256 consecutive
-  // elements, lanes contiguous within a chunk so row reads are coalesced.
+  // elements, lanes contiguous within a chunk so row reads are coalesced.  Each lane
+  // keeps its segment's base in registers, issues four loads before using them, and
+  // rejects most non-members with one Bloom-filter probe before the hash lookup.
   for (int c = warp; c * 256 < total; c += kCtaWarps) {
-    int k = c * 256 + lane;
+    const int kb = c * 256 + lane;
     int i;
-    {  // first segment: largest i with pre[i] <= k
+    {  // first segment: largest i with pre[i] <= kb
       int lo = 0, hi = s;
       while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
-        if (pre[mid] <= k) lo = mid; else hi = mid;
+        if (pre[mid] <= kb) lo = mid; else hi = mid;
       }
       i = lo;
     }
-#pragma unroll 2
-    for (int t = 0; t < 8; ++t, k += 32) {
-      if (k >= total) break;
-      while (pre[i + 1] <= k) ++i;
-      const int32_t x = ldg_i32(g.col + lb[i] + (k - pre[i]));
-      if (x <= smax) {
+    int seg_end = pre[i + 1];
+    long long seg_base = lb[i] - pre[i];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      int32_t xv[4];
+      int iv[4];
+      long long pv[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int k = kb + 32 * (4 * h + t);
+        xv[t] = 0x7FFFFFFF;  // above every id: rejected below
+        iv[t] = i;
+        pv[t] = 0;
+        if (k < total) {
+          while (k >= seg_end) {
+            ++i;
+            seg_end = pre[i + 1];
+            seg_base = lb[i] - pre[i];
+          }
+          pv[t] = seg_base + k;
+          iv[t] = i;
+          xv[t] = ldg_i32(g.col + pv[t]);
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int32_t x = xv[t];
+        if (x > smax) continue;
+        const uint32_t b = bloom_bit(x);
+        if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
         const int j = hash_find(hkey, hval, x);
-        if (j >= 0) {
-          if (Q == 2) {
-            acc += WGT ? (uint64_t)(pre[j + 1] - pre[j]) : 1;
-            if (PART) {
-              atomicAdd(&cnt[i], 1u);
-              atomicAdd(&cnt[j], 1u);
-              atomicAdd(&part.e[lb[i] + (k - pre[i])], 1u);
-            }
-          } else {
-            atomicOr(&rows[tri_row_off(i, W) + (j >> 5) - (i >> 5)], 1u << (j & 31));
-            if (MULTI) {
-              q2 += 1;
-              atomicAdd(&cnt[i], 1u);
-              atomicAdd(&cnt[j], 1u);
-              atomicAdd(&part.e[lb[i] + (k - pre[i])], 1u);
-            }
+        if (j < 0) continue;
+        const int ii = iv[t];
+        if (Q == 2) {
+          acc += WGT ? (uint64_t)(pre[j + 1] - pre[j]) : 1;
+          if (PART) {
+            atomicAdd(&cnt[ii], 1u);
+            atomicAdd(&cnt[j], 1u);
+            atomicAdd(&part.e[pv[t]], 1u);
+          }
+        } else {
+          atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
+          if (MULTI) {
+            q2 += 1;
+            atomicAdd(&cnt[ii], 1u);
+            atomicAdd(&cnt[j], 1u);
+            atomicAdd(&part.e[pv[t]], 1u);
           }
         }
       }
@@ -361,12 +457,24 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   const longlong2 d0 = ldg_ll2(g.dptr + v0);
   const int s = (int)(d0.y - d0.x);
   int len = 0;
+  int32_t xs = 0;
+  longlong2 dx = make_longlong2(0, 0);
   if (lane < s) {
-    const int32_t x = ldg_i32(g.col + d0.x + lane);
-    w.S[lane] = x;
-    const longlong2 d = ldg_ll2(g.dptr + x);
-    w.lb[lane] = d.x;
-    len = (int)(d.y - d.x);
+    xs = ldg_i32(g.col + d0.x + lane);
+    w.S[lane] = xs;
+    dx = ldg_ll2(g.dptr + xs);
+    w.lb[lane] = dx.x;
+    len = (int)(dx.y - dx.x);
+  }
+  const int32_t smax = __shfl_sync(kFull, xs, s - 1);
+  // clip long lists at max(S) (members above it cannot hit)
+  if (lane < s && len > kClipMin && ldg_i32(g.col + dx.y - 1) > smax) {
+    long long lo = dx.x, hi = dx.y;
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      if (ldg_i32(g.col + mid) <= smax) lo = mid + 1; else hi = mid;
+    }
+    len = (int)(lo - dx.x);
   }
   int inc = len;
 #pragma unroll
@@ -378,32 +486,62 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   if (lane == 31) w.pre[32] = inc;
   w.rows[lane] = 0u;
   w.cnt[lane] = 0u;
+  if (lane < 8) w.bloom[lane] = 0u;
+  __syncwarp();
+  if (lane < s) {
+    const uint32_t b = bloom_bit(xs) >> 6;  // 8 bits
+    atomicOr(&w.bloom[b >> 5], 1u << (b & 31));
+  }
   __syncwarp();  // pre[s] is the total: lanes >= s contributed length 0
   const int total = w.pre[s];
-  const int32_t smax = w.S[s - 1];
   uint64_t acc = 0, q2 = 0;
   int i = 0;
-  for (int k = lane; k < total; k += 32) {
-    while (w.pre[i + 1] <= k) ++i;
-    const int32_t x = ldg_i32(g.col + w.lb[i] + (k - w.pre[i]));
-    if (x <= smax) {
+  int seg_end = w.pre[1];
+  long long seg_base = w.lb[0];
+  for (int kb = lane; kb < total; kb += 128) {
+    int32_t xv[4];
+    int iv[4];
+    long long pv[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int k = kb + 32 * t;
+      xv[t] = 0x7FFFFFFF;
+      iv[t] = i;
+      pv[t] = 0;
+      if (k < total) {
+        while (k >= seg_end) {
+          ++i;
+          seg_end = w.pre[i + 1];
+          seg_base = w.lb[i] - w.pre[i];
+        }
+        pv[t] = seg_base + k;
+        iv[t] = i;
+        xv[t] = ldg_i32(g.col + pv[t]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int32_t x = xv[t];
+      if (x > smax) continue;
+      const uint32_t b = bloom_bit(x) >> 6;
+      if (!((w.bloom[b >> 5] >> (b & 31)) & 1u)) continue;
       const int j = warp_bsearch(w.S, s, x);
-      if (j >= 0) {
-        if (Q == 2) {
-          acc += WGT ? (uint64_t)(w.pre[j + 1] - w.pre[j]) : 1;
-          if (PART) {
-            atomicAdd(&w.cnt[i], 1u);
-            atomicAdd(&w.cnt[j], 1u);
-            atomicAdd(&part.e[w.lb[i] + (k - w.pre[i])], 1u);
-          }
-        } else {
-          atomicOr(&w.rows[i], 1u << j);
-          if (MULTI) {
-            q2 += 1;
-            atomicAdd(&w.cnt[i], 1u);
-            atomicAdd(&w.cnt[j], 1u);
-            atomicAdd(&part.e[w.lb[i] + (k - w.pre[i])], 1u);
-          }
+      if (j < 0) continue;
+      const int ii = iv[t];
+      if (Q == 2) {
+        acc += WGT ? (uint64_t)(w.pre[j + 1] - w.pre[j]) : 1;
+        if (PART) {
+          atomicAdd(&w.cnt[ii], 1u);
+          atomicAdd(&w.cnt[j], 1u);
+          atomicAdd(&part.e[pv[t]], 1u);
+        }
+      } else {
+        atomicOr(&w.rows[ii], 1u << j);
+        if (MULTI) {
+          q2 += 1;
+          atomicAdd(&w.cnt[ii], 1u);
+          atomicAdd(&w.cnt[j], 1u);
+          atomicAdd(&part.e[pv[t]], 1u);
         }
       }
     }
@@ -446,6 +584,182 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   return acc;
 }
 
+// One warp, local set S = N+(v0) with s <= 128 (rows of 4 words): Q-cliques of the
+// local DAG.  Same walk as the CTA tier (segment registers, four loads in flight, Bloom
+// pre-filter) with binary search in S; counting gives each lane whole rows.
+template <int Q, int MODE>
+__device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part part,
+                                   uint64_t* q2out = nullptr) {
+  static_assert(Q >= 2, "wide tasks count at least local edges");
+  constexpr bool MULTI = MODE == kModeMulti;
+  constexpr bool PART = MODE == kModePart || MULTI;
+  constexpr bool WGT = MODE == kModeWeight;
+  const int lane = threadIdx.x & 31;
+  const longlong2 d0 = ldg_ll2(g.dptr + v0);
+  const int s = (int)(d0.y - d0.x);
+  // lane owns items 4*lane .. 4*lane+3 (contiguous, for the scan)
+  int len[4];
+  long long lbv[4];
+  int32_t xs[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int i = 4 * lane + t;
+    len[t] = 0;
+    lbv[t] = 0;
+    xs[t] = 0;
+    if (i < s) {
+      xs[t] = ldg_i32(g.col + d0.x + i);
+      w.S[i] = xs[t];
+      const longlong2 d = ldg_ll2(g.dptr + xs[t]);
+      lbv[t] = d.x;
+      len[t] = (int)(d.y - d.x);
+    }
+  }
+  __syncwarp();
+  const int32_t smax = w.S[s - 1];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    if (len[t] > kClipMin && ldg_i32(g.col + lbv[t] + len[t] - 1) > smax) {
+      long long lo = lbv[t], hi = lbv[t] + len[t];
+      while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (ldg_i32(g.col + mid) <= smax) lo = mid + 1; else hi = mid;
+      }
+      len[t] = (int)(lo - lbv[t]);
+    }
+  }
+  const int mine = len[0] + len[1] + len[2] + len[3];
+  int inc = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  int ex = inc - mine;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int i = 4 * lane + t;
+    if (i <= s) w.pre[i] = ex;  // pre[s] = total (items >= s have length 0)
+    if (i < s) w.lb[i] = lbv[t];
+    ex += len[t];
+  }
+  if (lane == 31) w.pre[kWideCap] = inc;  // total when s == kWideCap
+  for (int x = lane; x < kWideCap * kWideWords; x += 32) w.rows[x] = 0u;
+  for (int x = lane; x < kWideCap; x += 32) w.cnt[x] = 0u;
+  if (lane < 16) w.bloom[lane] = 0u;
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < 4; ++t)
+    if (4 * lane + t < s) {
+      const uint32_t b = bloom_bit(xs[t]) >> 5;  // 9 bits
+      atomicOr(&w.bloom[b >> 5], 1u << (b & 31));
+    }
+  __syncwarp();
+  const int total = w.pre[s];
+  uint64_t acc = 0, q2 = 0;
+  int i = 0;
+  int seg_end = w.pre[1];
+  long long seg_base = w.lb[0];
+  for (int kb = lane; kb < total; kb += 128) {
+    int32_t xv[4];
+    int iv[4];
+    long long pv[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int k = kb + 32 * t;
+      xv[t] = 0x7FFFFFFF;
+      iv[t] = i;
+      pv[t] = 0;
+      if (k < total) {
+        while (k >= seg_end) {
+          ++i;
+          seg_end = w.pre[i + 1];
+          seg_base = w.lb[i] - w.pre[i];
+        }
+        pv[t] = seg_base + k;
+        iv[t] = i;
+        xv[t] = ldg_i32(g.col + pv[t]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int32_t x = xv[t];
+      if (x > smax) continue;
+      const uint32_t b = bloom_bit(x) >> 5;
+      if (!((w.bloom[b >> 5] >> (b & 31)) & 1u)) continue;
+      const int j = warp_bsearch(w.S, s, x);
+      if (j < 0) continue;
+      const int ii = iv[t];
+      if (Q == 2) {
+        acc += WGT ? (uint64_t)(w.pre[j + 1] - w.pre[j]) : 1;
+        if (PART) {
+          atomicAdd(&w.cnt[ii], 1u);
+          atomicAdd(&w.cnt[j], 1u);
+          atomicAdd(&part.e[pv[t]], 1u);
+        }
+      } else {
+        atomicOr(&w.rows[ii * kWideWords + (j >> 5)], 1u << (j & 31));
+        if (MULTI) {
+          q2 += 1;
+          atomicAdd(&w.cnt[ii], 1u);
+          atomicAdd(&w.cnt[j], 1u);
+          atomicAdd(&part.e[pv[t]], 1u);
+        }
+      }
+    }
+  }
+  if (MULTI) *q2out = q2;
+  __syncwarp();
+  if (PART)
+    for (int r = lane; r < s; r += 32)
+      if (w.cnt[r]) {
+        atomicAdd(&part.v[w.S[r]], (unsigned long long)w.cnt[r]);
+        atomicAdd(&part.e[d0.x + r], w.cnt[r]);
+      }
+  if (Q >= 3) {
+    for (int r = lane; r < s; r += 32) {
+      const uint32_t* Rr = w.rows + r * kWideWords;
+      for (int wj = r >> 5; wj < kWideWords; ++wj) {
+        uint32_t bits = Rr[wj];
+        while (bits) {
+          const int j = (wj << 5) + __ffs(bits) - 1;
+          bits &= bits - 1;
+          const uint32_t* Rj = w.rows + j * kWideWords;
+          for (int ww = j >> 5; ww < kWideWords; ++ww) {
+            const uint32_t m = Rr[ww] & Rj[ww];
+            if (!m) continue;
+            if (Q == 3) {
+              if (WGT) {
+                uint32_t b3 = m;
+                while (b3) {
+                  const int l = (ww << 5) + __ffs(b3) - 1;
+                  b3 &= b3 - 1;
+                  acc += (uint64_t)(w.pre[l + 1] - w.pre[l]);
+                }
+              } else {
+                acc += __popc(m);
+              }
+            } else {
+              uint32_t b3 = m;
+              while (b3) {
+                const int l = (ww << 5) + __ffs(b3) - 1;
+                b3 &= b3 - 1;
+                const uint32_t* Rl = w.rows + l * kWideWords;
+                for (int wl = l >> 5; wl < kWideWords; ++wl) {
+                  // m restricted to word wl is Rr[wl] & Rj[wl]
+                  acc += __popc(Rr[wl] & Rj[wl] & Rl[wl]);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncwarp();
+  return acc;
+}
+
 // ------------------------------------------------------------ persistent kernel
 // Per-task emission: one global total (gid == null) or per-graph totals
 // out[gid[v0] * stride + slot] (batched graphs).  Called by all 32 lanes of a warp.
@@ -479,6 +793,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
   __shared__ long long task_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long n_split = t.n[0], n_cta = t.n[1], n_warp = t.n[2], n_hubs = t.n[3];
+  const long long n_wide = t.n[4];
   uint64_t acc = 0;
 
   // 1) hub edge sub-tasks: local set N+(v0) & N+(v1), (K-2)-cliques of it
@@ -556,8 +871,36 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
     __syncthreads();
     if (t.log_cta && tid == 0) t.log_cta[ti] = clock64() - c0;
   }
-  // 3) warp vertex tasks (s <= 32); the CTA region is reused per warp
-  WarpSmem& ws = ((WarpSmem*)sm)[warp];
+  // 3) wide-warp vertex tasks (s <= 128); the CTA region is reused per warp
+  {
+    WideSmem& wd = ((WideSmem*)sm)[warp];
+    for (;;) {
+      long long ti = 0;
+      if (lane == 0) ti = (long long)atomicAdd(&q->wide, 1ull);
+      ti = __shfl_sync(kFull, ti, 0);
+      if (ti >= n_wide) break;
+      const long long c0 = t.log_wide ? clock64() : 0;
+      const int32_t v0 = t.wide[ti];
+      const longlong2 d0 = ldg_ll2(g.dptr + v0);
+      const int s = (int)(d0.y - d0.x);
+      if (s > kWideCap) {
+        if (lane == 0) atomicOr(err, ERR_CAPACITY);
+      } else if (s >= kMinS) {
+        uint64_t q2 = 0;
+        const uint64_t r = warp_wide_task<K - 1, MODE>(g, wd, v0, part, &q2);
+        if (PART) {
+          const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
+          if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
+        }
+        if (MULTI) emit(o, v0, q2, r, acc);
+        else if (MODE == kModeWeight) acc += r;
+        else if (!PART) emit(o, v0, r, 0, acc);
+      }
+      if (t.log_wide && lane == 0) t.log_wide[ti] = clock64() - c0;
+    }
+  }
+  // 4) warp vertex tasks (s <= 32), in a region disjoint from every wide region
+  WarpSmem& ws = ((WarpSmem*)(sm + kOffWarpRegion))[warp];
   for (;;) {
     long long ti = 0;
     if (lane == 0) ti = (long long)atomicAdd(&q->warp, 1ull);

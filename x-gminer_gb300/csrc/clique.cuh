@@ -9,23 +9,27 @@ constexpr int kCtaWarps = kCtaThreads / 32;
 constexpr int kCtaCap = 1024;               // largest local set a CTA task holds
 constexpr int kHashSize = 2048;             // open-addressing table for the local set
 constexpr int kWarpCap = 32;                // largest local set a warp task holds
+constexpr int kWideCap = 128;               // largest local set a wide-warp task holds
+constexpr int kWideWords = 4;               // bitmap words per row of a wide-warp task
 
 // Task lists of one counting launch.  Sizes live on the device (`n`), so task
 // generation and counting run without a host round trip and can be graph-captured:
 //   n[0] = hub edge sub-tasks, n[1] = CTA vertex tasks, n[2] = warp vertex tasks,
-//   n[3] = hub vertices.
+//   n[3] = hub vertices, n[4] = wide-warp vertex tasks.
 // Hub sub-task t belongs to hub split_v[h] with split_off[h] <= t < split_off[h+1];
 // its second vertex is the (t - split_off[h])-th out-neighbour of the hub.
 // Per-task timing logs (clock64 cycles) are indexed like the lists; any may be null.
 struct TaskLists {
   const int32_t* cta = nullptr;    // vertex tasks run by one CTA (out-degree <= kCtaCap)
   const int32_t* warp = nullptr;   // vertex tasks run by one warp (out-degree <= kWarpCap)
+  const int32_t* wide = nullptr;   // vertex tasks run by one warp with 4-word rows (<= kWideCap)
   const int32_t* split_v = nullptr;
   const int64_t* split_off = nullptr;
   const int64_t* n = nullptr;
   long long* log_cta = nullptr;
   long long* log_warp = nullptr;
   long long* log_split = nullptr;
+  long long* log_wide = nullptr;
 };
 
 // Per-graph outputs of batched launches: task totals go to out[gid[v0] * stride + slot]
@@ -40,7 +44,7 @@ struct GOut {
 
 // Work-queue heads, zeroed before each launch.
 struct QueueHeads {
-  unsigned long long split, cta, warp, pad;
+  unsigned long long split, cta, warp, wide;
 };
 
 size_t clique_smem_bytes();

@@ -6,16 +6,18 @@
 namespace xgm {
 
 // Variant codes per vertex task (var[]).
-enum : uint8_t { VAR_WARP = 0, VAR_CTA = 1, VAR_SPLIT = 2, VAR_SKIP = 3 };
+enum : uint8_t { VAR_WARP = 0, VAR_CTA = 1, VAR_SPLIT = 2, VAR_WIDE = 3, VAR_SKIP = 4 };
+constexpr int kNumVar = 4;
 
 // Device buffers of one schedule; sized for a graph's vertex count and reused.
 struct TaskBuf {
   int64_t cap_v = 0;
   int32_t* cta = nullptr;
   int32_t* warp = nullptr;
+  int32_t* wide = nullptr;
   int32_t* split_v = nullptr;
   int64_t* split_off = nullptr;
-  int64_t* n = nullptr;       // [4] see TaskLists
+  int64_t* n = nullptr;       // [5] see TaskLists
   uint8_t* var = nullptr;     // [cap_v] variant per vertex
   uint8_t* flag = nullptr;    // [cap_v] scratch
   int64_t* pos = nullptr;     // [cap_v] scratch
@@ -34,9 +36,10 @@ void taskbuf_free(TaskBuf& tb, cudaStream_t s);
 // Plain degree-threshold heuristic (the role of WARP_LIMIT / BLOCK_LIMIT,
 // xgminer/include/glumin/common.h:114-116, and the |W| <= 32 switch of
 // clique5_warp_edge_taskallocate.cuh:26): out-degree s < k-1 -> skip,
-// s <= warp_max -> WARP, s <= cta_max -> CTA, else SPLIT.  Lists keep vertex order.
-cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int cta_max, TaskBuf& tb,
-                               cudaStream_t s);
+// s <= warp_max -> WARP, s <= wide_max -> WIDE, s <= cta_max -> CTA, else SPLIT.  Lists
+// keep vertex order.
+cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int wide_max, int cta_max,
+                               TaskBuf& tb, cudaStream_t s);
 
 // Variant per out-degree bucket (XGM_SCHED_TUNED); roots with out-degree < kmin skip.
 cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& tab, TaskBuf& tb,

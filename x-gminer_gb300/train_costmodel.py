@@ -59,19 +59,15 @@ def main():
         g = ctx.graph_from_edges(nv, s, d)
         del s, d
         for pat in PATTERNS:
-            for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT):
-                # pick a stride so that at most `rows` samples come back
-                X, y, _ = model.collect(g, pat, var, stride=1, max_rows=1)
-                probe_n = None
-                X, y, cnt = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
-                if len(y) > args.rows:
+            for var in (xgm.VAR_WARP, xgm.VAR_WIDE, xgm.VAR_CTA, xgm.VAR_SPLIT):
+                X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
+                if len(y) > args.rows:  # uniform subsample
                     idx = np.random.default_rng(scale * 7 + var).choice(len(y), args.rows,
                                                                         replace=False)
                     X, y = X[idx], y[idx]
                 Xs.append(X)
                 ys.append(y)
                 meta.append({"scale": scale, "pattern": pat, "variant": var, "rows": len(y)})
-                del probe_n
         g.close()
         print(f"collected scale {scale}: {sum(len(y) for y in ys)} rows, {time.time()-t0:.0f}s",
               flush=True)

@@ -1,0 +1,62 @@
+"""Command-line counter, the engine's counterpart of the reference's solver binaries.
+
+    python x-gminer_gb300/xgm_count.py --graph <prefix> --pattern 4-clique
+    python x-gminer_gb300/xgm_count.py --rmat 21 --pattern 5-clique [--policy heuristic]
+
+Mirrors `clique_omp_base <graph> <k>` / `count_omp_base <graph> <pattern>`
+(codes/GraphMiner/src/{clique,count}/main.cc) and xgminer's `--graph --patternID`
+(xgminer/include/cmd_option.h:30-159): loads a graph in the reference's binary CSR
+layout (or generates a seeded R-MAT), counts one pattern on the GPU and prints the
+count with the call's device timings as one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+xgm = importlib.import_module("x-gminer_gb300")
+
+# GLUMIN patternIDs of the supported patterns (xgminer/include/glumin.h:34-46 maps
+# patternID - 16 to the GLUMIN pattern; 4/5-clique are P4/P5)
+PATTERN_IDS = {20: "4-clique", 21: "5-clique"}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    src = ap.add_mutually_exclusive_group(required=True)
+    src.add_argument("--graph", help="prefix of <prefix>.meta.txt / .vertex.bin / .edge.bin")
+    src.add_argument("--rmat", type=int, metavar="SCALE", help="seeded R-MAT, edge factor 16")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--pattern", default="4-clique")
+    ap.add_argument("--patternID", type=int, help="reference pattern id (20: 4-clique, 21: 5-clique)")
+    ap.add_argument("--policy", choices=["heuristic", "learned"], default="heuristic")
+    ap.add_argument("--repeat", type=int, default=1)
+    args = ap.parse_args()
+    pattern = PATTERN_IDS.get(args.patternID, args.pattern) if args.patternID else args.pattern
+    ctx = xgm.Context(0)
+    if args.graph:
+        g = ctx.load_graph(args.graph)
+    else:
+        nv, s, d = xgm.gen_rmat(args.rmat, 16, seed=args.seed)
+        g = ctx.graph_from_edges(nv, s, d)
+    kw = {}
+    if args.policy == "learned":
+        spec = json.load(open(os.path.join(HERE, "costmodel.json")))
+        import numpy as np
+
+        m = xgm.Model(ctx)
+        m.set_params(np.asarray(spec["params"], dtype=np.float32))
+        kw = {"policy": xgm.SCHED_LEARNED, "model": m}
+    for _ in range(args.repeat):
+        count, st = ctx.count(g, pattern, with_stats=True, **kw)
+        print(json.dumps({"pattern": pattern, "count": count, "graph": g.info(), **st}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
