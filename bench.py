@@ -160,15 +160,18 @@ def load_engine():
 
 
 def load_model(xgm, ctx):
+    """The trained cost model (x-gminer_gb300/costmodel.json) and its queue order."""
     if not os.path.exists(COSTMODEL):
-        return None
+        return None, 1
     with open(COSTMODEL) as f:
         spec = json.load(f)
+    if spec.get("features") != xgm.MODEL_FEATURES or len(spec["params"]) != xgm.MODEL_PARAMS:
+        return None, 1
     import numpy as np
 
     m = xgm.Model(ctx)
     m.set_params(np.asarray(spec["params"], dtype=np.float32))
-    return m
+    return m, int(spec.get("order_by_cost", 1))
 
 
 def measured_peaks() -> dict:
@@ -229,9 +232,9 @@ def engine_arm(args, dist: Dist) -> None:
     g = ctx.graph_from_edges(nv, src, dst)
     del src, dst
     info = g.info()
-    model = load_model(xgm, ctx) if args.policy == "learned" else None
+    model, order = load_model(xgm, ctx) if args.policy == "learned" else (None, 1)
     policy = xgm.SCHED_LEARNED if model is not None else xgm.SCHED_HEURISTIC
-    kw = {"policy": policy, "model": model}
+    kw = {"policy": policy, "model": model, "order_by_cost": order}
 
     def run(n, **k):
         prep, kern, cnt = [], [], None

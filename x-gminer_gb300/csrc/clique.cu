@@ -135,45 +135,6 @@ enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 
 // Count of (q)-cliques in the local DAG held by the CTA (q >= 3 uses the bitmap).  WGT
 // (Q == 3 only) weights each clique by d+ of its top member, d+(S[l]) = pre[l+1]-pre[l].
-//
-// A warp owns row i (words qi..W-1, nwi of them).  It splits into groups of
-// G = next_pow2(nwi) lanes; lane p of a group holds word qi+p, so each group can take a
-// different set bit j of row i per round: the group finds the rank-n bit with a
-// group-local prefix of popcounts, a ballot and __fns.  For Q == 4 each group then
-// walks the bits l of m = row_i & row_j the same way.  Short rows (most rows of small
-// tasks and the second half of every task) thus process 32/G bits at a time.
-__device__ __forceinline__ int group_width(int nwi) {
-  return nwi <= 1 ? 1 : nwi <= 2 ? 2 : nwi <= 4 ? 4 : nwi <= 8 ? 8 : nwi <= 16 ? 16 : 32;
-}
-
-// Rank-n set bit of the group's distributed word (lane p holds word qi+p; incl/excl are
-// group-local inclusive/exclusive popcount prefixes).  Returns the local bit index
-// (relative to word qi) or -1 when n is out of range; called by all 32 lanes.
-__device__ __forceinline__ int group_nth_bit(uint32_t word, int incl, int excl, int n, bool act,
-                                             int g, int G) {
-  const unsigned bal = __ballot_sync(kFull, act && incl <= n);
-  const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << (g * G));
-  const int pstar = __popc(bal & gmask);
-  const int src = g * G + (pstar < G ? pstar : G - 1);
-  const uint32_t wsrc = __shfl_sync(kFull, word, src);
-  const int ex = __shfl_sync(kFull, excl, src);
-  if (!act) return -1;
-  return (pstar << 5) + (int)__fns(wsrc, 0, n - ex + 1);
-}
-
-__device__ __forceinline__ void group_prefix(uint32_t word, int p, int G, int& incl, int& excl) {
-  const int c = __popc(word);
-  int v = c;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    if (o >= G) break;
-    const int y = __shfl_up_sync(kFull, v, o, G);
-    if (p >= o) v += y;
-  }
-  incl = v;
-  excl = v - c;
-}
-
 template <int Q, bool WGT>
 __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, const int32_t* pre) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -181,48 +142,44 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
   uint64_t acc = 0;
   for (int i = warp; i < s; i += kCtaWarps) {
     const int qi = i >> 5, nwi = W - qi;
-    const int G = group_width(nwi), NG = 32 / G;
-    const int g = lane / G, p = lane - g * G;
     const uint32_t* Ri = rows + tri_row_off(i, W);
-    const uint32_t wi = p < nwi ? Ri[p] : 0u;
-    const int w = qi + p;  // absolute word of this lane
-    int incl, excl;
-    group_prefix(wi, p, G, incl, excl);
-    const int T = __shfl_sync(kFull, incl, g * G + G - 1);  // bits in row i
-    for (int base = 0; base < T; base += NG) {
-      const int n = base + g;
-      const int jl = group_nth_bit(wi, incl, excl, n, n < T, g, G);
-      const int j = (qi << 5) + jl;
-      const int qj = j >> 5;
-      const uint32_t* Rj = rows + tri_row_off(j, W);
-      const uint32_t m = (jl >= 0 && p < nwi && w >= qj) ? (wi & Rj[w - qj]) : 0u;
-      if (Q == 3) {
-        if (WGT) {
-          uint32_t b3 = m;
-          while (b3) {
-            const int l = (w << 5) + __ffs(b3) - 1;
-            b3 &= b3 - 1;
-            acc += (uint64_t)(pre[l + 1] - pre[l]);
+    const uint32_t wi = lane < nwi ? Ri[lane] : 0u;
+    const int w = qi + lane;
+    unsigned nz = __ballot_sync(kFull, wi != 0u);
+    while (nz) {
+      const int src = __ffs(nz) - 1;
+      nz &= nz - 1;
+      uint32_t bits = __shfl_sync(kFull, wi, src);
+      while (bits) {
+        const int j = ((qi + src) << 5) + __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int qj = j >> 5;
+        const uint32_t* Rj = rows + tri_row_off(j, W);
+        const uint32_t m = (lane < nwi && w >= qj) ? (wi & Rj[w - qj]) : 0u;
+        if (Q == 3) {
+          if (WGT) {
+            uint32_t b3 = m;
+            while (b3) {
+              const int l = (w << 5) + __ffs(b3) - 1;
+              b3 &= b3 - 1;
+              acc += (uint64_t)(pre[l + 1] - pre[l]);
+            }
+          } else {
+            acc += __popc(m);
           }
         } else {
-          acc += __popc(m);
-        }
-      } else {
-        int incl2, excl2;
-        group_prefix(m, p, G, incl2, excl2);
-        const int T2 = __shfl_sync(kFull, incl2, g * G + G - 1);
-        int T2max = T2;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const int y = __shfl_xor_sync(kFull, T2max, o);
-          T2max = y > T2max ? y : T2max;
-        }
-        for (int n2 = 0; n2 < T2max; ++n2) {
-          const int ll = group_nth_bit(m, incl2, excl2, n2, n2 < T2, g, G);
-          if (ll >= 0) {
-            const int l = (qi << 5) + ll;
-            const int ql = l >> 5;
-            if (p < nwi && w >= ql && m) acc += __popc(m & rows[tri_row_off(l, W) + (w - ql)]);
+          unsigned nz2 = __ballot_sync(kFull, m != 0u);
+          while (nz2) {
+            const int src2 = __ffs(nz2) - 1;
+            nz2 &= nz2 - 1;
+            uint32_t bits2 = __shfl_sync(kFull, m, src2);
+            while (bits2) {
+              const int l = ((qi + src2) << 5) + __ffs(bits2) - 1;
+              bits2 &= bits2 - 1;
+              const int ql = l >> 5;
+              const uint32_t* Rl = rows + tri_row_off(l, W);
+              if (w >= ql && m) acc += __popc(m & Rl[w - ql]);
+            }
           }
         }
       }

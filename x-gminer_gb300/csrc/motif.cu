@@ -144,17 +144,44 @@ __device__ int c4_load_chunk(const GView& g, C4Smem& sm, int32_t v0, long long c
   return tot;
 }
 
-// Visits the v2 of every wedge of the loaded chunk (flattened, coalesced per row).
+// Visits the v2 of every wedge of the loaded chunk (flattened, coalesced per row): each
+// thread walks k = tid, tid + 256, ... keeping its segment (lower neighbour) in
+// registers, with four loads in flight per step.
 template <class F>
 __device__ __forceinline__ void c4_walk(const GView& g, const C4Smem& sm, int n, int total, F f) {
   const int tid = threadIdx.x;
-  for (int k = tid; k < total; k += kC4Threads) {
-    int lo = 0, hi = n;
+  if (tid >= total) return;
+  int i;
+  {
+    int lo = 0, hi = n;  // largest i with pre[i] <= tid
     while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (sm.pre[mid] <= k) lo = mid; else hi = mid;
+      const int mid = (lo + hi) >> 1;
+      if (sm.pre[mid] <= tid) lo = mid; else hi = mid;
     }
-    f(ldg_i32(g.col + sm.lb[lo] + (k - sm.pre[lo])));
+    i = lo;
+  }
+  int seg_end = sm.pre[i + 1];
+  long long seg_base = sm.lb[i] - sm.pre[i];
+  for (int kb = tid; kb < total; kb += 4 * kC4Threads) {
+    int32_t xv[4];
+    bool ok[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int k = kb + t * kC4Threads;
+      ok[t] = k < total;
+      xv[t] = 0;
+      if (ok[t]) {
+        while (k >= seg_end) {
+          ++i;
+          seg_end = sm.pre[i + 1];
+          seg_base = sm.lb[i] - sm.pre[i];
+        }
+        xv[t] = ldg_i32(g.col + seg_base + k);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (ok[t]) f(xv[t]);
   }
 }
 

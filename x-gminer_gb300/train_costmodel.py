@@ -83,20 +83,27 @@ def main():
     g = ctx.graph_from_edges(nv, s, d)
     del s, d
     evals = {}
-    for pat in ["4-clique", "5-clique", "diamond"]:
+    for pat in ["4-clique", "5-clique", "diamond", "triangle"]:
         c_h, t_h = timed_count(ctx, g, pat, 3)
-        c_l, t_l = timed_count(ctx, g, pat, 3, policy=xgm.SCHED_LEARNED, model=model)
-        assert c_h == c_l, (pat, c_h, c_l)
-        evals[pat] = {"count": c_h, "heuristic_ms": t_h, "learned_ms": t_l,
-                      "speedup": t_h / t_l}
-        print(pat, evals[pat], flush=True)
+        res = {"count": c_h, "heuristic_ms": t_h}
+        for order in (1, 0):
+            c_l, t_l = timed_count(ctx, g, pat, 3, policy=xgm.SCHED_LEARNED, model=model,
+                                   order_by_cost=order)
+            assert c_h == c_l, (pat, c_h, c_l)
+            res[f"learned_ms_order{order}"] = t_l
+        best = min(res["learned_ms_order1"], res["learned_ms_order0"])
+        res["speedup"] = t_h / best
+        evals[pat] = res
+        print(pat, res, flush=True)
     g.close()
+    order_gain = sum(v["learned_ms_order0"] - v["learned_ms_order1"] for v in evals.values())
     spec = {"params": [float(v) for v in model.params()],
             "features": xgm.MODEL_FEATURES, "hidden": xgm.MODEL_HIDDEN,
             "target": "log2(clock64 cycles x warps occupied) per vertex task and variant",
             "train": {"graphs": [f"rmat s{s} ef16 seed {10 + i}" for i, s in enumerate(args.scales)],
                       "patterns": PATTERNS, "rows": int(len(y)), "mse_initial": loss0,
                       "mse_final": loss, "epochs": args.epochs, "parts": meta},
+            "order_by_cost": 1 if order_gain > 0 else 0,
             "eval": {"graph": f"rmat s{args.eval_scale} ef16 seed 99", "results": evals}}
     with open(args.out, "w") as f:
         json.dump(spec, f, indent=1)
