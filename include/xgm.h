@@ -161,7 +161,8 @@ typedef enum {
   XGM_VAR_CTA = 1,    /* one CTA per task, frontier bitmap in shared memory */
   XGM_VAR_SPLIT = 2,  /* task split into per-edge sub-tasks (hub vertices) */
   XGM_VAR_WIDE = 3,   /* one warp per task, 4-word frontier bitmap rows (out-degree <= 128) */
-  XGM_NUM_VARIANTS = 4
+  XGM_VAR_SEARCH = 4, /* one warp per task (out-degree <= 32), rows by binary search */
+  XGM_NUM_VARIANTS = 5
 } xgm_variant;
 
 /* Autotuned schedule: the variant for each out-degree bucket.  Bucket b holds
@@ -182,6 +183,7 @@ typedef struct {
   const xgm_tune_table* table; /* for XGM_SCHED_TUNED */
   int flags;              /* XGM_SCHED_NO_GRAPH: batched calls launch directly, no CUDA graph */
   int wide_max;           /* heuristic: out-degree <= wide_max -> WIDE (0: default 128; -1: none) */
+  int search_max;         /* heuristic: out-degree <= search_max -> SEARCH (0: none) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };

@@ -78,3 +78,20 @@ def test_autotune_single_graph(xgm, ctx):
     base = ctx.count(g, "4-clique")
     res = ctx.autotune(g, "4-clique", reps=2)
     assert ctx.count(g, "4-clique", policy=xgm.SCHED_TUNED, table=res["table"]) == base
+
+
+def test_full_batch_config_matches_oracle(xgm, ctx, orc):
+    # the batched configuration at its full size: 4096 BA graphs, n in [100, 5000],
+    # m in {3..8}, seed 5; triangle + 4-clique + diamond per graph
+    vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=5)
+    b = ctx.batch_from_edges(vo, s, d)
+    got = ctx.count_batched(b, ["triangle", "4-clique", "diamond"])
+    assert got.shape == (4096, 3)
+    for g in range(4096):
+        lo = int(vo[g])
+        rowptr, col = orc.build_csr(int(vo[g + 1]) - lo, s[eo[g]:eo[g + 1]] - lo,
+                                    d[eo[g]:eo[g + 1]] - lo)
+        drow, dcol = orc.orient(rowptr, col)
+        want = (orc.count("tc", drow, dcol), orc.count("clique4", drow, dcol),
+                orc.count("diamond", rowptr, col))
+        assert tuple(int(x) for x in got[g]) == want, g

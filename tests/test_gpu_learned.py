@@ -42,11 +42,11 @@ def test_collect_and_learned_schedule_counts(xgm, ctx):
     g = ctx.graph_from_edges(nv, s, d)
     m = xgm.Model(ctx, seed=4)
     Xs, ys = [], []
-    for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE):
+    for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE, xgm.VAR_SEARCH):
         X, y, cnt = m.collect(g, "4-clique", var, stride=2, max_rows=50000)
         assert cnt == ctx.count(g, "4-clique")
         assert len(y) > 0 and np.all(np.isfinite(X)) and np.all(np.isfinite(y))
-        assert np.all(X[:, 8 + var] == 1.0)
+        assert np.all(X[:, 7 + var] == 1.0)
         Xs.append(X)
         ys.append(y)
     m.train(np.concatenate(Xs), np.concatenate(ys), epochs=10)

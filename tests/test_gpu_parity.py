@@ -63,11 +63,12 @@ def test_schedules_never_change_counts(xgm, ctx):
     g = ctx.graph_from_edges(nv, s, d)
     for pat in ("triangle", "4-clique", "5-clique", "diamond", "tailedtriangle"):
         base = ctx.count(g, pat)
-        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE):
+        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE, xgm.VAR_SEARCH):
             assert ctx.count(g, pat, policy=xgm.SCHED_FIXED, variant=var) == base, (pat, var)
-        for wmax, dmax, cmax in ((8, 0, 64), (32, 64, 128), (1, -1, 1), (16, 100, 2048)):
-            assert ctx.count(g, pat, warp_max=wmax, wide_max=dmax, cta_max=cmax) == base, \
-                (pat, wmax, dmax, cmax)
+        for smax, wmax, dmax, cmax in ((0, 8, 0, 64), (8, 32, 64, 128), (32, 1, -1, 1),
+                                       (4, 16, 100, 2048)):
+            assert ctx.count(g, pat, search_max=smax, warp_max=wmax, wide_max=dmax,
+                             cta_max=cmax) == base, (pat, smax, wmax, dmax, cmax)
 
 
 def test_upload_paths_agree(xgm, ctx, orc):
@@ -183,10 +184,12 @@ def test_plan_from_adjacency(xgm, ctx):
 
 
 def test_algo_bytes_match_oracle(xgm, ctx, orc):
-    nv, s, d = xgm.gen_rmat(12, 16, seed=17)
+    # scale 14: out-degrees above the clipping threshold exist, weights must be unclipped
+    nv, s, d = xgm.gen_rmat(14, 16, seed=17)
     g = ctx.graph_from_edges(nv, s, d)
     rowptr, col = orc.build_csr(nv, s, d)
     drow, dcol = orc.orient(rowptr, col)
+    assert g.info()["max_out_degree"] > 96
     for kind, pat in (("tc", "triangle"), ("clique4", "4-clique"), ("clique5", "5-clique")):
         assert ctx.algo_bytes(g, pat) == orc.algo_bytes(kind, drow, dcol), kind
     for kind, pat in (("diamond", "diamond"), ("tailed", "tailedtriangle")):

@@ -42,7 +42,7 @@ PATTERN_NAMES = {"triangle": TRIANGLE, "4-clique": CLIQUE4, "5-clique": CLIQUE5,
 SCHED_HEURISTIC, SCHED_LEARNED, SCHED_FIXED, SCHED_TUNED = 0, 1, 2, 3
 SCHED_NO_GRAPH = 1
 TUNE_BUCKETS = 16
-VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE = 0, 1, 2, 3
+VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH = 0, 1, 2, 3, 4
 
 MODEL_FEATURES, MODEL_HIDDEN = 12, 32
 MODEL_PARAMS = MODEL_HIDDEN * MODEL_FEATURES + 2 * MODEL_HIDDEN + 1
@@ -78,7 +78,8 @@ class TuneTable(C.Structure):
 class Sched(C.Structure):
     _fields_ = [("policy", C.c_int), ("variant", C.c_int), ("model", C.c_void_p),
                 ("warp_max", C.c_int), ("cta_max", C.c_int), ("order_by_cost", C.c_int),
-                ("table", C.c_void_p), ("flags", C.c_int), ("wide_max", C.c_int)]
+                ("table", C.c_void_p), ("flags", C.c_int), ("wide_max", C.c_int),
+                ("search_max", C.c_int)]
 
 
 class TuneResult(C.Structure):
@@ -88,7 +89,7 @@ class TuneResult(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("prep_ms", C.c_double), ("tasks", C.c_int64),
-                ("variant_tasks", C.c_int64 * 4), ("algo_bytes", C.c_uint64),
+                ("variant_tasks", C.c_int64 * 5), ("algo_bytes", C.c_uint64),
                 ("device_error", C.c_uint32), ("launches", C.c_int)]
 
     def as_dict(self) -> dict:
@@ -257,20 +258,20 @@ class Context:
 
     @staticmethod
     def _sched(policy=SCHED_HEURISTIC, variant=0, model=None, warp_max=0, cta_max=0,
-               order_by_cost=1, table=None, flags=0, wide_max=0):
+               order_by_cost=1, table=None, flags=0, wide_max=0, search_max=0):
         sp = Sched(policy, variant, model._h if model is not None else None, warp_max, cta_max,
                    order_by_cost, C.cast(C.pointer(table), C.c_void_p) if table is not None
-                   else None, flags, wide_max)
+                   else None, flags, wide_max, search_max)
         sp._keep = table  # keep the table alive with the struct
         return sp
 
     def count(self, graph: "Graph", pattern, policy: int = SCHED_HEURISTIC, variant: int = 0,
               model: Optional["Model"] = None, warp_max: int = 0, cta_max: int = 0,
               order_by_cost: int = 1, table: Optional[TuneTable] = None,
-              wide_max: int = 0, with_stats: bool = False):
+              wide_max: int = 0, search_max: int = 0, with_stats: bool = False):
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
         sp = self._sched(policy, variant, model, warp_max, cta_max, order_by_cost, table,
-                         wide_max=wide_max)
+                         wide_max=wide_max, search_max=search_max)
         out = C.c_uint64()
         st = Stats()
         _check(lib().xgm_count(self._h, graph._h, plan._h, C.byref(sp), C.byref(out),

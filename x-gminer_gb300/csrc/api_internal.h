@@ -16,7 +16,7 @@ struct Scalars {
   uint32_t pad;
   QueueHeads q;
   unsigned long long c4heads[2];
-  int64_t n[6];  // task list sizes, copied back for the stats
+  int64_t n[8];  // task list sizes, copied back for the stats
 };
 
 struct Model;  // learned cost model (learned.cu)

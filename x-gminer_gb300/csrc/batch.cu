@@ -505,7 +505,7 @@ xgm_status xgm_autotune(xgm_ctx* ctx, const xgm_graph* g, xgm_batch* b, const xg
       uint8_t bestv = keep;
       for (uint8_t v = 0; v < XGM_NUM_VARIANTS; ++v) {
         if (v == keep) continue;
-        if (v == XGM_VAR_WARP && smin > kWarpCap) continue;
+        if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && smin > kWarpCap) continue;
         if (v == XGM_VAR_WIDE && smin > kWideCap) continue;
         if (v == XGM_VAR_CTA && smin > kCtaCap) continue;
         tab.variant[k] = v;

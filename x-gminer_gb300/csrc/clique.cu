@@ -238,7 +238,8 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   for (int i = tid; i < s; i += kCtaThreads) {
     const longlong2 d = ldg_ll2(g.dptr + S[i]);
     long long hi = d.y;
-    if (d.y - d.x > kClipMin && ldg_i32(g.col + d.y - 1) > smax0) {
+    // (not in weighted mode: its weights are the full out-degrees pre[j+1] - pre[j])
+    if (!WGT && d.y - d.x > kClipMin && ldg_i32(g.col + d.y - 1) > smax0) {
       long long lo = d.x;
       while (lo < hi) {
         const long long mid = (lo + hi) >> 1;
@@ -425,7 +426,7 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   }
   const int32_t smax = __shfl_sync(kFull, xs, s - 1);
   // clip long lists at max(S) (members above it cannot hit)
-  if (lane < s && len > kClipMin && ldg_i32(g.col + dx.y - 1) > smax) {
+  if (!WGT && lane < s && len > kClipMin && ldg_i32(g.col + dx.y - 1) > smax) {
     long long lo = dx.x, hi = dx.y;
     while (lo < hi) {
       const long long mid = (lo + hi) >> 1;
@@ -541,6 +542,111 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   return acc;
 }
 
+// One warp, local set S = N+(v0) with s <= 32, rows built by binary search instead of
+// streaming: for row i, lane j-i-1 looks S[j] (j > i) up in the sorted N+(S[i]) (clipped
+// at max(S) outside the weighted mode) and a ballot gives the row.  Work per task is
+// ~ s^2/2 * log2(list length) dependent loads instead of the sum of the list lengths, so
+// it wins for small local sets with long neighbour lists (the merge-vs-binary-search
+// choice of the reference's intersection primitives, operations.cuh:106-114).
+template <int Q, int MODE>
+__device__ uint64_t warp_search_task(const GView& g, WarpSmem& w, int32_t v0, Part part,
+                                     uint64_t* q2out = nullptr) {
+  static_assert(Q >= 2, "search tasks count at least local edges");
+  constexpr bool MULTI = MODE == kModeMulti;
+  constexpr bool PART = MODE == kModePart || MULTI;
+  constexpr bool WGT = MODE == kModeWeight;
+  const int lane = threadIdx.x & 31;
+  const longlong2 d0 = ldg_ll2(g.dptr + v0);
+  const int s = (int)(d0.y - d0.x);
+  int32_t xs = 0;
+  longlong2 dx = make_longlong2(0, 0);
+  if (lane < s) {
+    xs = ldg_i32(g.col + d0.x + lane);
+    w.S[lane] = xs;
+    dx = ldg_ll2(g.dptr + xs);
+    w.lb[lane] = dx.x;
+  }
+  const int32_t smax = __shfl_sync(kFull, xs, s - 1);
+  long long hi_end = dx.y;
+  if (!WGT && lane < s && dx.y - dx.x > kClipMin && ldg_i32(g.col + dx.y - 1) > smax) {
+    long long lo = dx.x, hi = dx.y;
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      if (ldg_i32(g.col + mid) <= smax) lo = mid + 1; else hi = mid;
+    }
+    hi_end = lo;
+  }
+  w.pre[lane] = (int32_t)(dx.y - dx.x);  // full out-degree (the weighted mode's weights)
+  w.rows[lane] = 0u;
+  w.cnt[lane] = 0u;
+  __syncwarp();
+  uint64_t acc = 0, q2 = 0;
+  for (int i = 0; i + 1 < s; ++i) {
+    const long long a = __shfl_sync(kFull, dx.x, i), b = __shfl_sync(kFull, hi_end, i);
+    const int j = i + 1 + lane;
+    bool found = false;
+    long long at = 0;
+    if (j < s) {
+      const int32_t y = w.S[j];
+      long long lo = a, hi = b;
+      while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (ldg_i32(g.col + mid) < y) lo = mid + 1; else hi = mid;
+      }
+      found = lo < b && ldg_i32(g.col + lo) == y;
+      at = lo;
+    }
+    const unsigned bal = __ballot_sync(kFull, found);
+    if (Q == 2) {
+      if (found) acc += WGT ? (uint64_t)w.pre[j] : 1;
+    } else if (lane == 0) {
+      w.rows[i] = bal << (i + 1);
+    }
+    if (PART && found) {
+      atomicAdd(&w.cnt[j], 1u);
+      atomicAdd(&part.e[at], 1u);
+    }
+    if (lane == 0 && PART && bal) atomicAdd(&w.cnt[i], (unsigned)__popc(bal));
+    if (MULTI && found) q2 += 1;
+  }
+  if (MULTI) *q2out = q2;
+  __syncwarp();
+  if (PART && lane < s && w.cnt[lane]) {
+    atomicAdd(&part.v[w.S[lane]], (unsigned long long)w.cnt[lane]);
+    atomicAdd(&part.e[d0.x + lane], w.cnt[lane]);
+  }
+  if (Q >= 3 && lane < s) {
+    const uint32_t r = w.rows[lane];
+    uint32_t bits = r;
+    while (bits) {
+      const int j = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const uint32_t m = r & w.rows[j];
+      if (Q == 3) {
+        if (WGT) {
+          uint32_t b3 = m;
+          while (b3) {
+            const int l = __ffs(b3) - 1;
+            b3 &= b3 - 1;
+            acc += (uint64_t)w.pre[l];
+          }
+        } else {
+          acc += __popc(m);
+        }
+      } else {
+        uint32_t b2 = m;
+        while (b2) {
+          const int l = __ffs(b2) - 1;
+          b2 &= b2 - 1;
+          acc += __popc(m & w.rows[l]);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  return acc;
+}
+
 // One warp, local set S = N+(v0) with s <= 128 (rows of 4 words): Q-cliques of the
 // local DAG.  Same walk as the CTA tier (segment registers, four loads in flight, Bloom
 // pre-filter) with binary search in S; counting gives each lane whole rows.
@@ -576,7 +682,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
   const int32_t smax = w.S[s - 1];
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
-    if (len[t] > kClipMin && ldg_i32(g.col + lbv[t] + len[t] - 1) > smax) {
+    if (!WGT && len[t] > kClipMin && ldg_i32(g.col + lbv[t] + len[t] - 1) > smax) {
       long long lo = lbv[t], hi = lbv[t] + len[t];
       while (lo < hi) {
         const long long mid = (lo + hi) >> 1;
@@ -750,7 +856,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
   __shared__ long long task_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long n_split = t.n[0], n_cta = t.n[1], n_warp = t.n[2], n_hubs = t.n[3];
-  const long long n_wide = t.n[4];
+  const long long n_wide = t.n[4], n_search = t.n[5];
   uint64_t acc = 0;
 
   // 1) hub edge sub-tasks: local set N+(v0) & N+(v1), (K-2)-cliques of it
@@ -856,8 +962,33 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
       if (t.log_wide && lane == 0) t.log_wide[ti] = clock64() - c0;
     }
   }
-  // 4) warp vertex tasks (s <= 32), in a region disjoint from every wide region
+  // 4) warp vertex tasks (s <= 32), in a region disjoint from every wide region: first
+  //    those built by binary search, then those built by streaming
   WarpSmem& ws = ((WarpSmem*)(sm + kOffWarpRegion))[warp];
+  for (;;) {
+    long long ti = 0;
+    if (lane == 0) ti = (long long)atomicAdd(&q->search, 1ull);
+    ti = __shfl_sync(kFull, ti, 0);
+    if (ti >= n_search) break;
+    const long long c0 = t.log_search ? clock64() : 0;
+    const int32_t v0 = t.search[ti];
+    const longlong2 d0 = ldg_ll2(g.dptr + v0);
+    const int s = (int)(d0.y - d0.x);
+    if (s > kWarpCap) {
+      if (lane == 0) atomicOr(err, ERR_CAPACITY);
+    } else if (s >= kMinS) {
+      uint64_t q2 = 0;
+      const uint64_t r = warp_search_task<K - 1, MODE>(g, ws, v0, part, &q2);
+      if (PART) {
+        const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
+        if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
+      }
+      if (MULTI) emit(o, v0, q2, r, acc);
+      else if (MODE == kModeWeight) acc += r;
+      else if (!PART) emit(o, v0, r, 0, acc);
+    }
+    if (t.log_search && lane == 0) t.log_search[ti] = clock64() - c0;
+  }
   for (;;) {
     long long ti = 0;
     if (lane == 0) ti = (long long)atomicAdd(&q->warp, 1ull);

@@ -15,7 +15,7 @@ constexpr int kWideWords = 4;               // bitmap words per row of a wide-wa
 // Task lists of one counting launch.  Sizes live on the device (`n`), so task
 // generation and counting run without a host round trip and can be graph-captured:
 //   n[0] = hub edge sub-tasks, n[1] = CTA vertex tasks, n[2] = warp vertex tasks,
-//   n[3] = hub vertices, n[4] = wide-warp vertex tasks.
+//   n[3] = hub vertices, n[4] = wide-warp vertex tasks, n[5] = binary-search warp tasks.
 // Hub sub-task t belongs to hub split_v[h] with split_off[h] <= t < split_off[h+1];
 // its second vertex is the (t - split_off[h])-th out-neighbour of the hub.
 // Per-task timing logs (clock64 cycles) are indexed like the lists; any may be null.
@@ -23,6 +23,7 @@ struct TaskLists {
   const int32_t* cta = nullptr;    // vertex tasks run by one CTA (out-degree <= kCtaCap)
   const int32_t* warp = nullptr;   // vertex tasks run by one warp (out-degree <= kWarpCap)
   const int32_t* wide = nullptr;   // vertex tasks run by one warp with 4-word rows (<= kWideCap)
+  const int32_t* search = nullptr; // warp tasks (<= kWarpCap) built by binary search
   const int32_t* split_v = nullptr;
   const int64_t* split_off = nullptr;
   const int64_t* n = nullptr;
@@ -30,6 +31,7 @@ struct TaskLists {
   long long* log_warp = nullptr;
   long long* log_split = nullptr;
   long long* log_wide = nullptr;
+  long long* log_search = nullptr;
 };
 
 // Per-graph outputs of batched launches: task totals go to out[gid[v0] * stride + slot]
@@ -44,7 +46,7 @@ struct GOut {
 
 // Work-queue heads, zeroed before each launch.
 struct QueueHeads {
-  unsigned long long split, cta, warp, wide;
+  unsigned long long split, cta, warp, wide, search, pad[3];
 };
 
 size_t clique_smem_bytes();

@@ -63,12 +63,14 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
     }
     XGM_CUDA_TRY(classify_table(g, k - 1, *sp.table, tb, s));
   } else {
+    int smax = sp.search_max > 0 ? sp.search_max : 0;
     int wmax = sp.warp_max > 0 ? sp.warp_max : kWarpCap;
     int dmax = sp.wide_max > 0 ? sp.wide_max : (sp.wide_max < 0 ? 0 : kWideCap);
     int cmax = sp.cta_max > 0 ? sp.cta_max : kCtaCap;
     if (sp.policy == XGM_SCHED_FIXED) {
       switch (sp.variant) {
         case XGM_VAR_WARP: wmax = kWarpCap; dmax = kWideCap; cmax = kCtaCap; break;
+        case XGM_VAR_SEARCH: smax = kWarpCap; wmax = 0; dmax = kWideCap; cmax = kCtaCap; break;
         case XGM_VAR_WIDE: wmax = 0; dmax = kWideCap; cmax = kCtaCap; break;
         case XGM_VAR_CTA: wmax = 0; dmax = 0; cmax = kCtaCap; break;
         case XGM_VAR_SPLIT: wmax = 0; dmax = 0; cmax = 0; break;
@@ -80,7 +82,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
       set_thread_error("unknown schedule policy");
       return XGM_ERR_INVALID;
     }
-    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s));
+    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax));
   }
   XGM_CUDA_TRY(build_lists(g, tb, order, s));
   return XGM_OK;
@@ -181,7 +183,7 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   }
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   if (k || pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_TAILED_TRIANGLE)
-    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 5,
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 6,
                                  cudaMemcpyDeviceToDevice, s));
   xgm_status r = ctx_sync_scalars(ctx);
   if (r != XGM_OK) return r;
@@ -196,7 +198,9 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   st.variant_tasks[XGM_VAR_CTA] = ctx->h_sc->n[1];
   st.variant_tasks[XGM_VAR_SPLIT] = ctx->h_sc->n[0];
   st.variant_tasks[XGM_VAR_WIDE] = ctx->h_sc->n[4];
-  st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4];
+  st.variant_tasks[XGM_VAR_SEARCH] = ctx->h_sc->n[5];
+  st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4] +
+             ctx->h_sc->n[5];
   r = check_device_flag(ctx, ctx->h_sc->err);
   if (r != XGM_OK) return r;
   *out = ctx->h_sc->count;

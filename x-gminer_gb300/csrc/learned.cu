@@ -23,6 +23,10 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// A task leaves the heuristic's variant only for a predicted saving of at least 0.2 in
+// log2 warp-cycles (~15%): near-ties are where the model is least reliable.
+constexpr float kLearnedMargin = 0.2f;
+
 inline unsigned grid_for(int64_t n) {
   int64_t b = (n + kThreads - 1) / kThreads;
   if (b < 1) b = 1;
@@ -32,7 +36,7 @@ inline unsigned grid_for(int64_t n) {
 
 // Warps a task of each variant occupies while it runs (resource-time weight).
 __host__ __device__ inline float variant_warps(int v) {
-  return (v == XGM_VAR_WARP || v == XGM_VAR_WIDE) ? 1.0f : (float)kCtaWarps;
+  return (v == XGM_VAR_CTA || v == XGM_VAR_SPLIT) ? (float)kCtaWarps : 1.0f;
 }
 
 // Features of vertex task r (variant one-hot left zero for the caller).
@@ -49,7 +53,7 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
     maxd = l > maxd ? l : maxd;
   }
   const long long deg = d0.y - g.rowptr[r];
-  // 0-5 task shape, 6 clique depth, 7 bitmap words, 8-11 variant one-hot (caller)
+  // 0-5 task shape, 6 clique depth, 7-11 variant one-hot (caller)
   f[0] = log2f(1.0f + (float)s) / 11.0f;
   f[1] = log2f(1.0f + (float)sum) / 24.0f;
   f[2] = log2f(1.0f + (float)maxd) / 11.0f;
@@ -57,8 +61,7 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   f[4] = log2f(1.0f + (float)sumsq) / 34.0f;
   f[5] = (float)(sum / ((double)s * (double)maxd + 1.0));
   f[6] = (float)(k - 3) * 0.5f;
-  f[7] = log2f(1.0f + (float)s * (float)((s + 31) / 32)) / 16.0f;
-  f[8] = f[9] = f[10] = f[11] = 0.0f;
+  f[7] = f[8] = f[9] = f[10] = f[11] = 0.0f;
 }
 
 __device__ __forceinline__ float mlp_forward(const float* P, const float* f) {
@@ -92,22 +95,28 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
     }
     float f[kFeat];
     task_features(g, (int32_t)r, k, f);
-    float best = 3.0e38f;
-    uint8_t bv = VAR_SPLIT;
+    // the plain heuristic's variant stays unless the model predicts a clear saving
+    const uint8_t hv = s <= kWarpCap ? VAR_WARP : s <= kWideCap ? VAR_WIDE
+                       : s <= kCtaCap ? VAR_CTA : VAR_SPLIT;
+    float pred[XGM_NUM_VARIANTS];
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v) {
-      if (v == XGM_VAR_WARP && s > kWarpCap) continue;
+      pred[v] = 3.0e38f;
+      if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && s > kWarpCap) continue;
       if (v == XGM_VAR_WIDE && s > kWideCap) continue;
       if (v == XGM_VAR_CTA && s > kCtaCap) continue;
-      f[8 + v] = 1.0f;
-      const float c = mlp_forward(P, f);
-      f[8 + v] = 0.0f;
-      if (c < best) {
-        best = c;
+      f[7 + v] = 1.0f;
+      pred[v] = mlp_forward(P, f);
+      f[7 + v] = 0.0f;
+    }
+    uint8_t bv = hv;
+    float best = pred[hv];
+    for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
+      if (pred[v] < best - (v == hv ? 0.0f : kLearnedMargin)) {
+        best = pred[v] + kLearnedMargin;  // later candidates must beat the incumbent too
         bv = (uint8_t)v;
       }
-    }
     var[r] = bv;
-    cost[r] = best;
+    cost[r] = pred[bv];
   }
 }
 
@@ -204,7 +213,7 @@ __global__ void k_assemble(GView g, int k, int variant, const int32_t* list, con
     if ((int64_t)o >= max_rows) continue;
     float* f = X + o * kFeat;
     task_features(g, r, k, f);
-    f[8 + variant] = 1.0f;
+    f[7 + variant] = 1.0f;
     Y[o] = log2f((float)fmax(cyc, 1.0) * variant_warps(variant));
   }
 }
@@ -406,18 +415,19 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   TaskBuf& tb = ctx->tb;
   XGM_CUDA_TRY(cudaSetDevice(ctx->device));
   XGM_CUDA_TRY(taskbuf_reserve(tb, G.nv, s));
-  const int64_t need = 3 * tb.cap_v + (G.ne_dag > 0 ? G.ne_dag : 1);
+  const int64_t need = 4 * tb.cap_v + (G.ne_dag > 0 ? G.ne_dag : 1);
   if (tb.log_cap < need) {
     if (tb.log) cudaFreeAsync(tb.log, s);
     tb.log = nullptr;
     XGM_CUDA_TRY(cudaMallocAsync(&tb.log, sizeof(long long) * need, s));
     tb.log_cap = need;
   }
-  int wmax = kWarpCap, dmax = kWideCap, cmax = kCtaCap;
+  int smax = 0, wmax = kWarpCap, dmax = kWideCap, cmax = kCtaCap;
+  if (variant == XGM_VAR_SEARCH) smax = kWarpCap;
   if (variant == XGM_VAR_WIDE) wmax = 0;
   if (variant == XGM_VAR_CTA) wmax = dmax = 0;
   if (variant == XGM_VAR_SPLIT) wmax = dmax = cmax = 0;
-  XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s));
+  XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s, smax));
   XGM_CUDA_TRY(build_lists(G, tb, false, s));
   XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
   XGM_CUDA_TRY(launch_clique(k, G.view(), tb.lists(true), &ctx->d_sc->q, &ctx->d_sc->count,
@@ -427,15 +437,21 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   XGM_CUDA_TRY(cudaMallocAsync(&dx, sizeof(float) * cap * kFeat, s));
   XGM_CUDA_TRY(cudaMallocAsync(&dy, sizeof(float) * cap, s));
   const TaskLists tl = tb.lists(true);
-  const int32_t* list = variant == XGM_VAR_WARP  ? tb.warp
-                        : variant == XGM_VAR_CTA ? tb.cta
-                        : variant == XGM_VAR_WIDE ? tb.wide
-                                                  : tb.split_v;
-  const int nidx = variant == XGM_VAR_WARP ? 2 : variant == XGM_VAR_CTA ? 1 : variant == XGM_VAR_WIDE ? 4 : 3;
-  const long long* lg = variant == XGM_VAR_WARP  ? tl.log_warp
-                        : variant == XGM_VAR_CTA ? tl.log_cta
-                        : variant == XGM_VAR_WIDE ? tl.log_wide
-                                                  : tl.log_split;
+  const int32_t* list = variant == XGM_VAR_WARP     ? tb.warp
+                        : variant == XGM_VAR_CTA    ? tb.cta
+                        : variant == XGM_VAR_WIDE   ? tb.wide
+                        : variant == XGM_VAR_SEARCH ? tb.search
+                                                    : tb.split_v;
+  const int nidx = variant == XGM_VAR_WARP     ? 2
+                   : variant == XGM_VAR_CTA    ? 1
+                   : variant == XGM_VAR_WIDE   ? 4
+                   : variant == XGM_VAR_SEARCH ? 5
+                                               : 3;
+  const long long* lg = variant == XGM_VAR_WARP     ? tl.log_warp
+                        : variant == XGM_VAR_CTA    ? tl.log_cta
+                        : variant == XGM_VAR_WIDE   ? tl.log_wide
+                        : variant == XGM_VAR_SEARCH ? tl.log_search
+                                                    : tl.log_split;
   k_assemble<<<grid_for(G.nv), kThreads, 0, s>>>(G.view(), k, variant, list, tb.n, nidx, lg,
                                                  tb.split_off, stride, dx, dy, max_rows,
                                                  &ctx->d_sc->aux);

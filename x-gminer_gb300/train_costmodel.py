@@ -59,7 +59,7 @@ def main():
         g = ctx.graph_from_edges(nv, s, d)
         del s, d
         for pat in PATTERNS:
-            for var in (xgm.VAR_WARP, xgm.VAR_WIDE, xgm.VAR_CTA, xgm.VAR_SPLIT):
+            for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_WIDE, xgm.VAR_CTA, xgm.VAR_SPLIT):
                 X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
                 if len(y) > args.rows:  # uniform subsample
                     idx = np.random.default_rng(scale * 7 + var).choice(len(y), args.rows,
