@@ -44,7 +44,8 @@ constexpr int kOffRows = kOffCnt + 4 * kCtaCap;
 constexpr int kRowsWords = 16896;  // tri_words(1024)
 constexpr int kBloomWords = 512;  // 16 Kbit membership pre-filter of the local set
 constexpr int kOffBloom = kOffRows + 4 * kRowsWords;
-constexpr int kOffMisc = kOffBloom + 4 * kBloomWords;
+constexpr int kOffRowOff = kOffBloom + 4 * kBloomWords;  // int32[kCtaCap] row offsets
+constexpr int kOffMisc = kOffRowOff + 4 * kCtaCap;
 constexpr int kCtaSmem = kOffMisc + 8 * 16;
 constexpr int kClipMin = 96;  // lists longer than this are clipped at max(S)
 
@@ -136,13 +137,14 @@ enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 // Count of (q)-cliques in the local DAG held by the CTA (q >= 3 uses the bitmap).  WGT
 // (Q == 3 only) weights each clique by d+ of its top member, d+(S[l]) = pre[l+1]-pre[l].
 template <int Q, bool WGT>
-__device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, const int32_t* pre) {
+__device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, const int32_t* pre,
+                                                   const int32_t* roff) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = (s + 31) >> 5;
   uint64_t acc = 0;
   for (int i = warp; i < s; i += kCtaWarps) {
     const int qi = i >> 5, nwi = W - qi;
-    const uint32_t* Ri = rows + tri_row_off(i, W);
+    const uint32_t* Ri = rows + roff[i];
     const uint32_t wi = lane < nwi ? Ri[lane] : 0u;
     const int w = qi + lane;
     unsigned nz = __ballot_sync(kFull, wi != 0u);
@@ -154,7 +156,7 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
         const int j = ((qi + src) << 5) + __ffs(bits) - 1;
         bits &= bits - 1;
         const int qj = j >> 5;
-        const uint32_t* Rj = rows + tri_row_off(j, W);
+        const uint32_t* Rj = rows + roff[j];
         const uint32_t m = (lane < nwi && w >= qj) ? (wi & Rj[w - qj]) : 0u;
         if (Q == 3) {
           if (WGT) {
@@ -177,7 +179,7 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
               const int l = ((qi + src2) << 5) + __ffs(bits2) - 1;
               bits2 &= bits2 - 1;
               const int ql = l >> 5;
-              const uint32_t* Rl = rows + tri_row_off(l, W);
+              const uint32_t* Rl = rows + roff[l];
               if (w >= ql && m) acc += __popc(m & Rl[w - ql]);
             }
           }
@@ -226,6 +228,9 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   const int W = (s + 31) >> 5;
 
   uint32_t* bloom = (uint32_t*)(sm + kOffBloom);
+  int32_t* roff = (int32_t*)(sm + kOffRowOff);  // word offset of row i (triangular layout)
+  if (Q >= 3)
+    for (int i = tid; i < s; i += kCtaThreads) roff[i] = tri_row_off(i, W);
   for (int h = tid; h < kHashSize; h += kCtaThreads) hkey[h] = -1;
   for (int h = tid; h < kBloomWords; h += kCtaThreads) bloom[h] = 0u;
   if (Q >= 3)
@@ -318,7 +323,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
             atomicAdd(&part.e[pv[t]], 1u);
           }
         } else {
-          atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
+          atomicOr(&rows[roff[ii] + (j >> 5) - (ii >> 5)], 1u << (j & 31));
           if (MULTI) {
             q2 += 1;
             atomicAdd(&cnt[ii], 1u);
@@ -338,8 +343,8 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
         atomicAdd(&part.e[sbase + i], cnt[i]);
       }
   }
-  if (Q == 3) acc = cta_count_rows<3, WGT>(rows, s, pre);
-  if (Q == 4) acc = cta_count_rows<4, false>(rows, s, pre);
+  if (Q == 3) acc = cta_count_rows<3, WGT>(rows, s, pre, roff);
+  if (Q == 4) acc = cta_count_rows<4, false>(rows, s, pre, roff);
   return acc;
 }
 

@@ -104,6 +104,9 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
       if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && s > kWarpCap) continue;
       if (v == XGM_VAR_WIDE && s > kWideCap) continue;
       if (v == XGM_VAR_CTA && s > kCtaCap) continue;
+      // edge-splitting stays the capacity fallback: splitting a task a CTA can hold
+      // multiplies its set-up work and never paid off in any measured configuration
+      if (v == XGM_VAR_SPLIT && s <= kCtaCap) continue;
       f[7 + v] = 1.0f;
       pred[v] = mlp_forward(P, f);
       f[7 + v] = 0.0f;

@@ -71,6 +71,21 @@ def main():
         g.close()
         print(f"collected scale {scale}: {sum(len(y) for y in ys)} rows, {time.time()-t0:.0f}s",
               flush=True)
+    # the batched workload's graphs: 4096 Barabasi-Albert graphs packed as one graph
+    # (disjoint components; seed 6, not the benchmark's batch)
+    vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=6)
+    g = ctx.graph_from_edges(int(vo[-1]), s, d)
+    for pat in ["triangle", "4-clique", "diamond"]:
+        for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_WIDE, xgm.VAR_CTA):
+            X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
+            if len(y) > args.rows:
+                idx = np.random.default_rng(17 + var).choice(len(y), args.rows, replace=False)
+                X, y = X[idx], y[idx]
+            Xs.append(X)
+            ys.append(y)
+            meta.append({"graph": "ba x4096 seed 6", "pattern": pat, "variant": var,
+                         "rows": len(y)})
+    g.close()
     X = np.concatenate(Xs)
     y = np.concatenate(ys)
     loss0, _ = model.loss_grad(X, y)
@@ -97,6 +112,26 @@ def main():
         print(pat, res, flush=True)
     g.close()
     order_gain = sum(v["learned_ms_order0"] - v["learned_ms_order1"] for v in evals.values())
+    # batched form: the benchmark's 4096 BA graphs, triangle + 4-clique + diamond
+    vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=5)
+    b = ctx.batch_from_edges(vo, s, d)
+    pats = ["triangle", "4-clique", "diamond"]
+
+    def tb(**kw):
+        for _ in range(3):
+            ctx.count_batched(b, pats, **kw)
+        best, out = None, None
+        for _ in range(5):
+            out, st = ctx.count_batched(b, pats, with_stats=True, **kw)
+            best = st["kernel_ms"] if best is None else min(best, st["kernel_ms"])
+        return out, best
+
+    ob, th = tb()
+    ol, tl = tb(policy=xgm.SCHED_LEARNED, model=model, order_by_cost=1 if order_gain > 0 else 0)
+    assert np.array_equal(ob, ol)
+    evals["batch_ba4096"] = {"heuristic_ms": th, "learned_ms": tl, "speedup": th / tl}
+    print("batch", evals["batch_ba4096"], flush=True)
+    b.close()
     spec = {"params": [float(v) for v in model.params()],
             "features": xgm.MODEL_FEATURES, "hidden": xgm.MODEL_HIDDEN,
             "target": "log2(clock64 cycles x warps occupied) per vertex task and variant",
