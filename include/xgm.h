@@ -123,28 +123,46 @@ xgm_status xgm_graph_write_files(const char* prefix, const xgm_csr_host* csr);
 /* -------------------------------------------------------------------- plan */
 /* Builtin patterns.  Cliques and the triangle run on the degree-oriented DAG
  * (USE_DAG, codes/GraphMiner/include/defines.h:12); the other motifs are
- * edge-induced counts on the undirected graph (count/omp_base.cc:5-58). */
+ * edge-induced counts on the undirected graph (count/omp_base.cc:5-58) unless the
+ * plan is vertex-induced. */
 typedef enum {
   XGM_PATTERN_TRIANGLE = 1,
   XGM_PATTERN_CLIQUE4 = 2,
   XGM_PATTERN_CLIQUE5 = 3,
-  XGM_PATTERN_DIAMOND = 4,          /* edge-induced, diamond.h */
-  XGM_PATTERN_CYCLE4 = 5,           /* edge-induced, rectangle.h */
-  XGM_PATTERN_TAILED_TRIANGLE = 6   /* edge-induced, tailedtriangle.h */
+  XGM_PATTERN_DIAMOND = 4,          /* diamond.h; GLUMIN 4-diamond.yml */
+  XGM_PATTERN_CYCLE4 = 5,           /* rectangle.h; GLUMIN 4-cycle.yml */
+  XGM_PATTERN_TAILED_TRIANGLE = 6,  /* tailedtriangle.h; GLUMIN 4-tailed-triangle.yml */
+  XGM_PATTERN_WEDGE = 7,            /* 2-edge path; GLUMIN 3-path.yml, motif k = 3 */
+  XGM_PATTERN_STAR3 = 8,            /* K_{1,3}; GLUMIN 4-star.yml (P1) */
+  XGM_PATTERN_PATH4 = 9             /* 3-edge path; GLUMIN 4-path.yml */
 } xgm_pattern;
 
 typedef struct {
   int builtin;            /* xgm_pattern, or 0 to match `adj` */
   int num_vertices;       /* pattern size when builtin == 0 (3..5) */
   uint8_t adj[8][8];      /* pattern adjacency when builtin == 0 */
-  int induced;            /* 0: edge-induced (the only kind supported for motifs) */
+  int induced;            /* 0: edge-induced; 1: vertex-induced (the non-clique motifs are
+                             derived from edge-induced counts, the 4-clique count and the
+                             4-cycle count through exact identities; cliques are the same
+                             either way) */
 } xgm_plan_desc;
 
 xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* desc, xgm_plan** out);
-/* Plan for a reference pattern name ("triangle", "4-clique", "5-clique", "diamond",
- * "rectangle", "4-cycle", "tailedtriangle"; Pattern(name), count/main.cc:17) */
+/* Plan for a reference pattern name: the count app's names ("triangle", "4-clique",
+ * "5-clique", "diamond", "rectangle", "tailedtriangle"; Pattern(name),
+ * count/main.cc:17) and GLUMIN's .yml names ("3-triangle", "4-cycle", "4-diamond",
+ * "4-tailed-triangle", "3-path", "4-path", "4-star"), all edge-induced; and GLUMIN's
+ * pattern ids (codes/GLUMIN/src/G2Miner/main.cc:13-60), vertex-induced: "P1" (4-star),
+ * "P2" (4-diamond, reported as GLUMIN does: each diamond once per direction of its
+ * shared edge, i.e. twice), "P3" (4-tailed-triangle), "P4"/"P5" (4/5-clique). */
 xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out);
+/* Plan from a GLUMIN pattern description, the text of one of
+ * codes/GLUMIN/codegen/codegen/patterns/*.yml: its `edges: [AB, AC, ...]` list (vertices
+ * named by letters) is matched against the builtins.  GLUMIN's plans count
+ * vertex-induced embeddings (pass induced = 1 for the same meaning). */
+xgm_status xgm_plan_from_spec(xgm_ctx* ctx, const char* spec, int induced, xgm_plan** out);
 int xgm_plan_pattern(const xgm_plan* p);
+int xgm_plan_induced(const xgm_plan* p);
 void xgm_plan_destroy(xgm_plan* p);
 
 /* ---------------------------------------------------------------- schedule */
@@ -201,6 +219,14 @@ typedef struct {
 /* Counts `plan` on `g`.  out_count receives the exact uint64 total. */
 xgm_status xgm_count(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
                      const xgm_sched* sched, uint64_t* out_count, xgm_stats* stats);
+
+/* Vertex-induced k-motif census, replaces MotifSolver(g, k, total)
+ * (codes/GraphMiner/src/motif/omp_formula.cc:8, main.cc:8-31), same output order:
+ * k = 3 (n_counts >= 2): [wedges, triangles];
+ * k = 4 (n_counts >= 6): [3-stars, 4-paths, tailed triangles, 4-cycles, diamonds,
+ * 4-cliques]. */
+xgm_status xgm_motif_count(xgm_ctx* ctx, const xgm_graph* g, int k, const xgm_sched* sched,
+                           uint64_t* counts, int n_counts, xgm_stats* stats);
 
 /* Reference-shaped convenience entry points (same meaning as the solvers cited in the
  * file header; n_gpu / chunk arguments are dropped: one GPU, persistent queue). */

@@ -76,6 +76,8 @@ def lib():
             f = getattr(L, name)
             f.restype = U64
             f.argtypes = [I64, P, P, I64, I64, I64, I64]
+        L.orc_motif.restype = C.c_int
+        L.orc_motif.argtypes = [C.c_int, I64, P, P, I64, P]
         L.orc_algo_bytes.restype = U64
         L.orc_algo_bytes.argtypes = [C.c_int, I64, P, P, I64]
         _lib = L
@@ -141,6 +143,19 @@ def count(kind: str, rowptr: np.ndarray, col: np.ndarray, lo: int = 0, hi: int =
 ALGO_KIND = {"tc": 3, "clique4": 4, "clique5": 5, "diamond": 6, "cycle4": 7, "tailed": 8}
 
 
+def motif(k: int, rowptr: np.ndarray, col: np.ndarray) -> list:
+    """Vertex-induced k-motif census (k = 3: [wedges, triangles]; k = 4: [3-stars,
+    4-paths, tailed triangles, 4-cycles, diamonds, 4-cliques]) on the undirected CSR."""
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    nv = len(rowptr) - 1
+    md = int(np.diff(rowptr).max()) if nv else 0
+    out = np.zeros(6, dtype=np.uint64)
+    if lib().orc_motif(k, nv, rowptr.ctypes.data, col.ctypes.data, md, out.ctypes.data) != 0:
+        raise ValueError("motif census covers k = 3 and k = 4")
+    return [int(x) for x in out[: 2 if k == 3 else 6]]
+
+
 def algo_bytes(kind: str, rowptr: np.ndarray, col: np.ndarray) -> int:
     nv, rowptr, col = _args(rowptr, col)
     md = int(np.max(np.diff(rowptr))) if nv else 0
@@ -173,6 +188,22 @@ def run_ref(kind: str, prefix: str, threads_: int = 0) -> Tuple[int, float]:
     if not m:
         raise RuntimeError("unexpected reference output:\n" + r.stdout[-800:])
     return int(m.group(1)), float(t.group(1)) if t else float("nan")
+
+
+def run_ref_motif(k: int, prefix: str, threads_: int = 0) -> list:
+    """Runs the reference's motif_omp_formula (k = 3 or 4); returns its counts in order."""
+    env = dict(os.environ)
+    if threads_ > 0:
+        env["OMP_NUM_THREADS"] = str(threads_)
+    cmd = [os.path.join(REF_DIR, "motif_omp_formula"), prefix, str(k)]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd[0]} failed: {r.stderr[-500:]}")
+    found = dict((int(i), int(v)) for i, v in re.findall(r"pattern (\d+): (\d+)", r.stdout))
+    n = 2 if k == 3 else 6
+    if sorted(found) != list(range(n)):
+        raise RuntimeError("unexpected reference output:\n" + r.stdout[-800:])
+    return [found[i] for i in range(n)]
 
 
 def write_graph(prefix: str, rowptr: np.ndarray, col: np.ndarray) -> None:

@@ -8,6 +8,7 @@
 #   tc_omp_base     <- src/common/{graph,VertexSet}.cc src/triangle/{main,omp_base}.cc
 #   clique_omp_base <- src/common/{graph,VertexSet}.cc src/clique/{main,omp_base}.cc
 #   count_omp_base  <- + src/common/{pattern,intersect}.cc src/count/{main,omp_base}.cc
+#   motif_omp_formula <- src/common/{graph,VertexSet}.cc src/motif/{main,omp_formula}.cc
 #
 # count's intersect.cc uses x86 AVX2 intrinsics and rectangle.h misses <array>
 # under gcc 13, hence -mavx2 and -include array for that binary only; on hosts
@@ -33,6 +34,8 @@ build() {  # name, extra args...
 build tc_omp_base $COMMON "$GM/src/triangle/main.cc" "$GM/src/triangle/omp_base.cc" &
 build clique_omp_base -I"$GM/src/clique/cpu_kernels" $COMMON "$GM/src/clique/main.cc" \
   "$GM/src/clique/omp_base.cc" &
+build motif_omp_formula -I"$GM/src/motif/cpu_kernels" $COMMON "$GM/src/motif/main.cc" \
+  "$GM/src/motif/omp_formula.cc" &
 if [ "$(uname -m)" = "x86_64" ]; then
   build count_omp_base -mavx2 -include array -I"$GM/src/count/cpu_kernels" $COMMON \
     "$GM/src/common/pattern.cc" "$GM/src/common/intersect.cc" "$GM/src/count/main.cc" \

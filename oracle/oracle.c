@@ -15,6 +15,7 @@
  * Types follow codes/GraphMiner/include/common.h:36-40: vidType = int32,
  * eidType = int64, counts uint64.
  */
+#include <limits.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -327,6 +328,111 @@ uint64_t orc_tailed_triangle(int64_t nv, const int64_t* rowptr, const int32_t* c
     }
   }
   return counter;
+}
+
+/* Ordered-set difference a \ b, elements below `up`, skipping `skip` (the vertex whose
+ * neighbourhood b is): VertexSet::difference_buf, codes/GraphMiner/src/common/
+ * VertexSet.cc:21-67 (unbounded form: up = INT32_MAX). */
+static inline eid_t diff_set(const vid_t* a, eid_t na, const vid_t* b, eid_t nb, vid_t up,
+                             vid_t skip, vid_t* out) {
+  eid_t n = 0, l = 0, r = 0;
+  while (l < na && a[l] < up) {
+    vid_t x = a[l];
+    while (r < nb && b[r] < x) r++;
+    if ((r >= nb || b[r] != x) && x != skip) out[n++] = x;
+    l++;
+  }
+  return n;
+}
+
+/* Vertex-induced k-motif census (k = 3, 4) on the undirected graph:
+ * automine_3motif / automine_4motif, codes/GraphMiner/src/motif/cpu_kernels/
+ * automine_formula.h:2-57, followed by the formula post-processing of MotifSolver,
+ * src/motif/omp_formula.cc:38-48.  Output order as the reference prints it
+ * (main.cc:28-29): k = 3 [wedges, triangles]; k = 4 [3-stars, 4-paths, tailed
+ * triangles, 4-cycles, diamonds, 4-cliques].  Returns 0, or -1 for another k. */
+int orc_motif(int k, int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t max_deg,
+              uint64_t* out) {
+  uint64_t c[6] = {0, 0, 0, 0, 0, 0};
+  if (k == 3) {
+    uint64_t c0 = 0, c1 = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : c0, c1)
+    for (int64_t v0 = 0; v0 < nv; v0++) {
+      uint64_t n = (uint64_t)(rowptr[v0 + 1] - rowptr[v0]);
+      c0 += n * (n - (n > 0));
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+        int32_t v1 = col[e];
+        if (v1 >= v0) break;
+        c1 += isect_num_bound(ROW(v0), ROW(v1), v1);
+      }
+    }
+    out[0] = c0 / 2 - 3 * c1;
+    out[1] = c1;
+    return 0;
+  }
+  if (k != 4) return -1;
+  uint64_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0;
+#pragma omp parallel reduction(+ : c0, c1, c2, c3, c4, c5)
+  {
+    const size_t cap = (size_t)(max_deg + 1);
+    vid_t* y01 = (vid_t*)malloc(sizeof(vid_t) * cap);    /* y0f0y1f1 */
+    vid_t* n01 = (vid_t*)malloc(sizeof(vid_t) * cap);    /* n0f0y1 = N(v1) \ N(v0) */
+    vid_t* y0n1 = (vid_t*)malloc(sizeof(vid_t) * cap);   /* y0f0n1f1 */
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t v0 = 0; v0 < nv; v0++) {
+      const vid_t* y0 = col + rowptr[v0];
+      const eid_t d0 = rowptr[v0 + 1] - rowptr[v0];
+      eid_t nf0 = 0; /* |N(v0) below v0| */
+      while (nf0 < d0 && y0[nf0] < v0) nf0++;
+      for (eid_t i1 = 0; i1 < nf0; i1++) {
+        const int32_t v1 = y0[i1];
+        const vid_t* y1 = col + rowptr[v1];
+        const eid_t d1 = rowptr[v1 + 1] - rowptr[v1];
+        const uint64_t tri = isect_num(y0, d0, y1, d1);
+        const uint64_t su = (uint64_t)d0 - tri - 1, sv = (uint64_t)d1 - tri - 1;
+        c4 += tri * (tri - (tri > 0));
+        c2 += tri * (su + sv);
+        c1 += su * sv;
+        c0 += su * (su - (su > 0)) + sv * (sv - (sv > 0));
+        /* y0f0 & N(v1) below v1 */
+        eid_t n = 0;
+        {
+          eid_t l = 0, r = 0;
+          while (l < nf0 && r < d1) {
+            vid_t x = y0[l], y = y1[r];
+            if (x >= v1 || y >= v1) break;
+            if (x <= y) l++;
+            if (y <= x) r++;
+            if (x == y) y01[n++] = x;
+          }
+        }
+        const eid_t nn = diff_set(y1, d1, y0, d0, INT32_MAX, (vid_t)v0, n01);
+        const eid_t nd = diff_set(y0, nf0, y1, d1, v1, v1, y0n1);
+        for (eid_t i2 = 0; i2 < n; i2++) {
+          const int32_t v2 = y01[i2];
+          c5 += isect_num_bound(y01, n, ROW(v2), v2);
+        }
+        for (eid_t i2 = 0; i2 < nd; i2++) {
+          const int32_t v2 = y0n1[i2];
+          c3 += isect_num_bound(n01, nn, ROW(v2), (vid_t)v0);
+        }
+      }
+    }
+    free(y01);
+    free(n01);
+    free(y0n1);
+  }
+  c[4] = c4 / 2 - c5 * 6;
+  c[2] = c2 / 2 - c[4] * 2;
+  c[1] = c1 - c3 * 4;
+  c[0] = c0 / 6 - c[2] / 3;
+  out[0] = c[0];
+  out[1] = c[1];
+  out[2] = c[2];
+  out[3] = c3;
+  out[4] = c[4];
+  out[5] = c5;
+  return 0;
 }
 
 /* ----------------------------------------------------- algorithmic bytes */

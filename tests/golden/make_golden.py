@@ -3,7 +3,9 @@
 For each seeded synthetic graph below, the edge samples come from the engine's host
 generators (integer-only, identical on x86-64 and aarch64), the CSR from the oracle's
 CSR build, and every count from the reference's OWN OpenMP binaries (oracle/_ref,
-built from the reference sources by oracle/build_ref.sh) run on the graph files.  The
+built from the reference sources by oracle/build_ref.sh) run on the graph files:
+tc/clique/count omp_base for the six plans, motif_omp_formula for the k = 3 and k = 4
+vertex-induced motif census ("motif3", "motif4", in the reference's output order).  The
 oracle restatement is cross-checked on the way.  A sha256 of the CSR bytes lets the
 GPU tests confirm they regenerated the same graph.
 
@@ -74,6 +76,12 @@ def main() -> None:
             if ref != mine:
                 raise SystemExit(f"{case['name']} {k}: reference {ref} != oracle {mine}")
             counts[k] = ref
+        for k in (3, 4):  # vertex-induced motif census, motif_omp_formula
+            ref = oracle.run_ref_motif(k, prefix)
+            mine = oracle.motif(k, rowptr, col)
+            if ref != mine:
+                raise SystemExit(f"{case['name']} motif{k}: reference {ref} != oracle {mine}")
+            counts[f"motif{k}"] = ref
         rec = dict(case)
         rec.update({"V": int(nv), "E": int(len(col)), "E_dag": int(len(dcol)),
                     "csr_sha256": csr_digest(rowptr, col), "counts": counts,

@@ -91,3 +91,60 @@ def test_mlp_reference_gradient_is_consistent():
         yh = np.maximum(z, 0) @ q[M.H * M.F + M.H: M.H * M.F + 2 * M.H] + q[-1]
         lp = np.mean((yh - y) ** 2)
         assert abs((lp - loss) / eps - g[i]) < 1e-3 * max(1.0, abs(g[i]))
+
+
+def _spec(edges):
+    # the layout of a GLUMIN pattern description (codegen/codegen/patterns/*.yml)
+    return "pattern:\n  name: x\n  edges: [" + ", ".join(edges) + "]\n  orientation: []\n"
+
+
+def test_plan_names_and_ids(xgm):
+    # count-app names (edge-induced) and GLUMIN ids (vertex-induced); no GPU needed
+    for name, pat, ind in [("triangle", xgm.TRIANGLE, 0), ("4-diamond", xgm.DIAMOND, 0),
+                           ("rectangle", xgm.CYCLE4, 0), ("4-star", xgm.STAR3, 0),
+                           ("4-path", xgm.PATH4, 0), ("3-path", xgm.WEDGE, 0),
+                           ("P1", xgm.STAR3, 1), ("P2", xgm.DIAMOND, 1),
+                           ("P3", xgm.TAILED_TRIANGLE, 1), ("P4", xgm.CLIQUE4, 1),
+                           ("P5", xgm.CLIQUE5, 1)]:
+        p = xgm.plan(name)
+        assert (p.pattern, int(p.induced)) == (pat, ind), name
+    with pytest.raises(xgm.XgmError) as e:
+        xgm.plan("P6")
+    assert e.value.status == xgm.ERR_UNSUPPORTED
+
+
+def test_plan_from_spec(xgm):
+    cases = [(["AB", "BC", "AC"], xgm.TRIANGLE), (["AB", "AC", "AD"], xgm.STAR3),
+             (["AB", "BC", "CD"], xgm.PATH4), (["AB", "BC"], xgm.WEDGE),
+             (["AB", "BC", "CD", "AD"], xgm.CYCLE4), (["AB", "AC", "AD", "BC", "CD"], xgm.DIAMOND),
+             (["AB", "AC", "BC", "CD"], xgm.TAILED_TRIANGLE),
+             (["AB", "AC", "AD", "BC", "BD", "CD"], xgm.CLIQUE4)]
+    for edges, pat in cases:
+        p = xgm.plan_from_spec(_spec(edges))
+        assert p.pattern == pat and p.induced, edges
+        assert not xgm.plan_from_spec(_spec(edges), induced=False).induced
+    for bad, st in [(_spec(["AB", "A"]), xgm.ERR_INVALID), (_spec(["AA", "AB"]), xgm.ERR_INVALID),
+                    ("pattern:\n  name: x\n", xgm.ERR_INVALID), (_spec([]), xgm.ERR_INVALID),
+                    (_spec(["AB", "BC", "CD", "DE", "AE"]), xgm.ERR_UNSUPPORTED),  # 5-cycle
+                    (_spec(["AB", "CD"]), xgm.ERR_UNSUPPORTED)]:  # disconnected
+        with pytest.raises(xgm.XgmError) as e:
+            xgm.plan_from_spec(bad)
+        assert e.value.status == st, bad
+
+
+GLUMIN_PATTERNS = "/root/reference/codes/GLUMIN/codegen/codegen/patterns"
+
+
+@pytest.mark.skipif(not os.path.isdir(GLUMIN_PATTERNS), reason="reference tree absent")
+def test_reference_pattern_files(xgm):
+    want = {"3-triangle": xgm.TRIANGLE, "3-path": xgm.WEDGE, "4-clique": xgm.CLIQUE4,
+            "4-cycle": xgm.CYCLE4, "4-diamond": xgm.DIAMOND, "4-path": xgm.PATH4,
+            "4-star": xgm.STAR3, "4-tailed-triangle": xgm.TAILED_TRIANGLE,
+            "5-clique": xgm.CLIQUE5}
+    for f in sorted(os.listdir(GLUMIN_PATTERNS)):
+        name = f[:-4]
+        if name in want:
+            assert xgm.plan_from_spec(os.path.join(GLUMIN_PATTERNS, f)).pattern == want[name], f
+        else:  # 5-vertex motifs and the empty template are not plans of this engine
+            with pytest.raises(xgm.XgmError):
+                xgm.plan_from_spec(os.path.join(GLUMIN_PATTERNS, f))

@@ -27,6 +27,10 @@ def test_citeseer_known_answers(orc):
     assert c["diamond"] == 2200 + 6 * 255
     assert c["cycle4"] == 3094 + 2200 + 3 * 255
     assert c["tailed"] == 22900 + 4 * 2200 + 12 * 255
+    # the oracle's restatement of the formula motif counter, motif/README.md:52-60
+    # (wedges 23,380, triangles 1,166; 4-paths 111,153, 3-stars 222,630)
+    assert orc.motif(3, rowptr, col) == [23380, 1166]
+    assert orc.motif(4, rowptr, col) == [222630, 111153, 22900, 3094, 2200, 255]
 
 
 def test_golden_fixtures(xgm, orc, golden):
@@ -35,7 +39,10 @@ def test_golden_fixtures(xgm, orc, golden):
         rowptr, col = orc.build_csr(nv, src, dst)
         assert csr_digest(rowptr, col) == case["csr_sha256"], case["name"]
         c = oracle_counts(orc, rowptr, col)
-        assert c == case["counts"], case["name"]
+        assert c == {k: case["counts"][k] for k in c}, case["name"]
+        # vertex-induced census, fixtures from the reference's motif_omp_formula
+        assert orc.motif(3, rowptr, col) == case["counts"]["motif3"], case["name"]
+        assert orc.motif(4, rowptr, col) == case["counts"]["motif4"], case["name"]
 
 
 def _edge_list(path):
@@ -59,6 +66,9 @@ def test_reference_tiny_graphs(orc, name):
         if nv < 4 and k != "tc":
             continue
         assert orc.run_ref(k, prefix)[0] == v, k
+    if orc.ref_available("motif_omp_formula"):
+        for k in (3, 4):
+            assert orc.run_ref_motif(k, prefix) == orc.motif(k, rowptr, col), k
 
 
 def test_csr_build_cleans(orc):

@@ -35,9 +35,14 @@ BUILD_CLEAN = 7
 VIEW_UNDIRECTED, VIEW_DAG = 0, 1
 
 TRIANGLE, CLIQUE4, CLIQUE5, DIAMOND, CYCLE4, TAILED_TRIANGLE = 1, 2, 3, 4, 5, 6
+WEDGE, STAR3, PATH4 = 7, 8, 9
 PATTERN_NAMES = {"triangle": TRIANGLE, "4-clique": CLIQUE4, "5-clique": CLIQUE5,
                  "diamond": DIAMOND, "rectangle": CYCLE4, "4-cycle": CYCLE4,
-                 "tailedtriangle": TAILED_TRIANGLE}
+                 "tailedtriangle": TAILED_TRIANGLE, "wedge": WEDGE, "3-star": STAR3,
+                 "4-path": PATH4}
+# order of the motif census (MotifSolver output)
+MOTIF3_NAMES = ["wedge", "triangle"]
+MOTIF4_NAMES = ["3-star", "4-path", "tailed-triangle", "4-cycle", "diamond", "4-clique"]
 
 SCHED_HEURISTIC, SCHED_LEARNED, SCHED_FIXED, SCHED_TUNED = 0, 1, 2, 3
 SCHED_NO_GRAPH = 1
@@ -115,9 +120,13 @@ _SIGS = [
     ("xgm_graph_write_files", _I, [C.c_char_p, C.POINTER(CsrHost)]),
     ("xgm_plan_compile", _I, [_P, C.POINTER(PlanDesc), C.POINTER(_P)]),
     ("xgm_plan_from_name", _I, [_P, C.c_char_p, C.POINTER(_P)]),
+    ("xgm_plan_from_spec", _I, [_P, C.c_char_p, _I, C.POINTER(_P)]),
     ("xgm_plan_pattern", _I, [_P]),
+    ("xgm_plan_induced", _I, [_P]),
     ("xgm_plan_destroy", None, [_P]),
     ("xgm_count", _I, [_P, _P, _P, C.POINTER(Sched), C.POINTER(_U64), C.POINTER(Stats)]),
+    ("xgm_motif_count", _I, [_P, _P, _I, C.POINTER(Sched), C.POINTER(_U64), _I,
+                             C.POINTER(Stats)]),
     ("xgm_count_kernels", _I, [_P, _P, _P, C.POINTER(Sched), C.POINTER(_I)]),
     ("xgm_tc_solver", _I, [_P, _P, C.POINTER(_U64)]),
     ("xgm_tc_solver_static", _I, [_P, _P, C.POINTER(_U64)]),
@@ -237,24 +246,12 @@ class Context:
         return self._adopt(Graph(self, h))
 
     # plans / counting -----------------------------------------------------
-    def plan(self, pattern) -> "Plan":
-        h = C.c_void_p()
-        if isinstance(pattern, str):
-            _check(lib().xgm_plan_from_name(self._h, pattern.encode(), C.byref(h)), self)
-        elif isinstance(pattern, int):
-            d = PlanDesc()
-            d.builtin = pattern
-            _check(lib().xgm_plan_compile(self._h, C.byref(d), C.byref(h)), self)
-        else:  # adjacency matrix
-            adj = np.asarray(pattern, dtype=np.uint8)
-            d = PlanDesc()
-            d.builtin = 0
-            d.num_vertices = adj.shape[0]
-            for i in range(adj.shape[0]):
-                for j in range(adj.shape[1]):
-                    d.adj[i][j] = int(adj[i, j])
-            _check(lib().xgm_plan_compile(self._h, C.byref(d), C.byref(h)), self)
-        return Plan(h)
+    def plan(self, pattern, induced: bool = False) -> "Plan":
+        return plan(pattern, induced, self)
+
+    def plan_from_spec(self, spec: str, induced: bool = True) -> "Plan":
+        """Plan from a GLUMIN pattern .yml (text or path); GLUMIN counts vertex-induced."""
+        return plan_from_spec(spec, induced, self)
 
     @staticmethod
     def _sched(policy=SCHED_HEURISTIC, variant=0, model=None, warp_max=0, cta_max=0,
@@ -277,6 +274,18 @@ class Context:
         _check(lib().xgm_count(self._h, graph._h, plan._h, C.byref(sp), C.byref(out),
                                C.byref(st)), self)
         return (int(out.value), st.as_dict()) if with_stats else int(out.value)
+
+    def motif_count(self, graph: "Graph", k: int, policy: int = SCHED_HEURISTIC,
+                    variant: int = 0, model: Optional["Model"] = None,
+                    with_stats: bool = False):
+        """Vertex-induced k-motif census, k = 3 or 4 (MOTIF3_NAMES / MOTIF4_NAMES order)."""
+        sp = self._sched(policy, variant, model)
+        out = (C.c_uint64 * 6)()
+        st = Stats()
+        _check(lib().xgm_motif_count(self._h, graph._h, k, C.byref(sp), out, 6, C.byref(st)),
+               self)
+        res = [int(x) for x in out[: 2 if k == 3 else 6]]
+        return (res, st.as_dict()) if with_stats else res
 
     def count_kernels(self, graph: "Graph", pattern, policy: int = SCHED_HEURISTIC,
                       model: Optional["Model"] = None, order_by_cost: int = 1) -> int:
@@ -346,6 +355,41 @@ class Context:
         return int(out.value)
 
 
+def plan(pattern, induced: bool = False, ctx: Optional["Context"] = None) -> "Plan":
+    """Plan from a name, a builtin id or a pattern adjacency matrix (no GPU needed)."""
+    h = C.c_void_p()
+    ch = ctx._h if ctx is not None else None
+    if isinstance(pattern, str):
+        _check(lib().xgm_plan_from_name(ch, pattern.encode(), C.byref(h)), ctx)
+        if induced:  # names carry no induced flag: rebuild through the descriptor
+            p = lib().xgm_plan_pattern(h)
+            lib().xgm_plan_destroy(h)
+            return plan(p, induced, ctx)
+        return Plan(h)
+    d = PlanDesc()
+    d.induced = 1 if induced else 0
+    if isinstance(pattern, int):
+        d.builtin = pattern
+    else:
+        adj = np.asarray(pattern, dtype=np.uint8)
+        d.builtin = 0
+        d.num_vertices = adj.shape[0]
+        for i in range(adj.shape[0]):
+            for j in range(adj.shape[1]):
+                d.adj[i][j] = int(adj[i, j])
+    _check(lib().xgm_plan_compile(ch, C.byref(d), C.byref(h)), ctx)
+    return Plan(h)
+
+
+def plan_from_spec(spec: str, induced: bool = True, ctx: Optional["Context"] = None) -> "Plan":
+    if os.path.exists(spec):
+        spec = open(spec).read()
+    h = C.c_void_p()
+    _check(lib().xgm_plan_from_spec(ctx._h if ctx is not None else None, spec.encode(),
+                                    1 if induced else 0, C.byref(h)), ctx)
+    return Plan(h)
+
+
 class Plan:
     def __init__(self, h):
         self._h = h
@@ -353,6 +397,10 @@ class Plan:
     @property
     def pattern(self) -> int:
         return lib().xgm_plan_pattern(self._h)
+
+    @property
+    def induced(self) -> bool:
+        return bool(lib().xgm_plan_induced(self._h))
 
     def __del__(self):
         try:
@@ -507,6 +555,12 @@ def CliqueSolver(g: Graph, k: int) -> int:
     out = C.c_uint64()
     _check(lib().xgm_clique_solver(g.ctx._h, g._h, k, C.byref(out)), g.ctx)
     return int(out.value)
+
+
+def MotifSolver(g: Graph, k: int) -> list:
+    """Vertex-induced k-motif census in the reference's output order (MOTIF3_NAMES /
+    MOTIF4_NAMES)."""
+    return g.ctx.motif_count(g, k)
 
 
 def ScSolver(g: Graph, pattern: str) -> int:

@@ -1,6 +1,7 @@
 // C ABI of the engine (include/xgm.h): contexts, graphs, plans and the counting calls.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -340,21 +341,61 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* d, xgm_plan** out
     pat = match_pattern(d);
     if (pat <= 0) {
       set_thread_error(pat == 0 ? "pattern not supported (supported: triangle, 4/5-clique, "
-                                  "edge-induced diamond, 4-cycle, tailed triangle)"
+                                  "diamond, 4-cycle, tailed triangle, wedge, 3-star, 4-path)"
                                 : "pattern adjacency is malformed");
       return finish_status(ctx, pat == 0 ? XGM_ERR_UNSUPPORTED : XGM_ERR_INVALID);
     }
   }
-  if (pat < XGM_PATTERN_TRIANGLE || pat > XGM_PATTERN_TAILED_TRIANGLE) return XGM_ERR_INVALID;
+  if (pat < XGM_PATTERN_TRIANGLE || pat > XGM_PATTERN_PATH4) return XGM_ERR_INVALID;
   xgm_plan* p = new xgm_plan();
   p->pattern = pat;
+  p->induced = d->induced ? 1 : 0;
   *out = p;
   return XGM_OK;
 }
 
+xgm_status xgm_plan_from_spec(xgm_ctx* ctx, const char* spec, int induced, xgm_plan** out) {
+  if (!spec || !out) return XGM_ERR_INVALID;
+  *out = nullptr;
+  // the `edges:` list: [AB, AC, ...]; vertices are letters A..H
+  const char* e = std::strstr(spec, "edges:");
+  const char* lb = e ? std::strchr(e, '[') : nullptr;
+  const char* rb = lb ? std::strchr(lb, ']') : nullptr;
+  if (!rb) {
+    set_thread_error("pattern description has no `edges: [...]` list");
+    return finish_status(ctx, XGM_ERR_INVALID);
+  }
+  xgm_plan_desc d;
+  std::memset(&d, 0, sizeof(d));
+  int nv = 0;
+  for (const char* c = lb + 1; c < rb;) {
+    while (c < rb && (*c == ' ' || *c == ',' || *c == '\n' || *c == '\t')) ++c;
+    if (c >= rb) break;
+    if (c + 1 >= rb || *c < 'A' || *c > 'H' || c[1] < 'A' || c[1] > 'H') {
+      set_thread_error("pattern edges must be pairs of letters A..H");
+      return finish_status(ctx, XGM_ERR_INVALID);
+    }
+    const int a = *c - 'A', b = c[1] - 'A';
+    if (a == b) {
+      set_thread_error("pattern edge joins a vertex to itself");
+      return finish_status(ctx, XGM_ERR_INVALID);
+    }
+    d.adj[a][b] = d.adj[b][a] = 1;
+    nv = std::max(nv, std::max(a, b) + 1);
+    c += 2;
+  }
+  d.num_vertices = nv;
+  d.induced = induced;
+  return xgm_plan_compile(ctx, &d, out);
+}
+
+int xgm_plan_induced(const xgm_plan* p) { return p ? p->induced : 0; }
+
 xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out) {
   if (!name || !out) return XGM_ERR_INVALID;
-  const int pat = pattern_from_name(name);
+  int induced = 0;
+  uint64_t scale = 1;
+  const int pat = pattern_from_name(name, &induced, &scale);
   if (pat <= 0) {
     set_thread_error(std::string("unknown pattern name '") + name + "'");
     return finish_status(ctx, XGM_ERR_UNSUPPORTED);
@@ -362,7 +403,10 @@ xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out) {
   xgm_plan_desc d;
   std::memset(&d, 0, sizeof(d));
   d.builtin = pat;
-  return xgm_plan_compile(ctx, &d, out);
+  d.induced = induced;
+  xgm_status st = xgm_plan_compile(ctx, &d, out);
+  if (st == XGM_OK) (*out)->scale = scale;
+  return st;
 }
 
 int xgm_plan_pattern(const xgm_plan* p) { return p ? p->pattern : 0; }
@@ -378,8 +422,24 @@ xgm_status xgm_count(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan, con
   xgm_stats st_local;
   xgm_stats& st = stats ? *stats : st_local;
   std::memset(&st, 0, sizeof(st));
-  xgm_status r = count_dispatch(ctx, g->g, plan->pattern, sp, out_count, st);
+  xgm_status r = count_plan(ctx, g->g, plan->pattern, plan->induced, sp, out_count, st);
+  if (r == XGM_OK) *out_count *= plan->scale;
   return finish_status(ctx, r);
+}
+
+xgm_status xgm_motif_count(xgm_ctx* ctx, const xgm_graph* g, int k, const xgm_sched* sched,
+                           uint64_t* counts, int n_counts, xgm_stats* stats) {
+  if (!ctx || !g || !counts) return XGM_ERR_INVALID;
+  if ((k == 3 && n_counts < 2) || (k == 4 && n_counts < 6)) {
+    set_thread_error("counts[] too short: k = 3 gives 2 counts, k = 4 gives 6");
+    return finish_status(ctx, XGM_ERR_INVALID);
+  }
+  xgm_sched def;
+  std::memset(&def, 0, sizeof(def));
+  xgm_stats st_local;
+  xgm_stats& st = stats ? *stats : st_local;
+  std::memset(&st, 0, sizeof(st));
+  return finish_status(ctx, count_motifs(ctx, g->g, k, sched ? *sched : def, counts, st));
 }
 
 xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,

@@ -17,6 +17,7 @@ struct Scalars {
   QueueHeads q;
   unsigned long long c4heads[2];
   int64_t n[8];  // task list sizes, copied back for the stats
+  unsigned long long terms[6];  // motif-identity sums (launch_motif_terms)
 };
 
 struct Model;  // learned cost model (learned.cu)
@@ -57,6 +58,8 @@ struct xgm_graph {
 
 struct xgm_plan {
   int pattern = 0;
+  int induced = 0;     // vertex-induced motif counts (via the motif identities)
+  uint64_t scale = 1;  // embeddings per match in the caller's convention (GLUMIN P2: 2)
 };
 
 namespace xgm {
@@ -69,6 +72,11 @@ xgm_status ctx_sync_scalars(xgm_ctx* ctx);
 xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
                           uint64_t* out, xgm_stats& st);
 xgm_status algo_bytes_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, uint64_t* out);
+// One plan (pattern, edge- or vertex-induced), and the k = 3 / k = 4 motif census.
+xgm_status count_plan(xgm_ctx* ctx, const DevGraph& g, int pattern, int induced,
+                      const xgm_sched& sp, uint64_t* out, xgm_stats& st);
+xgm_status count_motifs(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp,
+                        uint64_t* out, xgm_stats& st);
 xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
                          int* n_kernels);
 void motif_buffers_free(xgm_ctx* ctx);
@@ -76,6 +84,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
                          cudaStream_t s);
 int ensure_clique_grid(xgm_ctx* ctx);
 int match_pattern(const xgm_plan_desc* d);  // builtin id, 0 unsupported, -1 malformed
-int pattern_from_name(const char* name);
+// Builtin id for a pattern name (0 if unknown); GLUMIN ids also set induced / scale.
+int pattern_from_name(const char* name, int* induced = nullptr, uint64_t* scale = nullptr);
 
 }  // namespace xgm

@@ -146,6 +146,10 @@ struct Slots {
 xgm_status slots_of(const xgm_plan* const* plans, int n, Slots& sl) {
   for (int p = 0; p < n; ++p) {
     if (!plans[p]) return XGM_ERR_INVALID;
+    if (plans[p]->induced || plans[p]->scale != 1) {
+      set_thread_error("vertex-induced plans are counted one graph at a time (xgm_count)");
+      return XGM_ERR_UNSUPPORTED;
+    }
     int* t = nullptr;
     switch (plans[p]->pattern) {
       case XGM_PATTERN_TRIANGLE: t = &sl.tri; break;
@@ -154,7 +158,10 @@ xgm_status slots_of(const xgm_plan* const* plans, int n, Slots& sl) {
       case XGM_PATTERN_DIAMOND: t = &sl.dia; break;
       case XGM_PATTERN_TAILED_TRIANGLE: t = &sl.tail; break;
       case XGM_PATTERN_CYCLE4: t = &sl.c4; break;
-      default: return XGM_ERR_INVALID;
+      default:
+        set_thread_error("batched counting covers the clique, diamond, 4-cycle and tailed "
+                         "triangle plans");
+        return XGM_ERR_UNSUPPORTED;
     }
     if (*t >= 0) {
       set_thread_error("a plan appears twice in the batched call");

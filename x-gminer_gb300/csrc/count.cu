@@ -298,6 +298,211 @@ xgm_status algo_bytes_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, uin
   return check_device_flag(ctx, ctx->h_sc->err);
 }
 
+namespace {
+
+// The sums of launch_motif_terms, after one triangle-participation pass when `part`.
+xgm_status motif_terms(xgm_ctx* ctx, const DevGraph& g, const xgm_sched& sp, bool part,
+                       uint64_t terms[6], xgm_stats& st) {
+  cudaStream_t s = ctx->stream;
+  XGM_CUDA_TRY(cudaSetDevice(ctx->device));
+  XGM_CUDA_TRY(taskbuf_reserve(ctx->tb, g.nv, s));
+  XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  const GView view = g.view();
+  if (part) {
+    xgm_sched tri = sp;
+    if (tri.policy == XGM_SCHED_LEARNED && !tri.model) tri.policy = XGM_SCHED_HEURISTIC;
+    xgm_status r = schedule_tasks(ctx, g, 3, tri);
+    if (r != XGM_OK) return r;
+    XGM_CUDA_TRY(grow(&ctx->vpart, &ctx->vpart_cap, g.nv, s));
+    XGM_CUDA_TRY(grow(&ctx->epart, &ctx->epart_cap, g.ne, s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->vpart, 0, sizeof(unsigned long long) * (g.nv > 0 ? g.nv : 1), s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->epart, 0, sizeof(unsigned) * (g.ne > 0 ? g.ne : 1), s));
+    XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+    XGM_CUDA_TRY(launch_triangle_participation(view, ctx->tb.lists(false), &ctx->d_sc->q,
+                                               ctx->vpart, ctx->epart, &ctx->d_sc->err,
+                                               ensure_clique_grid(ctx), s));
+  } else {
+    XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  }
+  XGM_CUDA_TRY(launch_motif_terms(view, part ? ctx->vpart : nullptr, part ? ctx->epart : nullptr,
+                                  ctx->d_sc->terms, s));
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+  if (part)
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 6,
+                                 cudaMemcpyDeviceToDevice, s));
+  xgm_status r = ctx_sync_scalars(ctx);
+  if (r != XGM_OK) return r;
+  float prep = 0, kern = 0;
+  cudaEventElapsedTime(&prep, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&kern, ctx->ev[1], ctx->ev[2]);
+  std::memset(&st, 0, sizeof(st));
+  st.prep_ms = prep;
+  st.kernel_ms = kern;
+  st.device_error = ctx->h_sc->err;
+  st.launches = part ? 2 : 1;
+  if (part) {
+    st.variant_tasks[XGM_VAR_WARP] = ctx->h_sc->n[2];
+    st.variant_tasks[XGM_VAR_CTA] = ctx->h_sc->n[1];
+    st.variant_tasks[XGM_VAR_SPLIT] = ctx->h_sc->n[0];
+    st.variant_tasks[XGM_VAR_WIDE] = ctx->h_sc->n[4];
+    st.variant_tasks[XGM_VAR_SEARCH] = ctx->h_sc->n[5];
+    st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4] +
+               ctx->h_sc->n[5];
+  }
+  r = check_device_flag(ctx, ctx->h_sc->err);
+  if (r != XGM_OK) return r;
+  for (int i = 0; i < 6; ++i) terms[i] = ctx->h_sc->terms[i];
+  return XGM_OK;
+}
+
+void add_stats(xgm_stats& acc, const xgm_stats& x) {
+  acc.kernel_ms += x.kernel_ms;
+  acc.prep_ms += x.prep_ms;
+  acc.tasks += x.tasks;
+  for (int i = 0; i < XGM_NUM_VARIANTS; ++i) acc.variant_tasks[i] += x.variant_tasks[i];
+  acc.algo_bytes += x.algo_bytes;
+  acc.device_error |= x.device_error;
+  acc.launches += x.launches;
+}
+
+// The pieces of the 4-vertex identities (all wrapping uint64).
+struct Motif4Parts {
+  uint64_t k4 = 0, c4e = 0;
+  uint64_t t[6] = {0, 0, 0, 0, 0, 0};  // motif_terms with participation
+};
+
+xgm_status motif4_parts(xgm_ctx* ctx, const DevGraph& g, const xgm_sched& sp, bool need_c4,
+                        Motif4Parts& m, xgm_stats& st) {
+  xgm_stats x;
+  xgm_status r = motif_terms(ctx, g, sp, true, m.t, x);
+  if (r != XGM_OK) return r;
+  add_stats(st, x);
+  std::memset(&x, 0, sizeof(x));
+  r = count_dispatch(ctx, g, XGM_PATTERN_CLIQUE4, sp, &m.k4, x);
+  if (r != XGM_OK) return r;
+  add_stats(st, x);
+  if (need_c4) {
+    std::memset(&x, 0, sizeof(x));
+    r = count_dispatch(ctx, g, XGM_PATTERN_CYCLE4, sp, &m.c4e, x);
+    if (r != XGM_OK) return r;
+    add_stats(st, x);
+  }
+  return XGM_OK;
+}
+
+// Vertex-induced 4-vertex motifs from the edge-induced counts.  Every edge-induced
+// embedding sits in exactly one induced connected 4-vertex subgraph; per 4-set:
+//                3-star 4-path tailed 4-cycle diamond K4
+//   3-stars        1      0      1      0       2     4      (sum_v C(d_v, 3))
+//   4-paths        0      1      2      4       6    12      (3-walks - 3 x triangles)
+//   tailed         .      .      1      0       4    12
+//   4-cycles       .      .      0      1       1     3
+//   diamonds       .      .      0      0       1     6
+// The triangular system is solved from the bottom up.  The reference's formula motif
+// counter (codes/GraphMiner/src/motif/omp_formula.cc:38-48 with
+// cpu_kernels/automine_formula.h:20-57) derives the same six numbers from
+// per-edge local counts plus enumerated 4-cycles and 4-cliques; its output order is
+// [3-star, 4-path, tailed triangle, 4-cycle, diamond, 4-clique].
+void motif4_solve(const Motif4Parts& m, uint64_t out[6]) {
+  const uint64_t k4 = m.k4, dia_e = m.t[4], tail_e = m.t[3];
+  const uint64_t star_e = m.t[1], path_e = m.t[2] - m.t[5];
+  const uint64_t dia = dia_e - 6 * k4;
+  const uint64_t c4 = m.c4e + 3 * k4 - dia_e;
+  const uint64_t tail = tail_e - 4 * dia - 12 * k4;
+  out[0] = star_e - tail - 2 * dia - 4 * k4;
+  out[1] = path_e - 2 * tail - 4 * c4 - 6 * dia - 12 * k4;
+  out[2] = tail;
+  out[3] = c4;
+  out[4] = dia;
+  out[5] = k4;
+}
+
+}  // namespace
+
+// Reference interface: MotifSolver(Graph&, int k, std::vector<uint64_t>& total, ...)
+// (codes/GraphMiner/src/motif/omp_formula.cc:8, main.cc:8-31): k = 3 gives
+// [wedges, triangles], k = 4 the six counts of motif4_solve, all vertex-induced.
+xgm_status count_motifs(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp,
+                        uint64_t* out, xgm_stats& st) {
+  std::memset(&st, 0, sizeof(st));
+  if (k == 3) {
+    uint64_t t[6], tri = 0;
+    xgm_stats x;
+    xgm_status r = motif_terms(ctx, g, sp, false, t, x);
+    if (r != XGM_OK) return r;
+    add_stats(st, x);
+    std::memset(&x, 0, sizeof(x));
+    r = count_dispatch(ctx, g, XGM_PATTERN_TRIANGLE, sp, &tri, x);
+    if (r != XGM_OK) return r;
+    add_stats(st, x);
+    out[0] = t[0] - 3 * tri;
+    out[1] = tri;
+    return XGM_OK;
+  }
+  if (k != 4) {
+    set_thread_error("motif counting covers k = 3 and k = 4");
+    return XGM_ERR_UNSUPPORTED;
+  }
+  Motif4Parts m;
+  xgm_status r = motif4_parts(ctx, g, sp, true, m, st);
+  if (r != XGM_OK) return r;
+  motif4_solve(m, out);
+  return XGM_OK;
+}
+
+// One plan: the clique and edge-induced motif kernels directly; wedges, 3-stars,
+// 4-paths and every vertex-induced motif through the motif sums and identities.
+xgm_status count_plan(xgm_ctx* ctx, const DevGraph& g, int pattern, int induced,
+                      const xgm_sched& sp, uint64_t* out, xgm_stats& st) {
+  const bool clique = pattern == XGM_PATTERN_TRIANGLE || pattern == XGM_PATTERN_CLIQUE4 ||
+                      pattern == XGM_PATTERN_CLIQUE5;
+  const bool kernel = pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_CYCLE4 ||
+                      pattern == XGM_PATTERN_TAILED_TRIANGLE;
+  if (clique || (kernel && !induced)) return count_dispatch(ctx, g, pattern, sp, out, st);
+  std::memset(&st, 0, sizeof(st));
+  if (pattern == XGM_PATTERN_WEDGE) {
+    if (induced) {
+      uint64_t m3[2];
+      xgm_status r = count_motifs(ctx, g, 3, sp, m3, st);
+      if (r == XGM_OK) *out = m3[0];
+      return r;
+    }
+    uint64_t t[6];
+    xgm_status r = motif_terms(ctx, g, sp, false, t, st);
+    if (r == XGM_OK) *out = t[0];
+    return r;
+  }
+  if (pattern == XGM_PATTERN_STAR3 && !induced) {
+    uint64_t t[6];
+    xgm_status r = motif_terms(ctx, g, sp, false, t, st);
+    if (r == XGM_OK) *out = t[1];
+    return r;
+  }
+  if (pattern == XGM_PATTERN_PATH4 && !induced) {
+    uint64_t t[6];
+    xgm_status r = motif_terms(ctx, g, sp, true, t, st);
+    if (r == XGM_OK) *out = t[2] - t[5];
+    return r;
+  }
+  // vertex-induced 4-vertex motifs; the 4-cycle kernel only where the identity needs it
+  const bool need_c4 = pattern == XGM_PATTERN_CYCLE4 || pattern == XGM_PATTERN_PATH4;
+  Motif4Parts m;
+  xgm_status r = motif4_parts(ctx, g, sp, need_c4, m, st);
+  if (r != XGM_OK) return r;
+  uint64_t v[6];
+  motif4_solve(m, v);
+  switch (pattern) {
+    case XGM_PATTERN_STAR3: *out = v[0]; break;
+    case XGM_PATTERN_PATH4: *out = v[1]; break;
+    case XGM_PATTERN_TAILED_TRIANGLE: *out = v[2]; break;
+    case XGM_PATTERN_CYCLE4: *out = v[3]; break;
+    case XGM_PATTERN_DIAMOND: *out = v[4]; break;
+    default: set_thread_error("unknown pattern"); return XGM_ERR_INVALID;
+  }
+  return XGM_OK;
+}
+
 // Pattern matching of a small adjacency matrix against the builtins (edge-induced).
 int match_pattern(const xgm_plan_desc* d) {
   const int n = d->num_vertices;
@@ -321,19 +526,46 @@ int match_pattern(const xgm_plan_desc* d) {
   if (n == 4 && m == 4 && sorted[0] == 2 && sorted[3] == 2) return XGM_PATTERN_CYCLE4;
   if (n == 4 && m == 4 && sorted[0] == 1 && sorted[1] == 2 && sorted[2] == 2 && sorted[3] == 3)
     return XGM_PATTERN_TAILED_TRIANGLE;
+  if (n == 3 && m == 2 && sorted[0] == 1) return XGM_PATTERN_WEDGE;
+  if (n == 4 && m == 3 && sorted[0] == 1 && sorted[2] == 1 && sorted[3] == 3) return XGM_PATTERN_STAR3;
+  if (n == 4 && m == 3 && sorted[0] == 1 && sorted[1] == 1 && sorted[2] == 2 && sorted[3] == 2)
+    return XGM_PATTERN_PATH4;
   return 0;
 }
 
-int pattern_from_name(const char* name) {
+int pattern_from_name(const char* name, int* induced, uint64_t* scale) {
   const std::string s(name);
-  if (s == "triangle" || s == "3-clique" || s == "clique3" || s == "tc") return XGM_PATTERN_TRIANGLE;
+  if (induced) *induced = 0;
+  if (scale) *scale = 1;
+  if (s == "triangle" || s == "3-clique" || s == "clique3" || s == "tc" || s == "3-triangle")
+    return XGM_PATTERN_TRIANGLE;
   if (s == "4-clique" || s == "clique4" || s == "k4") return XGM_PATTERN_CLIQUE4;
   if (s == "5-clique" || s == "clique5" || s == "k5") return XGM_PATTERN_CLIQUE5;
-  if (s == "diamond") return XGM_PATTERN_DIAMOND;
+  if (s == "diamond" || s == "4-diamond") return XGM_PATTERN_DIAMOND;
   if (s == "rectangle" || s == "4-cycle" || s == "cycle4") return XGM_PATTERN_CYCLE4;
-  if (s == "tailedtriangle" || s == "tailed-triangle" || s == "tailed_triangle")
+  if (s == "tailedtriangle" || s == "tailed-triangle" || s == "tailed_triangle" ||
+      s == "4-tailed-triangle")
     return XGM_PATTERN_TAILED_TRIANGLE;
-  return 0;
+  if (s == "wedge" || s == "3-path") return XGM_PATTERN_WEDGE;
+  if (s == "4-star" || s == "3-star") return XGM_PATTERN_STAR3;
+  if (s == "4-path") return XGM_PATTERN_PATH4;
+  // GLUMIN pattern ids (G2Miner/main.cc:13-60): vertex-induced.  P1 counts each star
+  // once (GM_kernels/P1-GM.yml.cuh: leaves ordered v3 < v2 < v1); P2 walks every
+  // directed edge as the diamond's shared edge (init_edgelist without symmetry
+  // breaking, gpu_GM_LUT.cu:89 / common/graph.cc:296-330; P2-GM.yml.cuh), so each diamond
+  // counts twice; P3 counts each tailed triangle once (v2 < v1 around the anchor v0).
+  int p = 0;
+  uint64_t k = 1;
+  if (s == "P1") p = XGM_PATTERN_STAR3;
+  else if (s == "P2") p = XGM_PATTERN_DIAMOND, k = 2;
+  else if (s == "P3") p = XGM_PATTERN_TAILED_TRIANGLE;
+  else if (s == "P4") p = XGM_PATTERN_CLIQUE4;
+  else if (s == "P5") p = XGM_PATTERN_CLIQUE5;
+  if (p) {
+    if (induced) *induced = 1;
+    if (scale) *scale = k;
+  }
+  return p;
 }
 
 }  // namespace xgm

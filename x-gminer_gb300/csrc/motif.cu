@@ -45,6 +45,59 @@ __global__ void k_tailed_reduce(const unsigned long long* vpart, const int64_t* 
   if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
+// C(d, 3) in wrapping uint64 arithmetic without an intermediate overflow for d < 2^32:
+// 3 divides one of d, d-1, d-2; when it does not divide x = d(d-1)/2 it divides d-2.
+__device__ __forceinline__ unsigned long long choose3(unsigned long long d) {
+  if (d < 3) return 0;
+  const unsigned long long x = d * (d - 1) / 2;
+  return x % 3 == 0 ? (x / 3) * (d - 2) : x * ((d - 2) / 3);
+}
+
+// The sums behind the motif identities, one warp per vertex (lane 0: vertex terms;
+// lanes stride the out-neighbours for the edge terms), wrapping uint64:
+//   out[0] = sum_v C(d_v, 2)                 edge-induced wedges
+//   out[1] = sum_v C(d_v, 3)                 edge-induced 3-stars
+//   out[2] = sum_{uv in E} (d_u-1)(d_v-1)    3-edge walks x-u-v-y, x != v, y != u
+//   out[3] = sum_v t_v (d_v - 2)             edge-induced tailed triangles
+//   out[4] = sum_{uv in E} C(t_uv, 2)        edge-induced diamonds
+//   out[5] = sum_v t_v                       3 x triangles
+// t_v / t_uv are the triangle-participation counters (vpart / epart, null for the
+// 3-vertex census: out[3..5] stay 0).
+__global__ void __launch_bounds__(kThreads) k_motif_terms(GView g, const unsigned long long* vpart,
+                                                          const unsigned* epart,
+                                                          unsigned long long* out) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
+  const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < g.nv; r += nwarps) {
+    const unsigned long long d = (unsigned long long)(g.rowptr[r + 1] - g.rowptr[r]);
+    if (lane == 0) {
+      acc[0] += d * (d - (d > 0)) / 2;
+      acc[1] += choose3(d);
+      if (vpart) {
+        const unsigned long long t = vpart[r];
+        if (d > 2) acc[3] += t * (d - 2);
+        acc[5] += t;
+      }
+    }
+    const longlong2 p = g.dptr[r];
+    for (long long j = p.x + lane; j < p.y; j += 32) {
+      const int32_t v = ldg_i32(g.col + j);
+      const unsigned long long dv = (unsigned long long)(g.rowptr[v + 1] - g.rowptr[v]);
+      acc[2] += (d - 1) * (dv - 1);
+      if (epart) {
+        const unsigned long long n = epart[j];
+        acc[4] += n * (n - (n > 0)) / 2;
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const unsigned long long w = warp_sum_u64(acc[i]);
+    if (lane == 0 && w) atomicAdd(out + i, w);
+  }
+}
+
 // Entries of row v1 below v0: col[rowptr[v1] .. first index with col >= v0).
 __device__ __forceinline__ long long lower_end(const GView& g, int32_t v1, int32_t v0) {
   long long lo = g.rowptr[v1], hi = g.dptr[v1].y;
@@ -317,6 +370,13 @@ cudaError_t launch_diamond_reduce(const unsigned* epart, int64_t ne, unsigned lo
 cudaError_t launch_tailed_reduce(const unsigned long long* vpart, const int64_t* rowptr, int64_t nv,
                                  unsigned long long* out, cudaStream_t s) {
   k_tailed_reduce<<<grid_for(nv), kThreads, 0, s>>>(vpart, rowptr, nv, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_motif_terms(const GView& g, const unsigned long long* vpart,
+                               const unsigned* epart, unsigned long long* out, cudaStream_t s) {
+  if (g.nv == 0) return cudaSuccess;
+  k_motif_terms<<<grid_for(g.nv * 32), kThreads, 0, s>>>(g, vpart, epart, out);
   return cudaGetLastError();
 }
 

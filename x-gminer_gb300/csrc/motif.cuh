@@ -12,6 +12,11 @@ cudaError_t launch_diamond_reduce(const unsigned* epart, int64_t ne, unsigned lo
 cudaError_t launch_tailed_reduce(const unsigned long long* vpart, const int64_t* rowptr, int64_t nv,
                                  unsigned long long* out, cudaStream_t s);
 
+// out[0..5] += wedge / 3-star / 3-walk / tailed-triangle / diamond / 3 x triangle sums
+// (edge-induced; vpart/epart null for the 3-vertex census).
+cudaError_t launch_motif_terms(const GView& g, const unsigned long long* vpart,
+                               const unsigned* epart, unsigned long long* out, cudaStream_t s);
+
 // 4-cycle: wedge counts per vertex, then the persistent grouping kernel.
 int cycle4_grid(int num_sms);
 int cycle4_hash_half();
