@@ -134,7 +134,9 @@ typedef enum {
   XGM_PATTERN_TAILED_TRIANGLE = 6,  /* tailedtriangle.h; GLUMIN 4-tailed-triangle.yml */
   XGM_PATTERN_WEDGE = 7,            /* 2-edge path; GLUMIN 3-path.yml, motif k = 3 */
   XGM_PATTERN_STAR3 = 8,            /* K_{1,3}; GLUMIN 4-star.yml (P1) */
-  XGM_PATTERN_PATH4 = 9             /* 3-edge path; GLUMIN 4-path.yml */
+  XGM_PATTERN_PATH4 = 9,            /* 3-edge path; GLUMIN 4-path.yml */
+  XGM_PATTERN_CLIQUE6 = 10,         /* GLUMIN P23 (clique6_warp_edge*.cuh) */
+  XGM_PATTERN_CLIQUE7 = 11          /* GLUMIN P24 (clique7_warp_edge*.cuh) */
 } xgm_pattern;
 
 typedef struct {
@@ -154,7 +156,8 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* desc, xgm_plan** 
  * "4-tailed-triangle", "3-path", "4-path", "4-star"), all edge-induced; and GLUMIN's
  * pattern ids (codes/GLUMIN/src/G2Miner/main.cc:13-60), vertex-induced: "P1" (4-star),
  * "P2" (4-diamond, reported as GLUMIN does: each diamond once per direction of its
- * shared edge, i.e. twice), "P3" (4-tailed-triangle), "P4"/"P5" (4/5-clique). */
+ * shared edge, i.e. twice), "P3" (4-tailed-triangle), "P4"/"P5"/"P23"/"P24"
+ * (4/5/6/7-clique). */
 xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out);
 /* Plan from a GLUMIN pattern description, the text of one of
  * codes/GLUMIN/codegen/codegen/patterns/*.yml: its `edges: [AB, AC, ...]` list (vertices

@@ -76,6 +76,8 @@ def lib():
             f = getattr(L, name)
             f.restype = U64
             f.argtypes = [I64, P, P, I64, I64, I64, I64]
+        L.orc_clique_k.restype = U64
+        L.orc_clique_k.argtypes = [C.c_int, I64, P, P, I64, I64, I64, I64]
         L.orc_motif.restype = C.c_int
         L.orc_motif.argtypes = [C.c_int, I64, P, P, I64, P]
         L.orc_algo_bytes.restype = U64
@@ -127,10 +129,14 @@ def _args(rowptr, col):
 
 def count(kind: str, rowptr: np.ndarray, col: np.ndarray, lo: int = 0, hi: int = -1,
           stride: int = 1) -> int:
-    """kind: tc / clique4 / clique5 (on a DAG) or diamond / cycle4 / tailed (undirected)."""
+    """kind: tc / clique4 .. clique7 (on a DAG) or diamond / cycle4 / tailed (undirected)."""
     nv, rowptr, col = _args(rowptr, col)
     hi = nv if hi < 0 else hi
     L = lib()
+    if kind in ("clique6", "clique7"):
+        md = int(np.max(np.diff(rowptr))) if nv else 0
+        return int(L.orc_clique_k(int(kind[-1]), nv, rowptr.ctypes.data, col.ctypes.data, md,
+                                  lo, hi, stride))
     if kind in ("clique4", "clique5"):
         md = int(np.max(np.diff(rowptr))) if nv else 0
         f = L.orc_clique4 if kind == "clique4" else L.orc_clique5

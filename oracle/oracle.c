@@ -255,6 +255,41 @@ uint64_t orc_clique5(int64_t nv, const int64_t* rowptr, const int32_t* col, int6
   return counter;
 }
 
+/* k-clique listing on the DAG for any k >= 3: the candidate-set recursion of
+ * automine_4clique / automine_5clique (clique_base.h:53-68, automine_omp.h:138-157)
+ * carried to depth k - 1, as GLUMIN's 6- and 7-clique kernels do on the GPU
+ * (codes/GLUMIN/src/G2Miner/gpu_GM_LUT_kernels/GM_kernels/clique6_warp_edge.cuh,
+ * clique7_warp_edge.cuh): candidates of the next level = candidates & N+(u).  `need`
+ * more members are to be picked from cand[0..n); buf holds one level per member. */
+static uint64_t kclique_rec(const int64_t* rowptr, const int32_t* col, const vid_t* cand,
+                            eid_t n, int need, vid_t* buf, size_t level) {
+  if (need == 1) return (uint64_t)n;
+  uint64_t total = 0;
+  for (eid_t i = 0; i < n; i++) {
+    const eid_t m = isect_set(cand, n, ROW(cand[i]), buf);
+    if (m >= need - 1) total += kclique_rec(rowptr, col, buf, m, need - 1, buf + level, level);
+  }
+  return total;
+}
+
+uint64_t orc_clique_k(int k, int64_t nv, const int64_t* rowptr, const int32_t* col,
+                      int64_t max_deg, int64_t lo, int64_t hi, int64_t stride) {
+  (void)nv;
+  uint64_t counter = 0;
+  if (k < 3) return 0;
+  const size_t level = (size_t)(max_deg + 1);
+#pragma omp parallel reduction(+ : counter)
+  {
+    vid_t* buf = (vid_t*)malloc(sizeof(vid_t) * level * (size_t)k);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t v0 = lo; v0 < hi; v0 += stride)
+      counter += kclique_rec(rowptr, col, col + rowptr[v0], rowptr[v0 + 1] - rowptr[v0], k - 1,
+                             buf, level);
+    free(buf);
+  }
+  return counter;
+}
+
 /* Edge-induced diamond, codes/GraphMiner/src/count/cpu_kernels/diamond.h:1-8
  * (undirected graph): sum over edges v1 < v0 of C(|N(v0) & N(v1)|, 2). */
 uint64_t orc_diamond(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t lo,

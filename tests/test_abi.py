@@ -105,7 +105,8 @@ def test_plan_names_and_ids(xgm):
                            ("4-path", xgm.PATH4, 0), ("3-path", xgm.WEDGE, 0),
                            ("P1", xgm.STAR3, 1), ("P2", xgm.DIAMOND, 1),
                            ("P3", xgm.TAILED_TRIANGLE, 1), ("P4", xgm.CLIQUE4, 1),
-                           ("P5", xgm.CLIQUE5, 1)]:
+                           ("P5", xgm.CLIQUE5, 1), ("6-clique", xgm.CLIQUE6, 0),
+                           ("P23", xgm.CLIQUE6, 1), ("P24", xgm.CLIQUE7, 1)]:
         p = xgm.plan(name)
         assert (p.pattern, int(p.induced)) == (pat, ind), name
     with pytest.raises(xgm.XgmError) as e:

@@ -35,11 +35,11 @@ BUILD_CLEAN = 7
 VIEW_UNDIRECTED, VIEW_DAG = 0, 1
 
 TRIANGLE, CLIQUE4, CLIQUE5, DIAMOND, CYCLE4, TAILED_TRIANGLE = 1, 2, 3, 4, 5, 6
-WEDGE, STAR3, PATH4 = 7, 8, 9
+WEDGE, STAR3, PATH4, CLIQUE6, CLIQUE7 = 7, 8, 9, 10, 11
 PATTERN_NAMES = {"triangle": TRIANGLE, "4-clique": CLIQUE4, "5-clique": CLIQUE5,
                  "diamond": DIAMOND, "rectangle": CYCLE4, "4-cycle": CYCLE4,
                  "tailedtriangle": TAILED_TRIANGLE, "wedge": WEDGE, "3-star": STAR3,
-                 "4-path": PATH4}
+                 "4-path": PATH4, "6-clique": CLIQUE6, "7-clique": CLIQUE7}
 # order of the motif census (MotifSolver output)
 MOTIF3_NAMES = ["wedge", "triangle"]
 MOTIF4_NAMES = ["3-star", "4-path", "tailed-triangle", "4-cycle", "diamond", "4-clique"]

@@ -346,7 +346,7 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* d, xgm_plan** out
       return finish_status(ctx, pat == 0 ? XGM_ERR_UNSUPPORTED : XGM_ERR_INVALID);
     }
   }
-  if (pat < XGM_PATTERN_TRIANGLE || pat > XGM_PATTERN_PATH4) return XGM_ERR_INVALID;
+  if (pat < XGM_PATTERN_TRIANGLE || pat > XGM_PATTERN_CLIQUE7) return XGM_ERR_INVALID;
   xgm_plan* p = new xgm_plan();
   p->pattern = pat;
   p->induced = d->induced ? 1 : 0;
@@ -456,11 +456,13 @@ xgm_status xgm_tc_solver(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total) {
 }
 
 xgm_status xgm_clique_solver(xgm_ctx* ctx, const xgm_graph* g, int k, uint64_t* total) {
-  if (k < 3 || k > 5) {
-    set_thread_error("k-clique counting supports k = 3, 4, 5");
+  if (k < 3 || k > 7) {
+    set_thread_error("k-clique counting supports k = 3 .. 7");
     return finish_status(ctx, XGM_ERR_UNSUPPORTED);
   }
-  xgm_plan p{k == 3 ? XGM_PATTERN_TRIANGLE : (k == 4 ? XGM_PATTERN_CLIQUE4 : XGM_PATTERN_CLIQUE5)};
+  static const int kPat[8] = {0, 0, 0, XGM_PATTERN_TRIANGLE, XGM_PATTERN_CLIQUE4,
+                              XGM_PATTERN_CLIQUE5, XGM_PATTERN_CLIQUE6, XGM_PATTERN_CLIQUE7};
+  xgm_plan p{kPat[k]};
   return xgm_count(ctx, g, &p, nullptr, total, nullptr);
 }
 

@@ -190,6 +190,86 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
   return acc;
 }
 
+// D-cliques of the local DAG inside a candidate set, for the 6- and 7-clique plans
+// (local clique depth 5 and 6).  The set is warp-distributed: this lane holds word w;
+// every candidate l > i, so the walk of cta_count_rows carries over level by level:
+// the next level's set is this level's set & R_l.
+template <int D>
+__device__ uint64_t rows_deep(const uint32_t* rows, const int32_t* roff, uint32_t m, int w, int qi) {
+  if constexpr (D == 1) {
+    return (uint64_t)__popc(m);
+  } else {
+    uint64_t acc = 0;
+    unsigned nz = __ballot_sync(kFull, m != 0u);
+    while (nz) {
+      const int src = __ffs(nz) - 1;
+      nz &= nz - 1;
+      uint32_t bits = __shfl_sync(kFull, m, src);
+      while (bits) {
+        const int l = ((qi + src) << 5) + __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int ql = l >> 5;
+        const uint32_t m2 = (m && w >= ql) ? (m & rows[roff[l] + (w - ql)]) : 0u;
+        acc += rows_deep<D - 1>(rows, roff, m2, w, qi);
+      }
+    }
+    return acc;
+  }
+}
+
+template <int Q>
+__device__ uint64_t cta_count_deep(const uint32_t* rows, int s, const int32_t* roff) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int W = (s + 31) >> 5;
+  uint64_t acc = 0;
+  for (int i = warp; i < s; i += kCtaWarps) {
+    const int qi = i >> 5, nwi = W - qi;
+    const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
+    acc += rows_deep<Q - 1>(rows, roff, wi, qi + lane, qi);
+  }
+  return acc;
+}
+
+// The same for one-word rows (local sets of up to 32, one lane per row).
+template <int D>
+__device__ uint64_t word_deep(const uint32_t* rows, uint32_t m) {
+  if constexpr (D == 1) {
+    return (uint64_t)__popc(m);
+  } else {
+    uint64_t acc = 0;
+    while (m) {
+      const int l = __ffs(m) - 1;
+      m &= m - 1;
+      acc += word_deep<D - 1>(rows, m & rows[l]);
+    }
+    return acc;
+  }
+}
+
+// And for the wide tier's 4-word rows (row l at rows + l * 4; one lane per row).
+template <int D>
+__device__ uint64_t wide_deep(const uint32_t* rows, const uint32_t (&m)[4]) {
+  if constexpr (D == 1) {
+    return (uint64_t)(__popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]));
+  } else {
+    uint64_t acc = 0;
+#pragma unroll 1
+    for (int x = 0; x < 4; ++x) {
+      uint32_t bits = m[x];
+      while (bits) {
+        const int l = (x << 5) + __ffs(bits) - 1;
+        bits &= bits - 1;
+        const uint32_t* Rl = rows + l * 4;
+        uint32_t m2[4];
+#pragma unroll
+        for (int y = 0; y < 4; ++y) m2[y] = y >= x ? (m[y] & Rl[y]) : 0u;
+        acc += wide_deep<D - 1>(rows, m2);
+      }
+    }
+    return acc;
+  }
+}
+
 // Participation counters of the triangle-participation mode.
 struct Part {
   unsigned long long* v;  // per vertex (rank ids)
@@ -197,7 +277,7 @@ struct Part {
 };
 
 // The CTA has S[0..s) (sorted, local set) in shared memory.  Counts the Q-cliques of the
-// DAG induced on S, Q = 1..4.  PART (Q == 2 only, S = N+(root) starting at col entry
+// DAG induced on S, Q = 1..6.  PART (Q == 2 only, S = N+(root) starting at col entry
 // sbase): every local edge (i, j) is the triangle (root, S[i], S[j]); it is credited to
 // vertices S[i], S[j] and edges (root,S[i]), (root,S[j]), (S[i],S[j]).  The root's own
 // credit is the returned count.
@@ -345,6 +425,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   }
   if (Q == 3) acc = cta_count_rows<3, WGT>(rows, s, pre, roff);
   if (Q == 4) acc = cta_count_rows<4, false>(rows, s, pre, roff);
+  if constexpr (Q >= 5) acc = cta_count_deep<Q>(rows, s, roff);
   return acc;
 }
 
@@ -515,7 +596,7 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
     atomicAdd(&part.v[w.S[lane]], (unsigned long long)w.cnt[lane]);
     atomicAdd(&part.e[d0.x + lane], w.cnt[lane]);
   }
-  if (Q >= 3 && lane < s) {
+  if (Q >= 3 && Q <= 4 && lane < s) {
     const uint32_t r = w.rows[lane];
     uint32_t bits = r;
     while (bits) {
@@ -542,6 +623,9 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
         }
       }
     }
+  }
+  if constexpr (Q >= 5) {
+    if (lane < s) acc += word_deep<Q - 1>(w.rows, w.rows[lane]);
   }
   __syncwarp();
   return acc;
@@ -620,7 +704,7 @@ __device__ uint64_t warp_search_task(const GView& g, WarpSmem& w, int32_t v0, Pa
     atomicAdd(&part.v[w.S[lane]], (unsigned long long)w.cnt[lane]);
     atomicAdd(&part.e[d0.x + lane], w.cnt[lane]);
   }
-  if (Q >= 3 && lane < s) {
+  if (Q >= 3 && Q <= 4 && lane < s) {
     const uint32_t r = w.rows[lane];
     uint32_t bits = r;
     while (bits) {
@@ -647,6 +731,9 @@ __device__ uint64_t warp_search_task(const GView& g, WarpSmem& w, int32_t v0, Pa
         }
       }
     }
+  }
+  if constexpr (Q >= 5) {
+    if (lane < s) acc += word_deep<Q - 1>(w.rows, w.rows[lane]);
   }
   __syncwarp();
   return acc;
@@ -784,7 +871,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
         atomicAdd(&part.v[w.S[r]], (unsigned long long)w.cnt[r]);
         atomicAdd(&part.e[d0.x + r], w.cnt[r]);
       }
-  if (Q >= 3) {
+  if (Q >= 3 && Q <= 4) {
     for (int r = lane; r < s; r += 32) {
       const uint32_t* Rr = w.rows + r * kWideWords;
       for (int wj = r >> 5; wj < kWideWords; ++wj) {
@@ -824,6 +911,14 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
       }
     }
   }
+  if constexpr (Q >= 5) {
+    for (int r = lane; r < s; r += 32) {
+      uint32_t m[4];
+#pragma unroll
+      for (int y = 0; y < 4; ++y) m[y] = w.rows[r * kWideWords + y];
+      acc += wide_deep<Q - 1>(w.rows, m);
+    }
+  }
   __syncwarp();
   return acc;
 }
@@ -845,7 +940,7 @@ __device__ __forceinline__ void emit(const GOut& o, int32_t v0, uint64_t r, uint
   }
 }
 
-// K = clique size (3, 4, 5).  MODE kModePart (K == 3) credits triangle participation to
+// K = clique size (3..7).  MODE kModePart (K == 3) credits triangle participation to
 // `part` instead of counting; kModeWeight (K <= 4) weights each clique by the out-degree
 // of its highest-ranked vertex; kModeMulti (K == 4) emits triangles to o.slot and
 // 4-cliques to o.slot2 and credits participation.
@@ -1060,6 +1155,8 @@ cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads*
     case 3: return launch_k<3, kModeCount>(g, t, q, count, err, none, grid, s, o);
     case 4: return launch_k<4, kModeCount>(g, t, q, count, err, none, grid, s, o);
     case 5: return launch_k<5, kModeCount>(g, t, q, count, err, none, grid, s, o);
+    case 6: return launch_k<6, kModeCount>(g, t, q, count, err, none, grid, s, o);
+    case 7: return launch_k<7, kModeCount>(g, t, q, count, err, none, grid, s, o);
     default: return cudaErrorInvalidValue;
   }
 }

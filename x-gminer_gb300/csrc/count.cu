@@ -29,6 +29,8 @@ int clique_kind(int pattern) {
     case XGM_PATTERN_TRIANGLE: return 3;
     case XGM_PATTERN_CLIQUE4: return 4;
     case XGM_PATTERN_CLIQUE5: return 5;
+    case XGM_PATTERN_CLIQUE6: return 6;
+    case XGM_PATTERN_CLIQUE7: return 7;
     default: return 0;
   }
 }
@@ -54,8 +56,8 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
       set_thread_error("XGM_SCHED_LEARNED needs a trained model (xgm_sched.model)");
       return XGM_ERR_INVALID;
     }
-    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, s));
     order = sp.order_by_cost != 0;
+    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, order, s));
   } else if (sp.policy == XGM_SCHED_TUNED) {
     if (!sp.table) {
       set_thread_error("XGM_SCHED_TUNED needs a variant table (xgm_sched.table)");
@@ -258,6 +260,11 @@ xgm_status algo_bytes_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, uin
   const GView view = g.view();
   unsigned long long* acc = &ctx->d_sc->count;
   const int k = clique_kind(pattern);
+  if (k > 5) {
+    set_thread_error("algorithmic bytes cover the triangle, 4/5-clique and edge-induced "
+                     "motif plans");
+    return XGM_ERR_UNSUPPORTED;
+  }
   xgm_sched heur;
   std::memset(&heur, 0, sizeof(heur));
   if (k) {
@@ -456,7 +463,8 @@ xgm_status count_motifs(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched&
 xgm_status count_plan(xgm_ctx* ctx, const DevGraph& g, int pattern, int induced,
                       const xgm_sched& sp, uint64_t* out, xgm_stats& st) {
   const bool clique = pattern == XGM_PATTERN_TRIANGLE || pattern == XGM_PATTERN_CLIQUE4 ||
-                      pattern == XGM_PATTERN_CLIQUE5;
+                      pattern == XGM_PATTERN_CLIQUE5 || pattern == XGM_PATTERN_CLIQUE6 ||
+                      pattern == XGM_PATTERN_CLIQUE7;
   const bool kernel = pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_CYCLE4 ||
                       pattern == XGM_PATTERN_TAILED_TRIANGLE;
   if (clique || (kernel && !induced)) return count_dispatch(ctx, g, pattern, sp, out, st);
@@ -522,6 +530,8 @@ int match_pattern(const xgm_plan_desc* d) {
   if (n == 3 && m == 3) return XGM_PATTERN_TRIANGLE;
   if (n == 4 && m == 6) return XGM_PATTERN_CLIQUE4;
   if (n == 5 && m == 10) return XGM_PATTERN_CLIQUE5;
+  if (n == 6 && m == 15) return XGM_PATTERN_CLIQUE6;
+  if (n == 7 && m == 21) return XGM_PATTERN_CLIQUE7;
   if (n == 4 && m == 5) return XGM_PATTERN_DIAMOND;  // K4 minus one edge
   if (n == 4 && m == 4 && sorted[0] == 2 && sorted[3] == 2) return XGM_PATTERN_CYCLE4;
   if (n == 4 && m == 4 && sorted[0] == 1 && sorted[1] == 2 && sorted[2] == 2 && sorted[3] == 3)
@@ -541,6 +551,8 @@ int pattern_from_name(const char* name, int* induced, uint64_t* scale) {
     return XGM_PATTERN_TRIANGLE;
   if (s == "4-clique" || s == "clique4" || s == "k4") return XGM_PATTERN_CLIQUE4;
   if (s == "5-clique" || s == "clique5" || s == "k5") return XGM_PATTERN_CLIQUE5;
+  if (s == "6-clique" || s == "clique6" || s == "k6") return XGM_PATTERN_CLIQUE6;
+  if (s == "7-clique" || s == "clique7" || s == "k7") return XGM_PATTERN_CLIQUE7;
   if (s == "diamond" || s == "4-diamond") return XGM_PATTERN_DIAMOND;
   if (s == "rectangle" || s == "4-cycle" || s == "cycle4") return XGM_PATTERN_CYCLE4;
   if (s == "tailedtriangle" || s == "tailed-triangle" || s == "tailed_triangle" ||
@@ -561,6 +573,8 @@ int pattern_from_name(const char* name, int* induced, uint64_t* scale) {
   else if (s == "P3") p = XGM_PATTERN_TAILED_TRIANGLE;
   else if (s == "P4") p = XGM_PATTERN_CLIQUE4;
   else if (s == "P5") p = XGM_PATTERN_CLIQUE5;
+  else if (s == "P23") p = XGM_PATTERN_CLIQUE6;
+  else if (s == "P24") p = XGM_PATTERN_CLIQUE7;
   if (p) {
     if (induced) *induced = 1;
     if (scale) *scale = k;

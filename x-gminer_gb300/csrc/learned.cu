@@ -43,13 +43,14 @@ __host__ __device__ inline float variant_warps(int v) {
 __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   const longlong2 d0 = g.dptr[r];
   const long long s = d0.y - d0.x;
-  double sum = 0, sumsq = 0;
-  long long maxd = 0;
+  // fp32 / integer sums (the GPU's fp64 rate is a small fraction of its fp32 rate)
+  long long sum = 0, maxd = 0;
+  float sumsq = 0.0f;
   for (long long e = d0.x; e < d0.y; ++e) {
     const longlong2 d = g.dptr[g.col[e]];
     const long long l = d.y - d.x;
-    sum += (double)l;
-    sumsq += (double)l * (double)l;
+    sum += l;
+    sumsq = fmaf((float)l, (float)l, sumsq);
     maxd = l > maxd ? l : maxd;
   }
   const long long deg = d0.y - g.rowptr[r];
@@ -58,8 +59,8 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   f[1] = log2f(1.0f + (float)sum) / 24.0f;
   f[2] = log2f(1.0f + (float)maxd) / 11.0f;
   f[3] = log2f(1.0f + (float)deg) / 18.0f;
-  f[4] = log2f(1.0f + (float)sumsq) / 34.0f;
-  f[5] = (float)(sum / ((double)s * (double)maxd + 1.0));
+  f[4] = log2f(1.0f + sumsq) / 34.0f;
+  f[5] = (float)sum / ((float)s * (float)maxd + 1.0f);
   f[6] = (float)(k - 3) * 0.5f;
   f[7] = f[8] = f[9] = f[10] = f[11] = 0.0f;
 }
@@ -81,7 +82,26 @@ __device__ __forceinline__ void load_params(const __half* wh, float* P) {
   __syncthreads();
 }
 
-__global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* var, float* cost) {
+// The model over the five variants of one task: the first layer's task-shape part
+// (features 0-6) is shared, each variant adds its one-hot column.
+__device__ __forceinline__ void mlp_variants(const float* P, const float* f, const bool* cand,
+                                             float* pred) {
+#pragma unroll
+  for (int v = 0; v < XGM_NUM_VARIANTS; ++v) pred[v] = P[kOffB2];
+#pragma unroll 4
+  for (int h = 0; h < kHidden; ++h) {
+    float a = P[kOffB1 + h];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) a = fmaf(P[h * kFeat + j], f[j], a);
+    const float w2 = P[kOffW2 + h];
+#pragma unroll
+    for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
+      if (cand[v]) pred[v] = fmaf(w2, fmaxf(a + P[h * kFeat + 7 + v], 0.0f), pred[v]);
+  }
+}
+
+__global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* var, float* cost,
+                                   int need_cost) {
   __shared__ float P[kParams];
   load_params(wh, P);
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < g.nv;
@@ -93,24 +113,30 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
       cost[r] = 0.0f;
       continue;
     }
-    float f[kFeat];
-    task_features(g, (int32_t)r, k, f);
     // the plain heuristic's variant stays unless the model predicts a clear saving
     const uint8_t hv = s <= kWarpCap ? VAR_WARP : s <= kWideCap ? VAR_WIDE
                        : s <= kCtaCap ? VAR_CTA : VAR_SPLIT;
-    float pred[XGM_NUM_VARIANTS];
+    bool cand[XGM_NUM_VARIANTS];
+    int ncand = 0;
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v) {
-      pred[v] = 3.0e38f;
-      if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && s > kWarpCap) continue;
-      if (v == XGM_VAR_WIDE && s > kWideCap) continue;
-      if (v == XGM_VAR_CTA && s > kCtaCap) continue;
       // edge-splitting stays the capacity fallback: splitting a task a CTA can hold
       // multiplies its set-up work and never paid off in any measured configuration
-      if (v == XGM_VAR_SPLIT && s <= kCtaCap) continue;
-      f[7 + v] = 1.0f;
-      pred[v] = mlp_forward(P, f);
-      f[7 + v] = 0.0f;
+      cand[v] = !(((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && s > kWarpCap) ||
+                  (v == XGM_VAR_WIDE && s > kWideCap) || (v == XGM_VAR_CTA && s > kCtaCap) ||
+                  (v == XGM_VAR_SPLIT && s <= kCtaCap));
+      ncand += cand[v];
     }
+    if (ncand == 1 && !need_cost) {  // nothing to decide and no order to give
+      var[r] = hv;
+      cost[r] = 0.0f;
+      continue;
+    }
+    float f[kFeat];
+    task_features(g, (int32_t)r, k, f);
+    float pred[XGM_NUM_VARIANTS];
+    mlp_variants(P, f, cand, pred);
+    for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
+      if (!cand[v]) pred[v] = 3.0e38f;
     uint8_t bv = hv;
     float best = pred[hv];
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
@@ -233,6 +259,8 @@ int clique_k(int pattern) {
     case XGM_PATTERN_TRIANGLE: return 3;
     case XGM_PATTERN_CLIQUE4: return 4;
     case XGM_PATTERN_CLIQUE5: return 5;
+    case XGM_PATTERN_CLIQUE6: return 6;
+    case XGM_PATTERN_CLIQUE7: return 7;
     case XGM_PATTERN_DIAMOND:
     case XGM_PATTERN_TAILED_TRIANGLE: return 3;  // same task structure (k = 3 kernel)
     default: return 0;
@@ -242,9 +270,10 @@ int clique_k(int pattern) {
 }  // namespace
 
 cudaError_t classify_learned(const DevGraph& g, int k, const xgm_model& m, TaskBuf& tb,
-                             cudaStream_t s) {
+                             bool need_cost, cudaStream_t s) {
   if (g.nv == 0) return cudaSuccess;
-  k_classify_learned<<<grid_for(g.nv), kThreads, 0, s>>>(g.view(), k, m.wh, tb.var, tb.cost);
+  k_classify_learned<<<grid_for(g.nv), kThreads, 0, s>>>(g.view(), k, m.wh, tb.var, tb.cost,
+                                                         need_cost ? 1 : 0);
   return cudaGetLastError();
 }
 
