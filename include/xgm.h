@@ -183,7 +183,10 @@ typedef enum {
   XGM_VAR_SPLIT = 2,  /* task split into per-edge sub-tasks (hub vertices) */
   XGM_VAR_WIDE = 3,   /* one warp per task, 4-word frontier bitmap rows (out-degree <= 128) */
   XGM_VAR_SEARCH = 4, /* one warp per task (out-degree <= 32), rows by binary search */
-  XGM_NUM_VARIANTS = 5
+  XGM_VAR_BUCKET = 5, /* as SEARCH, behind X-GMiner's bucket-bitmap pre-filter: 16 buckets
+                         per out-list, only common buckets searched
+                         (xgminer/include/xgminer_bitmap.cuh:161-278, 661-813) */
+  XGM_NUM_VARIANTS = 6
 } xgm_variant;
 
 /* Autotuned schedule: the variant for each out-degree bucket.  Bucket b holds
@@ -205,6 +208,7 @@ typedef struct {
   int flags;              /* XGM_SCHED_NO_GRAPH: batched calls launch directly, no CUDA graph */
   int wide_max;           /* heuristic: out-degree <= wide_max -> WIDE (0: default 128; -1: none) */
   int search_max;         /* heuristic: out-degree <= search_max -> SEARCH (0: none) */
+  int bucket_max;         /* heuristic: out-degree <= bucket_max -> BUCKET (0: none) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };
@@ -297,14 +301,14 @@ xgm_status xgm_count_batched(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const* 
 void xgm_batch_destroy(xgm_batch* b);
 
 /* -------------------------------------------------------------- cost model */
-/* Learned scheduler: a 12 -> 32 (ReLU) -> 1 MLP with fp16 weights and fp32
+/* Learned scheduler: a 13 -> 32 (ReLU) -> 1 MLP with fp16 weights and fp32
  * accumulation that predicts log2(warp-cycles) of a task under a kernel variant.  It is
  * trained by the engine's own forward/backward kernels on per-task timings the engine
  * logs (xgm_model_collect), and used by XGM_SCHED_LEARNED to pick each task's variant
  * and to order the queues heaviest-first.  It changes the schedule only, never a count.
  * No counterpart in the reference (its schedule is the fixed heuristic of
  * xgminer/include/glumin/common.h:114-116). */
-#define XGM_MODEL_FEATURES 12
+#define XGM_MODEL_FEATURES 13
 #define XGM_MODEL_HIDDEN 32
 #define XGM_MODEL_PARAMS (XGM_MODEL_HIDDEN * XGM_MODEL_FEATURES + 2 * XGM_MODEL_HIDDEN + 1)
 

@@ -64,12 +64,15 @@ def test_schedules_never_change_counts(xgm, ctx):
     g = ctx.graph_from_edges(nv, s, d)
     for pat in ("triangle", "4-clique", "5-clique", "diamond", "tailedtriangle"):
         base = ctx.count(g, pat)
-        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE, xgm.VAR_SEARCH):
+        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE, xgm.VAR_SEARCH,
+                    xgm.VAR_BUCKET):
             assert ctx.count(g, pat, policy=xgm.SCHED_FIXED, variant=var) == base, (pat, var)
         for smax, wmax, dmax, cmax in ((0, 8, 0, 64), (8, 32, 64, 128), (32, 1, -1, 1),
                                        (4, 16, 100, 2048)):
             assert ctx.count(g, pat, search_max=smax, warp_max=wmax, wide_max=dmax,
                              cta_max=cmax) == base, (pat, smax, wmax, dmax, cmax)
+        for bmax, smax in ((32, 0), (8, 32), (1, 4)):  # bucket-filtered search tiers
+            assert ctx.count(g, pat, bucket_max=bmax, search_max=smax) == base, (pat, bmax)
 
 
 def test_upload_paths_agree(xgm, ctx, orc):

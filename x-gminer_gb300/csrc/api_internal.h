@@ -82,6 +82,7 @@ xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm
 void motif_buffers_free(xgm_ctx* ctx);
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
                          cudaStream_t s);
+bool sched_may_bucket(const xgm_sched& sp);  // the policy can assign the BUCKET variant
 int ensure_clique_grid(xgm_ctx* ctx);
 int match_pattern(const xgm_plan_desc* d);  // builtin id, 0 unsupported, -1 malformed
 // Builtin id for a pattern name (0 if unknown); GLUMIN ids also set induced / scale.

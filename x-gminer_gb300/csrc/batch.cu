@@ -181,7 +181,8 @@ cudaError_t alloc_once(T** p, int64_t n, cudaStream_t s, bool zero = false) {
 }
 
 // Allocations a sequence needs, made before any capture.
-xgm_status batch_prepare(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P) {
+xgm_status batch_prepare(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P,
+                         const xgm_sched& sp) {
   cudaStream_t s = ctx->stream;
   const DevGraph& g = b->graph.g;
   const int64_t need = (int64_t)b->num_graphs * P;
@@ -212,6 +213,7 @@ xgm_status batch_prepare(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P) {
     XGM_CUDA_TRY(alloc_once(&b->c4_n, 2, s));
   }
   ensure_clique_grid(ctx);
+  if (sched_may_bucket(sp)) XGM_CUDA_TRY(ensure_bucket_index(g, s));  // before any capture
   XGM_CUDA_TRY(cudaStreamSynchronize(s));
   return XGM_OK;
 }
@@ -277,6 +279,8 @@ std::string sched_key(const Slots& sl, const xgm_sched& sp) {
   k.append(reinterpret_cast<const char*>(&sp.policy), sizeof(int) * 2);
   k.append(reinterpret_cast<const char*>(&sp.model), sizeof(void*));
   k.append(reinterpret_cast<const char*>(&sp.warp_max), sizeof(int) * 3);
+  const int more[3] = {sp.wide_max, sp.search_max, sp.bucket_max};
+  k.append(reinterpret_cast<const char*>(more), sizeof(more));
   if (sp.table) k.append(reinterpret_cast<const char*>(sp.table), sizeof(xgm_tune_table));
   return k;
 }
@@ -288,7 +292,7 @@ xgm_status count_batched_impl(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const*
   Slots sl;
   xgm_status r = slots_of(plans, P, sl);
   if (r != XGM_OK) return r;
-  r = batch_prepare(ctx, b, sl, P);
+  r = batch_prepare(ctx, b, sl, P, sp);
   if (r != XGM_OK) return r;
   const bool use_graph = !(sp.flags & XGM_SCHED_NO_GRAPH);
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
@@ -512,7 +516,8 @@ xgm_status xgm_autotune(xgm_ctx* ctx, const xgm_graph* g, xgm_batch* b, const xg
       uint8_t bestv = keep;
       for (uint8_t v = 0; v < XGM_NUM_VARIANTS; ++v) {
         if (v == keep) continue;
-        if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && smin > kWarpCap) continue;
+        if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH || v == XGM_VAR_BUCKET) && smin > kWarpCap)
+          continue;
         if (v == XGM_VAR_WIDE && smin > kWideCap) continue;
         if (v == XGM_VAR_CTA && smin > kCtaCap) continue;
         tab.variant[k] = v;

@@ -739,6 +739,66 @@ __device__ uint64_t warp_search_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   return acc;
 }
 
+// One warp, local set S = N+(v0) with s <= 32, rows by binary search behind X-GMiner's
+// bucket-bitmap pre-filter (xgminer/include/xgminer_bitmap.cuh:161-278): for row i,
+// lane j-i-1 tests bucket b = S[j] & 15 against the bucket bitmap of N+(S[i]) and
+// searches only that bucket of the bucket-grouped list (about 1/16 of it).  Plain
+// counting only (the participation and weighted modes run these tasks as SEARCH).
+template <int Q>
+__device__ uint64_t warp_bucket_task(const GView& g, WarpSmem& w, int32_t v0) {
+  static_assert(Q >= 2, "bucket tasks count at least local edges");
+  const int lane = threadIdx.x & 31;
+  const longlong2 d0 = ldg_ll2(g.dptr + v0);
+  const int s = (int)(d0.y - d0.x);
+  int32_t xs = 0, deg = 0;
+  long long base = 0;
+  uint32_t msk = 0u;
+  if (lane < s) {
+    xs = ldg_i32(g.col + d0.x + lane);
+    w.S[lane] = xs;
+    const longlong2 dx = ldg_ll2(g.dptr + xs);
+    base = dx.x;
+    deg = (int32_t)(dx.y - dx.x);
+    msk = g.bmask[xs];
+  }
+  w.rows[lane] = 0u;
+  __syncwarp();
+  uint64_t acc = 0;
+  for (int i = 0; i + 1 < s; ++i) {
+    const int32_t u = __shfl_sync(kFull, xs, i);
+    const long long bu = __shfl_sync(kFull, base, i);
+    const uint32_t mu = __shfl_sync(kFull, msk, i);
+    const int32_t du = __shfl_sync(kFull, deg, i);
+    const int j = i + 1 + lane;
+    bool found = false;
+    if (j < s) {
+      const int32_t y = w.S[j];
+      const int b = y & (kBuckets - 1);
+      if ((mu >> b) & 1u) {
+        const uint32_t* off = g.boff + (int64_t)u * kBuckets;
+        long long lo = bu + off[b];
+        const long long end = bu + (b + 1 < kBuckets ? (long long)off[b + 1] : (long long)du);
+        long long hi = end;
+        while (lo < hi) {
+          const long long mid = (lo + hi) >> 1;
+          if (ldg_i32(g.bcol + mid) < y) lo = mid + 1; else hi = mid;
+        }
+        found = lo < end && ldg_i32(g.bcol + lo) == y;
+      }
+    }
+    const unsigned bal = __ballot_sync(kFull, found);
+    if (Q == 2) {
+      acc += found ? 1u : 0u;
+    } else if (lane == 0) {
+      w.rows[i] = bal << (i + 1);
+    }
+  }
+  __syncwarp();
+  if (Q >= 3 && lane < s) acc += word_deep<Q - 1>(w.rows, w.rows[lane]);
+  __syncwarp();
+  return acc;
+}
+
 // One warp, local set S = N+(v0) with s <= 128 (rows of 4 words): Q-cliques of the
 // local DAG.  Same walk as the CTA tier (segment registers, four loads in flight, Bloom
 // pre-filter) with binary search in S; counting gives each lane whole rows.
@@ -956,7 +1016,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
   __shared__ long long task_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long n_split = t.n[0], n_cta = t.n[1], n_warp = t.n[2], n_hubs = t.n[3];
-  const long long n_wide = t.n[4], n_search = t.n[5];
+  const long long n_wide = t.n[4], n_search = t.n[5], n_bucket = t.n[6];
   uint64_t acc = 0;
 
   // 1) hub edge sub-tasks: local set N+(v0) & N+(v1), (K-2)-cliques of it
@@ -1088,6 +1148,31 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
       else if (!PART) emit(o, v0, r, 0, acc);
     }
     if (t.log_search && lane == 0) t.log_search[ti] = clock64() - c0;
+  }
+  for (;;) {  // bucket-filtered search tasks (run as SEARCH outside plain counting)
+    long long ti = 0;
+    if (lane == 0) ti = (long long)atomicAdd(&q->bucket, 1ull);
+    ti = __shfl_sync(kFull, ti, 0);
+    if (ti >= n_bucket) break;
+    const long long c0 = t.log_bucket ? clock64() : 0;
+    const int32_t v0 = t.bucket[ti];
+    const longlong2 d0 = ldg_ll2(g.dptr + v0);
+    const int s = (int)(d0.y - d0.x);
+    if (s > kWarpCap) {
+      if (lane == 0) atomicOr(err, ERR_CAPACITY);
+    } else if (s >= kMinS) {
+      uint64_t q2 = 0, r;
+      if (MODE == kModeCount && g.bcol) r = warp_bucket_task<K - 1>(g, ws, v0);
+      else r = warp_search_task<K - 1, MODE>(g, ws, v0, part, &q2);
+      if (PART) {
+        const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
+        if (lane == 0 && tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
+      }
+      if (MULTI) emit(o, v0, q2, r, acc);
+      else if (MODE == kModeWeight) acc += r;
+      else if (!PART) emit(o, v0, r, 0, acc);
+    }
+    if (t.log_bucket && lane == 0) t.log_bucket[ti] = clock64() - c0;
   }
   for (;;) {
     long long ti = 0;

@@ -15,7 +15,8 @@ constexpr int kWideWords = 4;               // bitmap words per row of a wide-wa
 // Task lists of one counting launch.  Sizes live on the device (`n`), so task
 // generation and counting run without a host round trip and can be graph-captured:
 //   n[0] = hub edge sub-tasks, n[1] = CTA vertex tasks, n[2] = warp vertex tasks,
-//   n[3] = hub vertices, n[4] = wide-warp vertex tasks, n[5] = binary-search warp tasks.
+//   n[3] = hub vertices, n[4] = wide-warp vertex tasks, n[5] = binary-search warp tasks,
+//   n[6] = bucket-filtered binary-search warp tasks.
 // Hub sub-task t belongs to hub split_v[h] with split_off[h] <= t < split_off[h+1];
 // its second vertex is the (t - split_off[h])-th out-neighbour of the hub.
 // Per-task timing logs (clock64 cycles) are indexed like the lists; any may be null.
@@ -24,6 +25,7 @@ struct TaskLists {
   const int32_t* warp = nullptr;   // vertex tasks run by one warp (out-degree <= kWarpCap)
   const int32_t* wide = nullptr;   // vertex tasks run by one warp with 4-word rows (<= kWideCap)
   const int32_t* search = nullptr; // warp tasks (<= kWarpCap) built by binary search
+  const int32_t* bucket = nullptr; // warp tasks (<= kWarpCap), bucket-filtered search
   const int32_t* split_v = nullptr;
   const int64_t* split_off = nullptr;
   const int64_t* n = nullptr;
@@ -32,6 +34,7 @@ struct TaskLists {
   long long* log_split = nullptr;
   long long* log_wide = nullptr;
   long long* log_search = nullptr;
+  long long* log_bucket = nullptr;
 };
 
 // Per-graph outputs of batched launches: task totals go to out[gid[v0] * stride + slot]
@@ -46,14 +49,14 @@ struct GOut {
 
 // Work-queue heads, zeroed before each launch.
 struct QueueHeads {
-  unsigned long long split, cta, warp, wide, search, pad[3];
+  unsigned long long split, cta, warp, wide, search, bucket, pad[2];
 };
 
 size_t clique_smem_bytes();
 // Resident counting CTAs per SM (dynamic shared memory bound).
 cudaError_t clique_occupancy(int* per_sm);
 
-// k in {3, 4, 5}: adds the k-clique count of g (DAG) over the listed tasks to *count.
+// k in {3, ..., 7}: adds the k-clique count of g (DAG) over the listed tasks to *count.
 cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads* q,
                           unsigned long long* count, uint32_t* err, int grid, cudaStream_t s,
                           const GOut& o = GOut{});

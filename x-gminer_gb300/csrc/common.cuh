@@ -24,11 +24,20 @@ enum : uint32_t {
 // rank(v) > rank(u), and the out-neighbours N+(r) of r are the upper part of its
 // sorted undirected row: col[dptr[r].x .. dptr[r].y).  Lower part (ids < r):
 // col[rowptr[r] .. dptr[r].x).
+// Bucket index of the out-lists (the BUCKET variant; null until a schedule needs it):
+// out-list N+(u) = col[dptr[u].x, dptr[u].y) regrouped by bucket b = id & 15 into
+// bcol[dptr[u].x, ...), ascending inside a bucket; bucket b starts boff[16u + b]
+// entries into the row; bit b of bmask[u] is set iff bucket b is not empty.
+constexpr int kBuckets = 16;
+
 struct GView {
   const int32_t* col;        // undirected adjacency, rank ids, sorted rows
   const int64_t* rowptr;     // [V+1] undirected row starts
   const longlong2* dptr;     // [V] {first out-neighbour, row end}
   int64_t nv;
+  const int32_t* bcol = nullptr;    // [E] bucket-grouped out-lists (same row positions)
+  const uint32_t* boff = nullptr;   // [16 V] bucket starts within each out-list
+  const uint16_t* bmask = nullptr;  // [V] non-empty buckets
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

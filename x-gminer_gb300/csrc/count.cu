@@ -46,8 +46,21 @@ int ensure_clique_grid(xgm_ctx* ctx) {
   return ctx->clique_grid;
 }
 
+bool sched_may_bucket(const xgm_sched& sp) {
+  if (sp.policy == XGM_SCHED_LEARNED) return true;
+  if (sp.policy == XGM_SCHED_FIXED) return sp.variant == XGM_VAR_BUCKET;
+  if (sp.policy == XGM_SCHED_TUNED && sp.table) {
+    for (int b = 0; b < XGM_TUNE_BUCKETS; ++b)
+      if (sp.table->variant[b] == XGM_VAR_BUCKET) return true;
+    return false;
+  }
+  return sp.bucket_max > 0;
+}
+
 // Fills tb from the schedule policy for a k-clique style launch (k = 3 for the
-// participation and multi-pattern launches).
+// participation and multi-pattern launches).  Builds the graph's bucket index first
+// when the policy can pick BUCKET (outside stream capture: callers that capture call
+// ensure_bucket_index before they begin).
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
                          cudaStream_t s) {
   bool order = false;
@@ -57,14 +70,21 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
       return XGM_ERR_INVALID;
     }
     order = sp.order_by_cost != 0;
+    XGM_CUDA_TRY(ensure_bucket_index(g, s));  // the model may pick BUCKET
     XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, order, s));
   } else if (sp.policy == XGM_SCHED_TUNED) {
     if (!sp.table) {
       set_thread_error("XGM_SCHED_TUNED needs a variant table (xgm_sched.table)");
       return XGM_ERR_INVALID;
     }
+    for (int b = 0; b < XGM_TUNE_BUCKETS; ++b)
+      if (sp.table->variant[b] == XGM_VAR_BUCKET) {
+        XGM_CUDA_TRY(ensure_bucket_index(g, s));
+        break;
+      }
     XGM_CUDA_TRY(classify_table(g, k - 1, *sp.table, tb, s));
   } else {
+    int bmax = sp.bucket_max > 0 ? sp.bucket_max : 0;
     int smax = sp.search_max > 0 ? sp.search_max : 0;
     int wmax = sp.warp_max > 0 ? sp.warp_max : kWarpCap;
     int dmax = sp.wide_max > 0 ? sp.wide_max : (sp.wide_max < 0 ? 0 : kWideCap);
@@ -76,6 +96,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
         case XGM_VAR_WIDE: wmax = 0; dmax = kWideCap; cmax = kCtaCap; break;
         case XGM_VAR_CTA: wmax = 0; dmax = 0; cmax = kCtaCap; break;
         case XGM_VAR_SPLIT: wmax = 0; dmax = 0; cmax = 0; break;
+        case XGM_VAR_BUCKET: bmax = kWarpCap; wmax = 0; dmax = kWideCap; cmax = kCtaCap; break;
         default:
           set_thread_error("unknown variant for XGM_SCHED_FIXED");
           return XGM_ERR_INVALID;
@@ -84,7 +105,8 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
       set_thread_error("unknown schedule policy");
       return XGM_ERR_INVALID;
     }
-    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax));
+    if (bmax > 0) XGM_CUDA_TRY(ensure_bucket_index(g, s));
+    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax, bmax));
   }
   XGM_CUDA_TRY(build_lists(g, tb, order, s));
   return XGM_OK;
@@ -185,7 +207,7 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   }
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   if (k || pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_TAILED_TRIANGLE)
-    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 6,
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 7,
                                  cudaMemcpyDeviceToDevice, s));
   xgm_status r = ctx_sync_scalars(ctx);
   if (r != XGM_OK) return r;
@@ -201,8 +223,9 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   st.variant_tasks[XGM_VAR_SPLIT] = ctx->h_sc->n[0];
   st.variant_tasks[XGM_VAR_WIDE] = ctx->h_sc->n[4];
   st.variant_tasks[XGM_VAR_SEARCH] = ctx->h_sc->n[5];
+  st.variant_tasks[XGM_VAR_BUCKET] = ctx->h_sc->n[6];
   st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4] +
-             ctx->h_sc->n[5];
+             ctx->h_sc->n[5] + ctx->h_sc->n[6];
   r = check_device_flag(ctx, ctx->h_sc->err);
   if (r != XGM_OK) return r;
   *out = ctx->h_sc->count;
@@ -222,6 +245,7 @@ xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm
     return XGM_ERR_UNSUPPORTED;
   }
   ensure_clique_grid(ctx);
+  if (sched_may_bucket(sp)) XGM_CUDA_TRY(ensure_bucket_index(g, s));
   XGM_CUDA_TRY(cudaStreamSynchronize(s));
   XGM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   xgm_status r = schedule_tasks(ctx, g, k, sp);
@@ -336,7 +360,7 @@ xgm_status motif_terms(xgm_ctx* ctx, const DevGraph& g, const xgm_sched& sp, boo
                                   ctx->d_sc->terms, s));
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   if (part)
-    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 6,
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 7,
                                  cudaMemcpyDeviceToDevice, s));
   xgm_status r = ctx_sync_scalars(ctx);
   if (r != XGM_OK) return r;
@@ -354,8 +378,9 @@ xgm_status motif_terms(xgm_ctx* ctx, const DevGraph& g, const xgm_sched& sp, boo
     st.variant_tasks[XGM_VAR_SPLIT] = ctx->h_sc->n[0];
     st.variant_tasks[XGM_VAR_WIDE] = ctx->h_sc->n[4];
     st.variant_tasks[XGM_VAR_SEARCH] = ctx->h_sc->n[5];
+    st.variant_tasks[XGM_VAR_BUCKET] = ctx->h_sc->n[6];
     st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4] +
-               ctx->h_sc->n[5];
+               ctx->h_sc->n[5] + ctx->h_sc->n[6];
   }
   r = check_device_flag(ctx, ctx->h_sc->err);
   if (r != XGM_OK) return r;

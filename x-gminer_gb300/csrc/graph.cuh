@@ -23,11 +23,18 @@ struct DevGraph {
   int32_t* col = nullptr;    // [ne] rank space, sorted rows
   longlong2* dptr = nullptr; // [nv] {first out-neighbour, row end}
   int32_t* gid = nullptr;    // [nv] rank -> graph id (batched graphs only)
+  // bucket index (GView), built on first use by a schedule that can pick BUCKET
+  mutable int32_t* bcol = nullptr;
+  mutable uint32_t* boff = nullptr;
+  mutable uint16_t* bmask = nullptr;
 
-  GView view() const { return GView{col, rowptr, dptr, nv}; }
+  GView view() const { return GView{col, rowptr, dptr, nv, bcol, boff, bmask}; }
 };
 
 void free_graph(DevGraph& g, cudaStream_t s);
+
+// Builds g's bucket index once (bucket.cu); later calls return at once.
+cudaError_t ensure_bucket_index(const DevGraph& g, cudaStream_t s);
 
 // Raw samples on the device -> undirected CSR in original ids (g.rowptr_o/col_o).
 // flags: XGM_BUILD_* bits.  err (device) gets ERR_BOUNDS for ids outside [0, nv).

@@ -1,4 +1,4 @@
-// Learned scheduler: task features, a 12 -> 32 -> 1 MLP (fp16 weights, fp32
+// Learned scheduler: task features, a 13 -> 32 -> 1 MLP (fp16 weights, fp32
 // accumulation) with hand-written forward / backward / Adam kernels, the fused
 // classify kernel used by XGM_SCHED_LEARNED, and per-task timing collection.
 //
@@ -54,7 +54,7 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
     maxd = l > maxd ? l : maxd;
   }
   const long long deg = d0.y - g.rowptr[r];
-  // 0-5 task shape, 6 clique depth, 7-11 variant one-hot (caller)
+  // 0-5 task shape, 6 clique depth, 7-12 variant one-hot (caller)
   f[0] = log2f(1.0f + (float)s) / 11.0f;
   f[1] = log2f(1.0f + (float)sum) / 24.0f;
   f[2] = log2f(1.0f + (float)maxd) / 11.0f;
@@ -62,7 +62,7 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   f[4] = log2f(1.0f + sumsq) / 34.0f;
   f[5] = (float)sum / ((float)s * (float)maxd + 1.0f);
   f[6] = (float)(k - 3) * 0.5f;
-  f[7] = f[8] = f[9] = f[10] = f[11] = 0.0f;
+  for (int v = 0; v < XGM_NUM_VARIANTS; ++v) f[7 + v] = 0.0f;
 }
 
 __device__ __forceinline__ float mlp_forward(const float* P, const float* f) {
@@ -121,7 +121,8 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v) {
       // edge-splitting stays the capacity fallback: splitting a task a CTA can hold
       // multiplies its set-up work and never paid off in any measured configuration
-      cand[v] = !(((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH) && s > kWarpCap) ||
+      cand[v] = !(((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH || v == XGM_VAR_BUCKET) &&
+                   s > kWarpCap) ||
                   (v == XGM_VAR_WIDE && s > kWideCap) || (v == XGM_VAR_CTA && s > kCtaCap) ||
                   (v == XGM_VAR_SPLIT && s <= kCtaCap));
       ncand += cand[v];
@@ -447,19 +448,23 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   TaskBuf& tb = ctx->tb;
   XGM_CUDA_TRY(cudaSetDevice(ctx->device));
   XGM_CUDA_TRY(taskbuf_reserve(tb, G.nv, s));
-  const int64_t need = 4 * tb.cap_v + (G.ne_dag > 0 ? G.ne_dag : 1);
+  const int64_t need = 5 * tb.cap_v + (G.ne_dag > 0 ? G.ne_dag : 1);
   if (tb.log_cap < need) {
     if (tb.log) cudaFreeAsync(tb.log, s);
     tb.log = nullptr;
     XGM_CUDA_TRY(cudaMallocAsync(&tb.log, sizeof(long long) * need, s));
     tb.log_cap = need;
   }
-  int smax = 0, wmax = kWarpCap, dmax = kWideCap, cmax = kCtaCap;
+  int bmax = 0, smax = 0, wmax = kWarpCap, dmax = kWideCap, cmax = kCtaCap;
+  if (variant == XGM_VAR_BUCKET) {
+    bmax = kWarpCap;
+    XGM_CUDA_TRY(ensure_bucket_index(G, s));
+  }
   if (variant == XGM_VAR_SEARCH) smax = kWarpCap;
   if (variant == XGM_VAR_WIDE) wmax = 0;
   if (variant == XGM_VAR_CTA) wmax = dmax = 0;
   if (variant == XGM_VAR_SPLIT) wmax = dmax = cmax = 0;
-  XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s, smax));
+  XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s, smax, bmax));
   XGM_CUDA_TRY(build_lists(G, tb, false, s));
   XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
   XGM_CUDA_TRY(launch_clique(k, G.view(), tb.lists(true), &ctx->d_sc->q, &ctx->d_sc->count,
@@ -473,16 +478,19 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
                         : variant == XGM_VAR_CTA    ? tb.cta
                         : variant == XGM_VAR_WIDE   ? tb.wide
                         : variant == XGM_VAR_SEARCH ? tb.search
+                        : variant == XGM_VAR_BUCKET ? tb.bucket
                                                     : tb.split_v;
   const int nidx = variant == XGM_VAR_WARP     ? 2
                    : variant == XGM_VAR_CTA    ? 1
                    : variant == XGM_VAR_WIDE   ? 4
                    : variant == XGM_VAR_SEARCH ? 5
+                   : variant == XGM_VAR_BUCKET ? 6
                                                : 3;
   const long long* lg = variant == XGM_VAR_WARP     ? tl.log_warp
                         : variant == XGM_VAR_CTA    ? tl.log_cta
                         : variant == XGM_VAR_WIDE   ? tl.log_wide
                         : variant == XGM_VAR_SEARCH ? tl.log_search
+                        : variant == XGM_VAR_BUCKET ? tl.log_bucket
                                                     : tl.log_split;
   k_assemble<<<grid_for(G.nv), kThreads, 0, s>>>(G.view(), k, variant, list, tb.n, nidx, lg,
                                                  tb.split_off, stride, dx, dy, max_rows,

@@ -43,7 +43,7 @@ struct StaticScalars {
   QueueHeads q;
   unsigned long long n_cta, n_warp;
   unsigned long long hub_packed;  // (hubs << 40) | sub-tasks, one atomic for both
-  int64_t n[6];                   // TaskLists sizes (no wide-warp or search list here)
+  int64_t n[8];                   // TaskLists sizes (no wide-warp, search or bucket list here)
 };
 static_assert(sizeof(StaticScalars) <= 256, "scalars fit the first 256 bytes");
 constexpr size_t kOffCtaL = 256;
@@ -87,6 +87,8 @@ __global__ void k_static_sizes(StaticScalars* sc, int64_t* off) {
   sc->n[3] = hubs;
   sc->n[4] = 0;
   sc->n[5] = 0;
+  sc->n[6] = 0;
+  sc->n[7] = 0;
   off[hubs] = sub;
 }
 

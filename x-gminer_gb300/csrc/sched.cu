@@ -26,13 +26,15 @@ inline unsigned grid_for(int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); \
        i += (int64_t)gridDim.x * blockDim.x)
 
-__global__ void k_classify_heur(const longlong2* dptr, int64_t nv, int kmin, int search_max,
-                                int warp_max, int wide_max, int cta_max, uint8_t* var) {
+__global__ void k_classify_heur(const longlong2* dptr, int64_t nv, int kmin, int bucket_max,
+                                int search_max, int warp_max, int wide_max, int cta_max,
+                                uint8_t* var) {
   GRID_STRIDE(r, nv) {
     const longlong2 d = dptr[r];
     const int64_t s = d.y - d.x;
     uint8_t v;
     if (s < kmin) v = VAR_SKIP;
+    else if (s <= bucket_max) v = VAR_BUCKET;
     else if (s <= search_max) v = VAR_SEARCH;
     else if (s <= warp_max) v = VAR_WARP;
     else if (s <= wide_max) v = VAR_WIDE;
@@ -57,8 +59,8 @@ __global__ void k_classify_table(const longlong2* dptr, int64_t nv, int kmin, xg
     uint8_t v = VAR_SKIP;
     if (s >= kmin) {
       v = tab.variant[degree_bucket(s)];
-      if (v > VAR_SEARCH) v = VAR_SPLIT;
-      if (v == VAR_SEARCH && s > kWarpCap) v = VAR_WIDE;
+      if (v > VAR_BUCKET) v = VAR_SPLIT;
+      if ((v == VAR_SEARCH || v == VAR_BUCKET) && s > kWarpCap) v = VAR_WIDE;
       if (v == VAR_WARP && s > kWarpCap) v = VAR_WIDE;
       if (v == VAR_WIDE && s > kWideCap) v = VAR_CTA;
       if (v == VAR_CTA && s > kCtaCap) v = VAR_SPLIT;
@@ -122,15 +124,16 @@ __global__ void k_bin_scan(unsigned long long* hist, int64_t* n) {
       hist[v * kBins + b] = run;
       run += c;
     }
-    // var code -> n[] slot: WARP 2, CTA 1, SPLIT 3, WIDE 4, SEARCH 5
-    n[v == VAR_WARP ? 2 : v == VAR_CTA ? 1 : v == VAR_SPLIT ? 3 : v == VAR_WIDE ? 4 : 5] =
-        (int64_t)run;
+    // var code -> n[] slot: WARP 2, CTA 1, SPLIT 3, WIDE 4, SEARCH 5, BUCKET 6
+    n[v == VAR_WARP ? 2 : v == VAR_CTA ? 1 : v == VAR_SPLIT ? 3 : v == VAR_WIDE ? 4
+      : v == VAR_SEARCH ? 5 : 6] = (int64_t)run;
   }
 }
 
 __global__ void k_bin_scatter(const uint8_t* var, const float* cost, int64_t nv,
                               unsigned long long* cursor, int32_t* warp_l, int32_t* cta_l,
-                              int32_t* hub_l, int32_t* wide_l, int32_t* search_l) {
+                              int32_t* hub_l, int32_t* wide_l, int32_t* search_l,
+                              int32_t* bucket_l) {
   GRID_STRIDE(r, nv) {
     const uint8_t v = var[r];
     if (v < kNumVar) {
@@ -139,7 +142,8 @@ __global__ void k_bin_scatter(const uint8_t* var, const float* cost, int64_t nv,
                      : v == VAR_CTA   ? cta_l
                      : v == VAR_SPLIT ? hub_l
                      : v == VAR_WIDE  ? wide_l
-                                      : search_l;
+                     : v == VAR_SEARCH ? search_l
+                                      : bucket_l;
       out[p] = (int32_t)r;
     }
   }
@@ -174,6 +178,7 @@ TaskLists TaskBuf::lists(bool with_log) const {
   t.warp = warp;
   t.wide = wide;
   t.search = search;
+  t.bucket = bucket;
   t.split_v = split_v;
   t.split_off = split_off;
   t.n = n;
@@ -182,7 +187,8 @@ TaskLists TaskBuf::lists(bool with_log) const {
     t.log_warp = log + cap_v;
     t.log_wide = log + 2 * cap_v;
     t.log_search = log + 3 * cap_v;
-    t.log_split = log + 4 * cap_v;
+    t.log_bucket = log + 4 * cap_v;
+    t.log_split = log + 5 * cap_v;
   }
   return t;
 }
@@ -195,6 +201,7 @@ cudaError_t taskbuf_reserve(TaskBuf& tb, int64_t nv, cudaStream_t s) {
   TRY(dalloc(&tb.warp, c, s));
   TRY(dalloc(&tb.wide, c, s));
   TRY(dalloc(&tb.search, c, s));
+  TRY(dalloc(&tb.bucket, c, s));
   TRY(dalloc(&tb.split_v, c, s));
   TRY(dalloc(&tb.split_off, c + 1, s));
   TRY(dalloc(&tb.n, 8, s));
@@ -209,7 +216,7 @@ cudaError_t taskbuf_reserve(TaskBuf& tb, int64_t nv, cudaStream_t s) {
 }
 
 void taskbuf_free(TaskBuf& tb, cudaStream_t s) {
-  void* ps[] = {tb.cta, tb.warp, tb.wide, tb.search, tb.split_v, tb.split_off, tb.n, tb.var,
+  void* ps[] = {tb.cta, tb.warp, tb.wide, tb.search, tb.bucket, tb.split_v, tb.split_off, tb.n, tb.var,
                 tb.flag, tb.pos, tb.w, tb.cost, tb.tmp, tb.log};
   for (void* p : ps)
     if (p) cudaFreeAsync(p, s);
@@ -217,15 +224,16 @@ void taskbuf_free(TaskBuf& tb, cudaStream_t s) {
 }
 
 cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int wide_max, int cta_max,
-                               TaskBuf& tb, cudaStream_t s, int search_max) {
+                               TaskBuf& tb, cudaStream_t s, int search_max, int bucket_max) {
   if (search_max > kWarpCap) search_max = kWarpCap;
+  if (bucket_max > kWarpCap) bucket_max = kWarpCap;
   if (warp_max > kWarpCap) warp_max = kWarpCap;
   if (wide_max > kWideCap) wide_max = kWideCap;
   if (k < 2) k = 2;
   if (cta_max > kCtaCap) cta_max = kCtaCap;
   if (g.nv == 0) return cudaSuccess;
-  k_classify_heur<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, k - 1, search_max, warp_max,
-                                                      wide_max, cta_max, tb.var);
+  k_classify_heur<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, k - 1, bucket_max, search_max,
+                                                      warp_max, wide_max, cta_max, tb.var);
   return cudaGetLastError();
 }
 
@@ -238,14 +246,14 @@ cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& ta
 
 cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s) {
   const int64_t nv = g.nv;
-  TRY(cudaMemsetAsync(tb.n, 0, 6 * sizeof(int64_t), s));
+  TRY(cudaMemsetAsync(tb.n, 0, 8 * sizeof(int64_t), s));
   if (nv == 0) return cudaMemsetAsync(tb.split_off, 0, sizeof(int64_t), s);
   if (!order) {
     // the hub pass goes last: its positions are reused for the hub offsets below
-    const uint8_t codes[5] = {VAR_CTA, VAR_WARP, VAR_WIDE, VAR_SEARCH, VAR_SPLIT};
-    int32_t* outs[5] = {tb.cta, tb.warp, tb.wide, tb.search, tb.split_v};
-    int64_t* cnts[5] = {tb.n + 1, tb.n + 2, tb.n + 4, tb.n + 5, tb.n + 3};
-    for (int x = 0; x < 5; ++x) {
+    const uint8_t codes[6] = {VAR_CTA, VAR_WARP, VAR_WIDE, VAR_SEARCH, VAR_BUCKET, VAR_SPLIT};
+    int32_t* outs[6] = {tb.cta, tb.warp, tb.wide, tb.search, tb.bucket, tb.split_v};
+    int64_t* cnts[6] = {tb.n + 1, tb.n + 2, tb.n + 4, tb.n + 5, tb.n + 6, tb.n + 3};
+    for (int x = 0; x < 6; ++x) {
       k_flag_eq<<<grid_for(nv), kThreads, 0, s>>>(tb.var, nv, codes[x], tb.flag);
       TRY(scan_excl(tb.flag, tb.pos, nv, cnts[x], s));
       k_scatter<<<grid_for(nv), kThreads, 0, s>>>(tb.flag, tb.pos, nv, outs[x]);
@@ -261,7 +269,7 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
     k_bin_hist<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.cost, nv, hist);
     k_bin_scan<<<1, 32, 0, s>>>(hist, tb.n);
     k_bin_scatter<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.cost, nv, hist, tb.warp, tb.cta,
-                                                    tb.split_v, tb.wide, tb.search);
+                                                    tb.split_v, tb.wide, tb.search, tb.bucket);
     cudaFreeAsync(hist, s);
     // hub offsets follow the ordered hub list (at most nv hubs; the unused tail of w
     // is zero so the scan total is the number of hub sub-tasks)

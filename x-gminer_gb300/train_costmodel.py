@@ -3,7 +3,7 @@
 Training data: per-task clock64 timings the engine logs (xgm_model_collect) for the
 4-clique, 5-clique and diamond plans (the diamond plan runs the triangle-participation
 kernel, whose tasks are the k = 3 tasks) on R-MAT graphs of scales 18-22, edge factor
-16, seeds 10-14, under every kernel variant.  The network (12 -> 32 -> 1, fp16
+16, seeds 10-14, under every kernel variant.  The network (13 -> 32 -> 1, fp16
 weights) is trained by the engine's own forward/backward/Adam kernels.  Evaluation: a
 held-out R-MAT scale 23 (seed 99) graph, learned vs plain degree-threshold schedule,
 same counts.
@@ -38,7 +38,7 @@ def timed_count(ctx, g, pat, reps, **kw):
         cnt, st = ctx.count(g, pat, with_stats=True, **kw)
         t = st["prep_ms"] + st["kernel_ms"]
         best = t if best is None else min(best, t)
-    return cnt, best
+    return cnt, best, st["variant_tasks"]
 
 
 def main():
@@ -59,7 +59,8 @@ def main():
         g = ctx.graph_from_edges(nv, s, d)
         del s, d
         for pat in PATTERNS:
-            for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_WIDE, xgm.VAR_CTA, xgm.VAR_SPLIT):
+            for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_BUCKET, xgm.VAR_WIDE, xgm.VAR_CTA,
+                        xgm.VAR_SPLIT):
                 X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
                 if len(y) > args.rows:  # uniform subsample
                     idx = np.random.default_rng(scale * 7 + var).choice(len(y), args.rows,
@@ -76,7 +77,7 @@ def main():
     vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=6)
     g = ctx.graph_from_edges(int(vo[-1]), s, d)
     for pat in ["triangle", "4-clique", "diamond"]:
-        for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_WIDE, xgm.VAR_CTA):
+        for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_BUCKET, xgm.VAR_WIDE, xgm.VAR_CTA):
             X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
             if len(y) > args.rows:
                 idx = np.random.default_rng(17 + var).choice(len(y), args.rows, replace=False)
@@ -99,13 +100,14 @@ def main():
     del s, d
     evals = {}
     for pat in ["4-clique", "5-clique", "diamond", "triangle"]:
-        c_h, t_h = timed_count(ctx, g, pat, 3)
-        res = {"count": c_h, "heuristic_ms": t_h}
+        c_h, t_h, v_h = timed_count(ctx, g, pat, 3)
+        res = {"count": c_h, "heuristic_ms": t_h, "heuristic_variants": v_h}
         for order in (1, 0):
-            c_l, t_l = timed_count(ctx, g, pat, 3, policy=xgm.SCHED_LEARNED, model=model,
-                                   order_by_cost=order)
+            c_l, t_l, v_l = timed_count(ctx, g, pat, 3, policy=xgm.SCHED_LEARNED, model=model,
+                                        order_by_cost=order)
             assert c_h == c_l, (pat, c_h, c_l)
             res[f"learned_ms_order{order}"] = t_l
+            res["learned_variants"] = v_l
         best = min(res["learned_ms_order1"], res["learned_ms_order0"])
         res["speedup"] = t_h / best
         evals[pat] = res
