@@ -301,14 +301,14 @@ xgm_status xgm_count_batched(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const* 
 void xgm_batch_destroy(xgm_batch* b);
 
 /* -------------------------------------------------------------- cost model */
-/* Learned scheduler: a 13 -> 32 (ReLU) -> 1 MLP with fp16 weights and fp32
+/* Learned scheduler: a 12 -> 32 (ReLU) -> 1 MLP with fp16 weights and fp32
  * accumulation that predicts log2(warp-cycles) of a task under a kernel variant.  It is
  * trained by the engine's own forward/backward kernels on per-task timings the engine
  * logs (xgm_model_collect), and used by XGM_SCHED_LEARNED to pick each task's variant
  * and to order the queues heaviest-first.  It changes the schedule only, never a count.
  * No counterpart in the reference (its schedule is the fixed heuristic of
  * xgminer/include/glumin/common.h:114-116). */
-#define XGM_MODEL_FEATURES 13
+#define XGM_MODEL_FEATURES 12
 #define XGM_MODEL_HIDDEN 32
 #define XGM_MODEL_PARAMS (XGM_MODEL_HIDDEN * XGM_MODEL_FEATURES + 2 * XGM_MODEL_HIDDEN + 1)
 

@@ -1,6 +1,6 @@
 """Numpy restatement of the engine's cost model (test infrastructure only).
 
-The model is 13 -> 32 (ReLU) -> 1 with parameters W1[32][13], b1[32], w2[32], b2 stored
+The model is 12 -> 32 (ReLU) -> 1 with parameters W1[32][12], b1[32], w2[32], b2 stored
 flat in that order, fp16 weights and fp32 arithmetic; the loss is the mean squared
 error.  The tests compare the engine's hand-written forward / backward kernels with
 these functions.  The model has no counterpart in the reference.
@@ -9,7 +9,7 @@ from __future__ import annotations
 
 import numpy as np
 
-F, H = 13, 32
+F, H = 12, 32
 NPARAM = H * F + 2 * H + 1
 
 

@@ -47,7 +47,7 @@ def test_collect_and_learned_schedule_counts(xgm, ctx):
         X, y, cnt = m.collect(g, "4-clique", var, stride=2, max_rows=50000)
         assert cnt == ctx.count(g, "4-clique")
         assert len(y) > 0 and np.all(np.isfinite(X)) and np.all(np.isfinite(y))
-        assert np.all(X[:, 7 + var] == 1.0)
+        assert np.all(X[:, 6 + var] == 1.0)  # one-hot after 5 shape features + depth
         Xs.append(X)
         ys.append(y)
     m.train(np.concatenate(Xs), np.concatenate(ys), epochs=10)

@@ -133,6 +133,17 @@ def test_dense_hub_split_tasks(xgm, ctx):
     assert ctx.count(g, "rectangle") == want["cycle4"]
 
 
+def test_cycle4_grouped_dense_tasks(xgm, ctx, orc):
+    # R-MAT scale 19: hub tasks with many wedges relative to their id range run in
+    # L2-resident counter groups (more than one group here); the rest in the persistent
+    # kernel.  Both paths add to the same exact count.
+    nv, s, d = xgm.gen_rmat(19, 16, seed=2)
+    rowptr, col = orc.build_csr(nv, s, d)
+    g = ctx.graph_from_csr(rowptr, col)
+    assert ctx.count(g, "rectangle") == orc.count("cycle4", rowptr, col)
+    g.close()
+
+
 def test_edge_cases(xgm, ctx, orc):
     # no edges at all
     g = ctx.graph_from_edges(10, np.zeros(0, np.int32), np.zeros(0, np.int32))

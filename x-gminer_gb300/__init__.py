@@ -50,7 +50,7 @@ TUNE_BUCKETS = 16
 VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH, VAR_BUCKET = 0, 1, 2, 3, 4, 5
 NUM_VARIANTS = 6
 
-MODEL_FEATURES, MODEL_HIDDEN = 13, 32
+MODEL_FEATURES, MODEL_HIDDEN = 12, 32
 MODEL_PARAMS = MODEL_HIDDEN * MODEL_FEATURES + 2 * MODEL_HIDDEN + 1
 
 
@@ -481,7 +481,7 @@ class Batch:
 
 
 class Model:
-    """Learned cost model (13 -> 32 -> 1 MLP, fp16 weights) trained on the GPU."""
+    """Learned cost model (12 -> 32 -> 1 MLP, fp16 weights) trained on the GPU."""
 
     def __init__(self, ctx: Context, seed: int = 1):
         self.ctx = ctx

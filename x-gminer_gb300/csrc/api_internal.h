@@ -48,6 +48,18 @@ struct xgm_ctx {
   int32_t* c4_small = nullptr;
   int64_t* c4_n = nullptr;
   int64_t c4_vcap = 0;
+  // grouped dense 4-cycle tasks (motif.cu): counters (kept zeroed), task info,
+  // segment arrays and the groups' task tables
+  uint32_t* c4_counters = nullptr;
+  int64_t* c4_info = nullptr;
+  int64_t c4_info_cap = 0;
+  int64_t* c4_seg_base = nullptr;
+  int64_t* c4_seg_pre = nullptr;
+  int32_t* c4_seg_cnt = nullptr;
+  int64_t c4_seg_cap = 0;
+  int32_t* c4_tv0 = nullptr;
+  int64_t* c4_ttab = nullptr;  // per group: tseg[m+1] then tcnt[m]
+  int64_t c4_task_cap = 0;
   int clique_grid = 0;
 };
 

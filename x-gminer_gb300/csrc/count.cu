@@ -1,4 +1,5 @@
 // Count dispatch behind xgm_count: schedule -> persistent counting launch -> uint64.
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -145,10 +146,118 @@ xgm_status ensure_c4(xgm_ctx* ctx, const DevGraph& g) {
 
 }  // namespace
 
+namespace {
+
+// Large 4-cycle tasks whose wedges are at least a quarter of their id range (v2 < v0)
+// and numerous are counted a group at a time with L2-resident counters
+// (launch_c4_dense_walk); the others stay in the persistent kernel's list.  Reads the
+// large list back, rewrites it without the dense tasks, and launches the groups.
+constexpr int64_t kC4DenseMinWedges = int64_t(1) << 16;
+
+xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
+  cudaStream_t s = ctx->stream;
+  int64_t nls[2] = {0, 0};
+  XGM_CUDA_TRY(cudaMemcpyAsync(nls, ctx->c4_n, sizeof(nls), cudaMemcpyDeviceToHost, s));
+  XGM_CUDA_TRY(cudaStreamSynchronize(s));
+  const int64_t nl = nls[0];
+  if (nl == 0) return XGM_OK;
+  XGM_CUDA_TRY(grow(&ctx->c4_info, &ctx->c4_info_cap, 2 * nl, s));
+  XGM_CUDA_TRY(launch_c4_task_info(g.view(), ctx->c4_large, nl, ctx->wedges, ctx->c4_info, s));
+  std::vector<int32_t> list(nl);
+  std::vector<int64_t> info(2 * nl);
+  XGM_CUDA_TRY(cudaMemcpyAsync(list.data(), ctx->c4_large, sizeof(int32_t) * nl,
+                               cudaMemcpyDeviceToHost, s));
+  XGM_CUDA_TRY(cudaMemcpyAsync(info.data(), ctx->c4_info, sizeof(int64_t) * 2 * nl,
+                               cudaMemcpyDeviceToHost, s));
+  XGM_CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<int32_t> sparse, dense;
+  for (int64_t t = 0; t < nl; ++t) {
+    const int64_t w = info[2 * t], v0 = list[t];
+    if (w >= kC4DenseMinWedges && 4 * w >= v0 && v0 <= kC4GroupCounters) dense.push_back((int32_t)t);
+    else sparse.push_back(list[t]);
+  }
+  if (dense.empty()) return XGM_OK;
+  std::sort(dense.begin(), dense.end(), [&](int32_t a, int32_t b) { return list[a] > list[b]; });
+  // groups: consecutive dense tasks whose ranges fit the counter array
+  std::vector<int32_t> tv0;
+  std::vector<int64_t> ttab;
+  struct Group { int64_t t0, m, tab, nseg, ncnt; };
+  std::vector<Group> groups;
+  int64_t max_seg = 0;
+  for (size_t i = 0; i < dense.size();) {
+    Group gr{(int64_t)tv0.size(), 0, (int64_t)ttab.size(), 0, 0};
+    std::vector<int64_t> tseg{0}, tcnt;
+    while (i < dense.size() && (gr.m == 0 || gr.ncnt + list[dense[i]] <= kC4GroupCounters)) {
+      const int32_t t = dense[i++];
+      tv0.push_back(list[t]);
+      tcnt.push_back(gr.ncnt);
+      gr.ncnt += list[t];
+      tseg.push_back(tseg.back() + info[2 * t + 1]);
+      ++gr.m;
+    }
+    gr.nseg = tseg.back();
+    max_seg = std::max(max_seg, gr.nseg);
+    ttab.insert(ttab.end(), tseg.begin(), tseg.end());
+    ttab.insert(ttab.end(), tcnt.begin(), tcnt.end());
+    groups.push_back(gr);
+  }
+  if (!ctx->c4_counters) {
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_counters, sizeof(uint32_t) * kC4GroupCounters, s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_counters, 0, sizeof(uint32_t) * kC4GroupCounters, s));
+  }
+  if (ctx->c4_seg_cap < max_seg) {
+    void* ps[] = {ctx->c4_seg_base, ctx->c4_seg_pre, ctx->c4_seg_cnt};
+    for (void* p : ps)
+      if (p) cudaFreeAsync(p, s);
+    ctx->c4_seg_cap = 0;
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_base, sizeof(int64_t) * max_seg, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_pre, sizeof(int64_t) * (max_seg + 1), s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_cnt, sizeof(int32_t) * max_seg, s));
+    ctx->c4_seg_cap = max_seg;
+  }
+  const int64_t need = std::max<int64_t>((int64_t)tv0.size(), (int64_t)ttab.size());
+  if (ctx->c4_task_cap < need) {
+    if (ctx->c4_tv0) cudaFreeAsync(ctx->c4_tv0, s);
+    if (ctx->c4_ttab) cudaFreeAsync(ctx->c4_ttab, s);
+    ctx->c4_task_cap = 0;
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_tv0, sizeof(int32_t) * need, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_ttab, sizeof(int64_t) * need, s));
+    ctx->c4_task_cap = need;
+  }
+  // the sparse large tasks stay with the persistent kernel; all tables go up at once
+  const int64_t ns = (int64_t)sparse.size();
+  if (ns) XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_large, sparse.data(), sizeof(int32_t) * ns,
+                                      cudaMemcpyHostToDevice, s));
+  XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_n, &ns, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_tv0, tv0.data(), sizeof(int32_t) * tv0.size(),
+                               cudaMemcpyHostToDevice, s));
+  XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_ttab, ttab.data(), sizeof(int64_t) * ttab.size(),
+                               cudaMemcpyHostToDevice, s));
+  XGM_CUDA_TRY(cudaStreamSynchronize(s));  // host tables are freed on return
+  const GView view = g.view();
+  const int grid = 4 * ctx->num_sms;
+  for (const Group& gr : groups) {
+    const int64_t* tseg = ctx->c4_ttab + gr.tab;
+    const int64_t* tcnt = tseg + gr.m + 1;
+    XGM_CUDA_TRY(launch_c4_segments(view, ctx->c4_tv0 + gr.t0, tseg, tcnt, (int)gr.m, gr.nseg,
+                                    ctx->c4_seg_base, ctx->c4_seg_pre, ctx->c4_seg_cnt, s));
+    XGM_CUDA_TRY(scan_excl(ctx->c4_seg_pre, ctx->c4_seg_pre, gr.nseg, ctx->c4_seg_pre + gr.nseg, s));
+    XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre, ctx->c4_seg_base, ctx->c4_seg_cnt,
+                                      gr.nseg, ctx->c4_counters, &ctx->d_sc->count, grid, s));
+    XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_counters, 0, sizeof(uint32_t) * gr.ncnt, s));
+    *launches += 3;
+  }
+  return XGM_OK;
+}
+
+}  // namespace
+
 void motif_buffers_free(xgm_ctx* ctx) {
   cudaStream_t s = ctx->stream;
   void* ps[] = {ctx->vpart, ctx->epart, ctx->c4_scratch, ctx->wedges, ctx->c4_flag_large,
-                ctx->c4_flag_small, ctx->c4_pos, ctx->c4_large, ctx->c4_small, ctx->c4_n};
+                ctx->c4_flag_small, ctx->c4_pos, ctx->c4_large, ctx->c4_small, ctx->c4_n,
+                ctx->c4_counters, ctx->c4_info, ctx->c4_seg_base, ctx->c4_seg_pre,
+                ctx->c4_seg_cnt, ctx->c4_tv0, ctx->c4_ttab};
   for (void* p : ps)
     if (p) cudaFreeAsync(p, s);
 }
@@ -197,10 +306,12 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
     XGM_CUDA_TRY(scan_excl(ctx->c4_flag_small, ctx->c4_pos, g.nv, ctx->c4_n + 1, s));
     XGM_CUDA_TRY(launch_scatter_flags(ctx->c4_flag_small, ctx->c4_pos, g.nv, ctx->c4_small, s));
     XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+    launches = 1;
+    r = cycle4_dense_groups(ctx, g, &launches);
+    if (r != XGM_OK) return r;
     XGM_CUDA_TRY(launch_cycle4(view, ctx->c4_large, ctx->c4_small, ctx->c4_n, ctx->d_sc->c4heads,
                                ctx->c4_scratch, &ctx->d_sc->count, &ctx->d_sc->err,
                                cycle4_grid(ctx->num_sms), s));
-    launches = 1;
   } else {
     set_thread_error("unknown pattern");
     return XGM_ERR_INVALID;

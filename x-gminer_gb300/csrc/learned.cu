@@ -1,4 +1,4 @@
-// Learned scheduler: task features, a 13 -> 32 -> 1 MLP (fp16 weights, fp32
+// Learned scheduler: task features, a 12 -> 32 -> 1 MLP (fp16 weights, fp32
 // accumulation) with hand-written forward / backward / Adam kernels, the fused
 // classify kernel used by XGM_SCHED_LEARNED, and per-task timing collection.
 //
@@ -43,26 +43,22 @@ __host__ __device__ inline float variant_warps(int v) {
 __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   const longlong2 d0 = g.dptr[r];
   const long long s = d0.y - d0.x;
-  // fp32 / integer sums (the GPU's fp64 rate is a small fraction of its fp32 rate)
   long long sum = 0, maxd = 0;
-  float sumsq = 0.0f;
   for (long long e = d0.x; e < d0.y; ++e) {
     const longlong2 d = g.dptr[g.col[e]];
     const long long l = d.y - d.x;
     sum += l;
-    sumsq = fmaf((float)l, (float)l, sumsq);
     maxd = l > maxd ? l : maxd;
   }
   const long long deg = d0.y - g.rowptr[r];
-  // 0-5 task shape, 6 clique depth, 7-12 variant one-hot (caller)
+  // 0-4 task shape, 5 clique depth, 6-11 variant one-hot (caller)
   f[0] = log2f(1.0f + (float)s) / 11.0f;
   f[1] = log2f(1.0f + (float)sum) / 24.0f;
   f[2] = log2f(1.0f + (float)maxd) / 11.0f;
   f[3] = log2f(1.0f + (float)deg) / 18.0f;
-  f[4] = log2f(1.0f + sumsq) / 34.0f;
-  f[5] = (float)sum / ((float)s * (float)maxd + 1.0f);
-  f[6] = (float)(k - 3) * 0.5f;
-  for (int v = 0; v < XGM_NUM_VARIANTS; ++v) f[7 + v] = 0.0f;
+  f[4] = (float)sum / ((float)s * (float)maxd + 1.0f);
+  f[5] = (float)(k - 3) * 0.5f;
+  for (int v = 0; v < XGM_NUM_VARIANTS; ++v) f[kShapeFeat + v] = 0.0f;
 }
 
 __device__ __forceinline__ float mlp_forward(const float* P, const float* f) {
@@ -82,8 +78,8 @@ __device__ __forceinline__ void load_params(const __half* wh, float* P) {
   __syncthreads();
 }
 
-// The model over the five variants of one task: the first layer's task-shape part
-// (features 0-6) is shared, each variant adds its one-hot column.
+// The model over the variants of one task: the first layer's task-shape part
+// (features 0-5) is shared, each variant adds its one-hot column.
 __device__ __forceinline__ void mlp_variants(const float* P, const float* f, const bool* cand,
                                              float* pred) {
 #pragma unroll
@@ -92,11 +88,11 @@ __device__ __forceinline__ void mlp_variants(const float* P, const float* f, con
   for (int h = 0; h < kHidden; ++h) {
     float a = P[kOffB1 + h];
 #pragma unroll
-    for (int j = 0; j < 7; ++j) a = fmaf(P[h * kFeat + j], f[j], a);
+    for (int j = 0; j < kShapeFeat; ++j) a = fmaf(P[h * kFeat + j], f[j], a);
     const float w2 = P[kOffW2 + h];
 #pragma unroll
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
-      if (cand[v]) pred[v] = fmaf(w2, fmaxf(a + P[h * kFeat + 7 + v], 0.0f), pred[v]);
+      if (cand[v]) pred[v] = fmaf(w2, fmaxf(a + P[h * kFeat + kShapeFeat + v], 0.0f), pred[v]);
   }
 }
 
@@ -243,7 +239,7 @@ __global__ void k_assemble(GView g, int k, int variant, const int32_t* list, con
     if ((int64_t)o >= max_rows) continue;
     float* f = X + o * kFeat;
     task_features(g, r, k, f);
-    f[7 + variant] = 1.0f;
+    f[kShapeFeat + variant] = 1.0f;
     Y[o] = log2f((float)fmax(cyc, 1.0) * variant_warps(variant));
   }
 }

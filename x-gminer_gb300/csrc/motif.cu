@@ -317,6 +317,85 @@ __global__ void __launch_bounds__(kC4Threads) k_cycle4(GView g, const int32_t* l
   if ((tid & 31) == 0 && acc && out) atomicAdd(out, acc);
 }
 
+// ---------------------------------------------- 4-cycle, grouped dense tasks
+// Tasks with many wedges relative to their id range (v2 < v0) are counted a group at a
+// time by the whole GPU: each task of the group owns v0 counters of one L2-resident
+// array (the group's ranges add up to at most kC4GroupCounters), every wedge adds one
+// to counter v2 of its task, and the count grows by the counter's old value (the k-th
+// wedge into a group closes k-1 new cycles, so the sum of old values is C(c, 2) per
+// group) — one pass, no read-back; the host clears the array between groups.
+// Segments: one per (task, lower neighbour v1), the part of N(v1) below v0.
+__global__ void k_c4_segments(GView g, const int32_t* tv0, const int64_t* tseg,
+                              const int64_t* tcnt, int m, int64_t nseg, int64_t* seg_base,
+                              int64_t* seg_len, int32_t* seg_cnt) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nseg;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = m;  // task t with tseg[t] <= e < tseg[t+1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (tseg[mid] <= e) lo = mid; else hi = mid;
+    }
+    const int32_t v0 = tv0[lo];
+    const int32_t v1 = ldg_i32(g.col + g.rowptr[v0] + (e - tseg[lo]));
+    const long long b = g.rowptr[v1];
+    seg_base[e] = b;
+    seg_len[e] = lower_end(g, v1, v0) - b;
+    seg_cnt[e] = (int32_t)tcnt[lo];
+  }
+}
+
+__global__ void k_c4_task_info(GView g, const int32_t* list, int64_t n, const long long* wedges,
+                               int64_t* info) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = list[t];
+    info[2 * t] = wedges[r];
+    info[2 * t + 1] = g.dptr[r].x - g.rowptr[r];
+  }
+}
+
+constexpr int kC4TileIters = 16;  // a warp walks 32 x 16 consecutive wedges per tile
+
+__global__ void __launch_bounds__(kThreads) k_c4_dense_walk(const int32_t* col,
+                                                            const int64_t* seg_pre,
+                                                            const int64_t* seg_base,
+                                                            const int32_t* seg_cnt, int64_t nseg,
+                                                            uint32_t* counters,
+                                                            unsigned long long* out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = seg_pre[nseg];
+  const int64_t tile = 32 * kC4TileIters;
+  const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+  unsigned long long acc = 0;
+  for (int64_t t0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * tile; t0 < total;
+       t0 += nwarps * tile) {
+    // segment of the tile's first wedge (lane 0 searches, the warp shares it)
+    int64_t e = 0;
+    if (lane == 0) {
+      int64_t lo = 0, hi = nseg;  // largest e with seg_pre[e] <= t0
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (seg_pre[mid] <= t0) lo = mid; else hi = mid;
+      }
+      e = lo;
+    }
+    e = __shfl_sync(kFull, e, 0);
+    int64_t seg_end = seg_pre[e + 1];
+    for (int j = 0; j < kC4TileIters; ++j) {
+      const int64_t k = t0 + j * 32 + lane;
+      if (k >= total) break;
+      while (k >= seg_end) {
+        ++e;
+        seg_end = seg_pre[e + 1];
+      }
+      const int32_t v2 = ldg_i32(col + seg_base[e] + (k - seg_pre[e]));
+      acc += atomicAdd(&counters[(int64_t)seg_cnt[e] + v2], 1u);
+    }
+  }
+  acc = warp_sum_u64(acc);
+  if (lane == 0 && acc) atomicAdd(out, acc);
+}
+
 // Per-graph diamond / tailed-triangle totals from the participation counters: block
 // of consecutive rank ids (graphs are contiguous in rank order), shared-memory
 // aggregation by graph id, then one atomic per (block, graph).
@@ -403,6 +482,31 @@ cudaError_t launch_cycle4(const GView& g, const int32_t* large, const int32_t* s
                           unsigned long long* out, uint32_t* err, int grid, cudaStream_t s,
                           const GOut& o) {
   k_cycle4<<<grid, kC4Threads, 0, s>>>(g, large, small, n, heads, scratch, out, err, o);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c4_segments(const GView& g, const int32_t* tv0, const int64_t* tseg,
+                               const int64_t* tcnt, int m, int64_t nseg, int64_t* seg_base,
+                               int64_t* seg_len, int32_t* seg_cnt, cudaStream_t s) {
+  if (nseg == 0) return cudaSuccess;
+  k_c4_segments<<<grid_for(nseg), kThreads, 0, s>>>(g, tv0, tseg, tcnt, m, nseg, seg_base,
+                                                    seg_len, seg_cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c4_task_info(const GView& g, const int32_t* list, int64_t n,
+                                const long long* wedges, int64_t* info, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_c4_task_info<<<grid_for(n), kThreads, 0, s>>>(g, list, n, wedges, info);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c4_dense_walk(const int32_t* col, const int64_t* seg_pre,
+                                 const int64_t* seg_base, const int32_t* seg_cnt, int64_t nseg,
+                                 uint32_t* counters, unsigned long long* out, int grid,
+                                 cudaStream_t s) {
+  if (nseg == 0) return cudaSuccess;
+  k_c4_dense_walk<<<grid, kThreads, 0, s>>>(col, seg_pre, seg_base, seg_cnt, nseg, counters, out);
   return cudaGetLastError();
 }
 

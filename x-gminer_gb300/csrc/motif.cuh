@@ -30,6 +30,21 @@ cudaError_t launch_cycle4(const GView& g, const int32_t* large, const int32_t* s
                           const int64_t* n, unsigned long long* heads, uint32_t* scratch,
                           unsigned long long* out, uint32_t* err, int grid, cudaStream_t s,
                           const GOut& o = GOut{});
+// 4-cycle tasks counted a group at a time (see motif.cu): segments of the group's tasks
+// (tv0[m] task roots, tseg[m+1] prefix of their lower degrees, tcnt[m] counter offsets),
+// then the walk over the scanned segment lengths (seg_pre[nseg+1]).
+constexpr int64_t kC4GroupCounters = int64_t(16) << 20;  // 64 MB of counters per group
+cudaError_t launch_c4_segments(const GView& g, const int32_t* tv0, const int64_t* tseg,
+                               const int64_t* tcnt, int m, int64_t nseg, int64_t* seg_base,
+                               int64_t* seg_len, int32_t* seg_cnt, cudaStream_t s);
+cudaError_t launch_c4_dense_walk(const int32_t* col, const int64_t* seg_pre,
+                                 const int64_t* seg_base, const int32_t* seg_cnt, int64_t nseg,
+                                 uint32_t* counters, unsigned long long* out, int grid,
+                                 cudaStream_t s);
+// wedges and lower degree of each listed task: info[2t] = wedges, info[2t+1] = lower degree
+cudaError_t launch_c4_task_info(const GView& g, const int32_t* list, int64_t n,
+                                const long long* wedges, int64_t* info, cudaStream_t s);
+
 // Batched graphs: per-graph diamond (slot_d) and tailed-triangle (slot_t) totals from the
 // participation counters; a slot < 0 is skipped.
 cudaError_t launch_part_reduce_graphs(const GView& g, const int32_t* gid,

@@ -3,7 +3,7 @@
 Training data: per-task clock64 timings the engine logs (xgm_model_collect) for the
 4-clique, 5-clique and diamond plans (the diamond plan runs the triangle-participation
 kernel, whose tasks are the k = 3 tasks) on R-MAT graphs of scales 18-22, edge factor
-16, seeds 10-14, under every kernel variant.  The network (13 -> 32 -> 1, fp16
+16, seeds 10-14, under every kernel variant.  The network (12 -> 32 -> 1, fp16
 weights) is trained by the engine's own forward/backward/Adam kernels.  Evaluation: a
 held-out R-MAT scale 23 (seed 99) graph, learned vs plain degree-threshold schedule,
 same counts.
