@@ -168,8 +168,9 @@ def load_model(xgm, ctx):
         return None, 1
     with open(COSTMODEL) as f:
         spec = json.load(f)
-    if spec.get("features") != xgm.MODEL_FEATURES or len(spec["params"]) != xgm.MODEL_PARAMS:
-        return None, 1
+    if (spec.get("features") != xgm.MODEL_FEATURES or spec.get("variants") != xgm.NUM_VARIANTS
+            or len(spec["params"]) != xgm.MODEL_PARAMS):
+        return None, 1  # trained for another feature layout: fall back to the heuristic
     import numpy as np
 
     m = xgm.Model(ctx)

@@ -186,7 +186,9 @@ typedef enum {
   XGM_VAR_BUCKET = 5, /* as SEARCH, behind X-GMiner's bucket-bitmap pre-filter: 16 buckets
                          per out-list, only common buckets searched
                          (xgminer/include/xgminer_bitmap.cuh:161-278, 661-813) */
-  XGM_NUM_VARIANTS = 6
+  XGM_VAR_GROUP = 6,  /* eight lanes per task, four tasks per warp (out-degree <= 8), rows
+                         by binary search */
+  XGM_NUM_VARIANTS = 7
 } xgm_variant;
 
 /* Autotuned schedule: the variant for each out-degree bucket.  Bucket b holds
@@ -209,6 +211,7 @@ typedef struct {
   int wide_max;           /* heuristic: out-degree <= wide_max -> WIDE (0: default 128; -1: none) */
   int search_max;         /* heuristic: out-degree <= search_max -> SEARCH (0: none) */
   int bucket_max;         /* heuristic: out-degree <= bucket_max -> BUCKET (0: none) */
+  int group_max;          /* heuristic: out-degree <= group_max -> GROUP (0: none; <= 8) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };

@@ -53,8 +53,7 @@ def test_clique67_every_variant(xgm, ctx, orc):
     g = ctx.graph_from_csr(rowptr, col)
     for k in (6, 7):
         want = orc.count(f"clique{k}", drow, dcol)
-        for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_BUCKET, xgm.VAR_WIDE, xgm.VAR_CTA,
-                    xgm.VAR_SPLIT):
+        for var in xgm.ALL_VARIANTS:
             assert ctx.count(g, f"{k}-clique", policy=xgm.SCHED_FIXED, variant=var) == want, \
                 (k, var)
     g.close()

@@ -42,12 +42,11 @@ def test_collect_and_learned_schedule_counts(xgm, ctx):
     g = ctx.graph_from_edges(nv, s, d)
     m = xgm.Model(ctx, seed=4)
     Xs, ys = [], []
-    for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE, xgm.VAR_SEARCH,
-                xgm.VAR_BUCKET):
+    for var in xgm.ALL_VARIANTS:
         X, y, cnt = m.collect(g, "4-clique", var, stride=2, max_rows=50000)
         assert cnt == ctx.count(g, "4-clique")
         assert len(y) > 0 and np.all(np.isfinite(X)) and np.all(np.isfinite(y))
-        assert np.all(X[:, 6 + var] == 1.0)  # one-hot after 5 shape features + depth
+        assert np.all(X[:, 5 + var] == 1.0)  # one-hot after 4 shape features + depth
         Xs.append(X)
         ys.append(y)
     m.train(np.concatenate(Xs), np.concatenate(ys), epochs=10)

@@ -61,8 +61,7 @@ def test_census_schedules_agree(xgm, ctx, golden):
     case = next(c for c in golden if c["name"] == "rmat_s14_ef16")
     nv, s, d = golden_samples(xgm, case)
     g = ctx.graph_from_edges(nv, s, d)
-    for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_BUCKET, xgm.VAR_WIDE, xgm.VAR_CTA,
-                xgm.VAR_SPLIT):
+    for var in xgm.ALL_VARIANTS:
         assert ctx.motif_count(g, 4, policy=xgm.SCHED_FIXED, variant=var) == \
             case["counts"]["motif4"], var
     g.close()

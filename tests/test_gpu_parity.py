@@ -1,7 +1,7 @@
 """GPU engine vs the reference (golden counts from its binaries) and the oracle.
 
 Every count is compared bit-exactly.  Sizes are small enough for the oracle to finish
-in seconds; larger graphs are covered by size-independent checks in test_gpu_scale.py.
+in seconds (R-MAT up to scale 19); the full 4096-graph batch is in test_gpu_batch.py.
 """
 from __future__ import annotations
 
@@ -64,8 +64,7 @@ def test_schedules_never_change_counts(xgm, ctx):
     g = ctx.graph_from_edges(nv, s, d)
     for pat in ("triangle", "4-clique", "5-clique", "diamond", "tailedtriangle"):
         base = ctx.count(g, pat)
-        for var in (xgm.VAR_WARP, xgm.VAR_CTA, xgm.VAR_SPLIT, xgm.VAR_WIDE, xgm.VAR_SEARCH,
-                    xgm.VAR_BUCKET):
+        for var in xgm.ALL_VARIANTS:
             assert ctx.count(g, pat, policy=xgm.SCHED_FIXED, variant=var) == base, (pat, var)
         for smax, wmax, dmax, cmax in ((0, 8, 0, 64), (8, 32, 64, 128), (32, 1, -1, 1),
                                        (4, 16, 100, 2048)):
@@ -73,6 +72,8 @@ def test_schedules_never_change_counts(xgm, ctx):
                              cta_max=cmax) == base, (pat, smax, wmax, dmax, cmax)
         for bmax, smax in ((32, 0), (8, 32), (1, 4)):  # bucket-filtered search tiers
             assert ctx.count(g, pat, bucket_max=bmax, search_max=smax) == base, (pat, bmax)
+        for gmax, bmax in ((8, 0), (3, 16), (5, 32)):  # eight-lane group tasks
+            assert ctx.count(g, pat, group_max=gmax, bucket_max=bmax) == base, (pat, gmax)
 
 
 def test_upload_paths_agree(xgm, ctx, orc):

@@ -47,8 +47,9 @@ MOTIF4_NAMES = ["3-star", "4-path", "tailed-triangle", "4-cycle", "diamond", "4-
 SCHED_HEURISTIC, SCHED_LEARNED, SCHED_FIXED, SCHED_TUNED = 0, 1, 2, 3
 SCHED_NO_GRAPH = 1
 TUNE_BUCKETS = 16
-VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH, VAR_BUCKET = 0, 1, 2, 3, 4, 5
-NUM_VARIANTS = 6
+VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH, VAR_BUCKET, VAR_GROUP = 0, 1, 2, 3, 4, 5, 6
+NUM_VARIANTS = 7
+ALL_VARIANTS = (VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH, VAR_BUCKET, VAR_GROUP)
 
 MODEL_FEATURES, MODEL_HIDDEN = 12, 32
 MODEL_PARAMS = MODEL_HIDDEN * MODEL_FEATURES + 2 * MODEL_HIDDEN + 1
@@ -85,7 +86,7 @@ class Sched(C.Structure):
     _fields_ = [("policy", C.c_int), ("variant", C.c_int), ("model", C.c_void_p),
                 ("warp_max", C.c_int), ("cta_max", C.c_int), ("order_by_cost", C.c_int),
                 ("table", C.c_void_p), ("flags", C.c_int), ("wide_max", C.c_int),
-                ("search_max", C.c_int), ("bucket_max", C.c_int)]
+                ("search_max", C.c_int), ("bucket_max", C.c_int), ("group_max", C.c_int)]
 
 
 class TuneResult(C.Structure):
@@ -256,10 +257,11 @@ class Context:
 
     @staticmethod
     def _sched(policy=SCHED_HEURISTIC, variant=0, model=None, warp_max=0, cta_max=0,
-               order_by_cost=1, table=None, flags=0, wide_max=0, search_max=0, bucket_max=0):
+               order_by_cost=1, table=None, flags=0, wide_max=0, search_max=0, bucket_max=0,
+               group_max=0):
         sp = Sched(policy, variant, model._h if model is not None else None, warp_max, cta_max,
                    order_by_cost, C.cast(C.pointer(table), C.c_void_p) if table is not None
-                   else None, flags, wide_max, search_max, bucket_max)
+                   else None, flags, wide_max, search_max, bucket_max, group_max)
         sp._keep = table  # keep the table alive with the struct
         return sp
 
@@ -267,10 +269,11 @@ class Context:
               model: Optional["Model"] = None, warp_max: int = 0, cta_max: int = 0,
               order_by_cost: int = 1, table: Optional[TuneTable] = None,
               wide_max: int = 0, search_max: int = 0, bucket_max: int = 0,
-              with_stats: bool = False):
+              group_max: int = 0, with_stats: bool = False):
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
         sp = self._sched(policy, variant, model, warp_max, cta_max, order_by_cost, table,
-                         wide_max=wide_max, search_max=search_max, bucket_max=bucket_max)
+                         wide_max=wide_max, search_max=search_max, bucket_max=bucket_max,
+                         group_max=group_max)
         out = C.c_uint64()
         st = Stats()
         _check(lib().xgm_count(self._h, graph._h, plan._h, C.byref(sp), C.byref(out),

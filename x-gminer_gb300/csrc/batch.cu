@@ -518,6 +518,7 @@ xgm_status xgm_autotune(xgm_ctx* ctx, const xgm_graph* g, xgm_batch* b, const xg
         if (v == keep) continue;
         if ((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH || v == XGM_VAR_BUCKET) && smin > kWarpCap)
           continue;
+        if (v == XGM_VAR_GROUP && smin > kGroupCap) continue;
         if (v == XGM_VAR_WIDE && smin > kWideCap) continue;
         if (v == XGM_VAR_CTA && smin > kCtaCap) continue;
         tab.variant[k] = v;

@@ -799,6 +799,76 @@ __device__ uint64_t warp_bucket_task(const GView& g, WarpSmem& w, int32_t v0) {
   return acc;
 }
 
+// Eight lanes per task, four tasks per warp, local set S = N+(v0) with s <= 8: rows by
+// binary search as in the SEARCH tier, each group of eight lanes its own task (the
+// per-task granularity the reference fixes at one warp, glumin_GM_solver.cu:324-346).
+// rows / cnt are the group's 8-entry slices of the warp's region.  Returns this lane's
+// partial count (the caller sums the group); *q2out gets its local-edge partial.
+template <int Q, int MODE>
+__device__ uint64_t group_task(const GView& g, uint32_t* rows, uint32_t* cnt, int32_t v0, bool ok,
+                               Part part, uint64_t* q2out) {
+  static_assert(Q >= 2, "group tasks count at least local edges");
+  constexpr bool MULTI = MODE == kModeMulti;
+  constexpr bool PART = MODE == kModePart || MULTI;
+  const int lane = threadIdx.x & 31, gl = lane & 7, gbase = lane & ~7;
+  longlong2 d0 = make_longlong2(0, 0);
+  if (ok) d0 = ldg_ll2(g.dptr + v0);
+  const int s = ok ? (int)(d0.y - d0.x) : 0;
+  int32_t xs = 0;
+  longlong2 dx = make_longlong2(0, 0);
+  if (gl < s) {
+    xs = ldg_i32(g.col + d0.x + gl);
+    dx = ldg_ll2(g.dptr + xs);
+  }
+  cnt[gl] = 0u;
+  __syncwarp();
+  uint32_t myrow = 0u;
+  uint64_t acc = 0, q2 = 0;
+  for (int i = 0; i < kGroupCap - 1; ++i) {  // uniform trip count: every group shuffles alike
+    const long long a = __shfl_sync(kFull, dx.x, gbase + i), b = __shfl_sync(kFull, dx.y, gbase + i);
+    const int j = i + 1 + gl;
+    const int32_t y = __shfl_sync(kFull, xs, gbase + (j < kGroupCap ? j : kGroupCap - 1));
+    bool found = false;
+    long long at = 0;
+    if (j < s) {
+      long long lo = a, hi = b;
+      while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (ldg_i32(g.col + mid) < y) lo = mid + 1; else hi = mid;
+      }
+      found = lo < b && ldg_i32(g.col + lo) == y;
+      at = lo;
+    }
+    const uint32_t bits = (__ballot_sync(kFull, found) >> gbase) & 0xFFu;
+    if (gl == i) myrow = bits << (i + 1);
+    if (Q == 2 && found) acc += 1;
+    if (PART) {
+      if (found) {
+        atomicAdd(&cnt[j], 1u);
+        atomicAdd(&part.e[at], 1u);
+      }
+      if (gl == 0 && bits) atomicAdd(&cnt[i], (unsigned)__popc(bits));
+    }
+    if (MULTI && found) q2 += 1;
+  }
+  rows[gl] = myrow;
+  __syncwarp();
+  if (PART && gl < s && cnt[gl]) {
+    atomicAdd(&part.v[xs], (unsigned long long)cnt[gl]);
+    atomicAdd(&part.e[d0.x + gl], cnt[gl]);
+  }
+  if (Q >= 3 && gl < s) acc += word_deep<Q - 1>(rows, myrow);
+  __syncwarp();
+  if (MULTI) *q2out = q2;
+  return acc;
+}
+
+__device__ __forceinline__ uint64_t group_sum_u64(uint64_t v) {
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
 // One warp, local set S = N+(v0) with s <= 128 (rows of 4 words): Q-cliques of the
 // local DAG.  Same walk as the CTA tier (segment registers, four loads in flight, Bloom
 // pre-filter) with binary search in S; counting gives each lane whole rows.
@@ -984,6 +1054,18 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
 }
 
 // ------------------------------------------------------------ persistent kernel
+// Emission by one lane that holds a task's totals (grouped tasks).
+__device__ __forceinline__ void emit_one(const GOut& o, int32_t v0, uint64_t a, uint64_t b,
+                                         uint64_t& acc) {
+  if (o.gid) {
+    const long long base = (long long)o.gid[v0] * o.stride;
+    if (a && o.slot >= 0) atomicAdd(&o.out[base + o.slot], (unsigned long long)a);
+    if (b && o.slot2 >= 0) atomicAdd(&o.out[base + o.slot2], (unsigned long long)b);
+  } else {
+    acc += a;
+  }
+}
+
 // Per-task emission: one global total (gid == null) or per-graph totals
 // out[gid[v0] * stride + slot] (batched graphs).  Called by all 32 lanes of a warp.
 __device__ __forceinline__ void emit(const GOut& o, int32_t v0, uint64_t r, uint64_t r2,
@@ -1016,7 +1098,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
   __shared__ long long task_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long n_split = t.n[0], n_cta = t.n[1], n_warp = t.n[2], n_hubs = t.n[3];
-  const long long n_wide = t.n[4], n_search = t.n[5], n_bucket = t.n[6];
+  const long long n_wide = t.n[4], n_search = t.n[5], n_bucket = t.n[6], n_group = t.n[7];
   uint64_t acc = 0;
 
   // 1) hub edge sub-tasks: local set N+(v0) & N+(v1), (K-2)-cliques of it
@@ -1148,6 +1230,51 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
       else if (!PART) emit(o, v0, r, 0, acc);
     }
     if (t.log_search && lane == 0) t.log_search[ti] = clock64() - c0;
+  }
+  // grouped tasks: four per warp, eight lanes each (weighted mode: one task at a time)
+  for (;;) {
+    long long base = 0;
+    if (lane == 0) base = (long long)atomicAdd(&q->group, (unsigned long long)kGroupsPerWarp);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= n_group) break;
+    if constexpr (MODE == kModeWeight) {
+      for (int x = 0; x < kGroupsPerWarp && base + x < n_group; ++x) {
+        const int32_t v0 = t.group[base + x];
+        const longlong2 d0 = ldg_ll2(g.dptr + v0);
+        const int s = (int)(d0.y - d0.x);
+        if (s > kGroupCap) {
+          if (lane == 0) atomicOr(err, ERR_CAPACITY);
+        } else if (s >= kMinS) {
+          acc += warp_search_task<K - 1, MODE>(g, ws, v0, part, nullptr);
+        }
+      }
+    } else {
+      const int gi = lane >> 3;
+      const long long ti = base + gi;
+      const bool live = ti < n_group;
+      const long long c0 = t.log_group ? clock64() : 0;
+      const int32_t v0 = live ? t.group[ti] : 0;
+      int s = 0;
+      if (live) {
+        const longlong2 d0 = ldg_ll2(g.dptr + v0);
+        s = (int)(d0.y - d0.x);
+        if (s > kGroupCap && (lane & 7) == 0) atomicOr(err, ERR_CAPACITY);
+      }
+      const bool ok = live && s >= kMinS && s <= kGroupCap;
+      uint64_t q2 = 0;
+      const uint64_t r = group_sum_u64(
+          group_task<K - 1, MODE>(g, ws.rows + 8 * gi, ws.cnt + 8 * gi, v0, ok, part, &q2));
+      q2 = group_sum_u64(q2);
+      if (ok && (lane & 7) == 0) {
+        if (PART) {
+          const uint64_t tot = MULTI ? q2 : r;
+          if (tot) atomicAdd(&part.v[v0], (unsigned long long)tot);
+        }
+        if (MULTI) emit_one(o, v0, q2, r, acc);
+        else if (!PART) emit_one(o, v0, r, 0, acc);
+      }
+      if (t.log_group && live && (lane & 7) == 0) t.log_group[ti] = clock64() - c0;
+    }
   }
   for (;;) {  // bucket-filtered search tasks (run as SEARCH outside plain counting)
     long long ti = 0;

@@ -11,12 +11,14 @@ constexpr int kHashSize = 2048;             // open-addressing table for the loc
 constexpr int kWarpCap = 32;                // largest local set a warp task holds
 constexpr int kWideCap = 128;               // largest local set a wide-warp task holds
 constexpr int kWideWords = 4;               // bitmap words per row of a wide-warp task
+constexpr int kGroupCap = 8;                // largest local set of an eight-lane group task
+constexpr int kGroupsPerWarp = 32 / kGroupCap;
 
 // Task lists of one counting launch.  Sizes live on the device (`n`), so task
 // generation and counting run without a host round trip and can be graph-captured:
 //   n[0] = hub edge sub-tasks, n[1] = CTA vertex tasks, n[2] = warp vertex tasks,
 //   n[3] = hub vertices, n[4] = wide-warp vertex tasks, n[5] = binary-search warp tasks,
-//   n[6] = bucket-filtered binary-search warp tasks.
+//   n[6] = bucket-filtered binary-search warp tasks, n[7] = eight-lane group tasks.
 // Hub sub-task t belongs to hub split_v[h] with split_off[h] <= t < split_off[h+1];
 // its second vertex is the (t - split_off[h])-th out-neighbour of the hub.
 // Per-task timing logs (clock64 cycles) are indexed like the lists; any may be null.
@@ -26,6 +28,7 @@ struct TaskLists {
   const int32_t* wide = nullptr;   // vertex tasks run by one warp with 4-word rows (<= kWideCap)
   const int32_t* search = nullptr; // warp tasks (<= kWarpCap) built by binary search
   const int32_t* bucket = nullptr; // warp tasks (<= kWarpCap), bucket-filtered search
+  const int32_t* group = nullptr;  // tasks run four to a warp (<= kGroupCap)
   const int32_t* split_v = nullptr;
   const int64_t* split_off = nullptr;
   const int64_t* n = nullptr;
@@ -35,6 +38,7 @@ struct TaskLists {
   long long* log_wide = nullptr;
   long long* log_search = nullptr;
   long long* log_bucket = nullptr;
+  long long* log_group = nullptr;
 };
 
 // Per-graph outputs of batched launches: task totals go to out[gid[v0] * stride + slot]
@@ -49,7 +53,7 @@ struct GOut {
 
 // Work-queue heads, zeroed before each launch.
 struct QueueHeads {
-  unsigned long long split, cta, warp, wide, search, bucket, pad[2];
+  unsigned long long split, cta, warp, wide, search, bucket, group, pad;
 };
 
 size_t clique_smem_bytes();

@@ -85,6 +85,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
       }
     XGM_CUDA_TRY(classify_table(g, k - 1, *sp.table, tb, s));
   } else {
+    int gmax = sp.group_max > 0 ? sp.group_max : 0;
     int bmax = sp.bucket_max > 0 ? sp.bucket_max : 0;
     int smax = sp.search_max > 0 ? sp.search_max : 0;
     int wmax = sp.warp_max > 0 ? sp.warp_max : kWarpCap;
@@ -98,6 +99,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
         case XGM_VAR_CTA: wmax = 0; dmax = 0; cmax = kCtaCap; break;
         case XGM_VAR_SPLIT: wmax = 0; dmax = 0; cmax = 0; break;
         case XGM_VAR_BUCKET: bmax = kWarpCap; wmax = 0; dmax = kWideCap; cmax = kCtaCap; break;
+        case XGM_VAR_GROUP: gmax = kGroupCap; wmax = kWarpCap; dmax = kWideCap; cmax = kCtaCap; break;
         default:
           set_thread_error("unknown variant for XGM_SCHED_FIXED");
           return XGM_ERR_INVALID;
@@ -107,7 +109,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
       return XGM_ERR_INVALID;
     }
     if (bmax > 0) XGM_CUDA_TRY(ensure_bucket_index(g, s));
-    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax, bmax));
+    XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax, bmax, gmax));
   }
   XGM_CUDA_TRY(build_lists(g, tb, order, s));
   return XGM_OK;
@@ -318,7 +320,7 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   }
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   if (k || pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_TAILED_TRIANGLE)
-    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 7,
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 8,
                                  cudaMemcpyDeviceToDevice, s));
   xgm_status r = ctx_sync_scalars(ctx);
   if (r != XGM_OK) return r;
@@ -335,8 +337,9 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   st.variant_tasks[XGM_VAR_WIDE] = ctx->h_sc->n[4];
   st.variant_tasks[XGM_VAR_SEARCH] = ctx->h_sc->n[5];
   st.variant_tasks[XGM_VAR_BUCKET] = ctx->h_sc->n[6];
+  st.variant_tasks[XGM_VAR_GROUP] = ctx->h_sc->n[7];
   st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4] +
-             ctx->h_sc->n[5] + ctx->h_sc->n[6];
+             ctx->h_sc->n[5] + ctx->h_sc->n[6] + ctx->h_sc->n[7];
   r = check_device_flag(ctx, ctx->h_sc->err);
   if (r != XGM_OK) return r;
   *out = ctx->h_sc->count;
@@ -471,7 +474,7 @@ xgm_status motif_terms(xgm_ctx* ctx, const DevGraph& g, const xgm_sched& sp, boo
                                   ctx->d_sc->terms, s));
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   if (part)
-    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 7,
+    XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->tb.n, sizeof(int64_t) * 8,
                                  cudaMemcpyDeviceToDevice, s));
   xgm_status r = ctx_sync_scalars(ctx);
   if (r != XGM_OK) return r;
@@ -490,8 +493,9 @@ xgm_status motif_terms(xgm_ctx* ctx, const DevGraph& g, const xgm_sched& sp, boo
     st.variant_tasks[XGM_VAR_WIDE] = ctx->h_sc->n[4];
     st.variant_tasks[XGM_VAR_SEARCH] = ctx->h_sc->n[5];
     st.variant_tasks[XGM_VAR_BUCKET] = ctx->h_sc->n[6];
+    st.variant_tasks[XGM_VAR_GROUP] = ctx->h_sc->n[7];
     st.tasks = ctx->h_sc->n[1] + ctx->h_sc->n[2] + ctx->h_sc->n[3] + ctx->h_sc->n[4] +
-               ctx->h_sc->n[5] + ctx->h_sc->n[6];
+               ctx->h_sc->n[5] + ctx->h_sc->n[6] + ctx->h_sc->n[7];
   }
   r = check_device_flag(ctx, ctx->h_sc->err);
   if (r != XGM_OK) return r;

@@ -36,7 +36,9 @@ inline unsigned grid_for(int64_t n) {
 
 // Warps a task of each variant occupies while it runs (resource-time weight).
 __host__ __device__ inline float variant_warps(int v) {
-  return (v == XGM_VAR_CTA || v == XGM_VAR_SPLIT) ? (float)kCtaWarps : 1.0f;
+  return (v == XGM_VAR_CTA || v == XGM_VAR_SPLIT) ? (float)kCtaWarps
+         : v == XGM_VAR_GROUP                      ? 1.0f / kGroupsPerWarp
+                                                   : 1.0f;
 }
 
 // Features of vertex task r (variant one-hot left zero for the caller).
@@ -50,14 +52,12 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
     sum += l;
     maxd = l > maxd ? l : maxd;
   }
-  const long long deg = d0.y - g.rowptr[r];
-  // 0-4 task shape, 5 clique depth, 6-11 variant one-hot (caller)
+  // 0-3 task shape, 4 clique depth, 5-11 variant one-hot (caller)
   f[0] = log2f(1.0f + (float)s) / 11.0f;
   f[1] = log2f(1.0f + (float)sum) / 24.0f;
   f[2] = log2f(1.0f + (float)maxd) / 11.0f;
-  f[3] = log2f(1.0f + (float)deg) / 18.0f;
-  f[4] = (float)sum / ((float)s * (float)maxd + 1.0f);
-  f[5] = (float)(k - 3) * 0.5f;
+  f[3] = (float)sum / ((float)s * (float)maxd + 1.0f);
+  f[4] = (float)(k - 3) * 0.5f;
   for (int v = 0; v < XGM_NUM_VARIANTS; ++v) f[kShapeFeat + v] = 0.0f;
 }
 
@@ -119,6 +119,7 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
       // multiplies its set-up work and never paid off in any measured configuration
       cand[v] = !(((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH || v == XGM_VAR_BUCKET) &&
                    s > kWarpCap) ||
+                  (v == XGM_VAR_GROUP && s > kGroupCap) ||
                   (v == XGM_VAR_WIDE && s > kWideCap) || (v == XGM_VAR_CTA && s > kCtaCap) ||
                   (v == XGM_VAR_SPLIT && s <= kCtaCap));
       ncand += cand[v];
@@ -444,14 +445,15 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   TaskBuf& tb = ctx->tb;
   XGM_CUDA_TRY(cudaSetDevice(ctx->device));
   XGM_CUDA_TRY(taskbuf_reserve(tb, G.nv, s));
-  const int64_t need = 5 * tb.cap_v + (G.ne_dag > 0 ? G.ne_dag : 1);
+  const int64_t need = 6 * tb.cap_v + (G.ne_dag > 0 ? G.ne_dag : 1);
   if (tb.log_cap < need) {
     if (tb.log) cudaFreeAsync(tb.log, s);
     tb.log = nullptr;
     XGM_CUDA_TRY(cudaMallocAsync(&tb.log, sizeof(long long) * need, s));
     tb.log_cap = need;
   }
-  int bmax = 0, smax = 0, wmax = kWarpCap, dmax = kWideCap, cmax = kCtaCap;
+  int gmax = 0, bmax = 0, smax = 0, wmax = kWarpCap, dmax = kWideCap, cmax = kCtaCap;
+  if (variant == XGM_VAR_GROUP) gmax = kGroupCap;
   if (variant == XGM_VAR_BUCKET) {
     bmax = kWarpCap;
     XGM_CUDA_TRY(ensure_bucket_index(G, s));
@@ -460,7 +462,7 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   if (variant == XGM_VAR_WIDE) wmax = 0;
   if (variant == XGM_VAR_CTA) wmax = dmax = 0;
   if (variant == XGM_VAR_SPLIT) wmax = dmax = cmax = 0;
-  XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s, smax, bmax));
+  XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s, smax, bmax, gmax));
   XGM_CUDA_TRY(build_lists(G, tb, false, s));
   XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
   XGM_CUDA_TRY(launch_clique(k, G.view(), tb.lists(true), &ctx->d_sc->q, &ctx->d_sc->count,
@@ -475,18 +477,21 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
                         : variant == XGM_VAR_WIDE   ? tb.wide
                         : variant == XGM_VAR_SEARCH ? tb.search
                         : variant == XGM_VAR_BUCKET ? tb.bucket
+                        : variant == XGM_VAR_GROUP  ? tb.group
                                                     : tb.split_v;
   const int nidx = variant == XGM_VAR_WARP     ? 2
                    : variant == XGM_VAR_CTA    ? 1
                    : variant == XGM_VAR_WIDE   ? 4
                    : variant == XGM_VAR_SEARCH ? 5
                    : variant == XGM_VAR_BUCKET ? 6
+                   : variant == XGM_VAR_GROUP  ? 7
                                                : 3;
   const long long* lg = variant == XGM_VAR_WARP     ? tl.log_warp
                         : variant == XGM_VAR_CTA    ? tl.log_cta
                         : variant == XGM_VAR_WIDE   ? tl.log_wide
                         : variant == XGM_VAR_SEARCH ? tl.log_search
                         : variant == XGM_VAR_BUCKET ? tl.log_bucket
+                        : variant == XGM_VAR_GROUP  ? tl.log_group
                                                     : tl.log_split;
   k_assemble<<<grid_for(G.nv), kThreads, 0, s>>>(G.view(), k, variant, list, tb.n, nidx, lg,
                                                  tb.split_off, stride, dx, dy, max_rows,

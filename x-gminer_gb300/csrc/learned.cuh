@@ -9,7 +9,7 @@ namespace xgm {
 
 constexpr int kFeat = XGM_MODEL_FEATURES;
 constexpr int kShapeFeat = kFeat - XGM_NUM_VARIANTS;  // task shape + depth; then one-hot
-static_assert(kShapeFeat == 6, "features: 5 task-shape values, the clique depth, a variant one-hot");
+static_assert(kShapeFeat == 5, "features: 4 task-shape values, the clique depth, a variant one-hot");
 constexpr int kHidden = XGM_MODEL_HIDDEN;
 constexpr int kParams = XGM_MODEL_PARAMS;
 constexpr int kOffB1 = kHidden * kFeat;

@@ -26,14 +26,15 @@ inline unsigned grid_for(int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); \
        i += (int64_t)gridDim.x * blockDim.x)
 
-__global__ void k_classify_heur(const longlong2* dptr, int64_t nv, int kmin, int bucket_max,
-                                int search_max, int warp_max, int wide_max, int cta_max,
-                                uint8_t* var) {
+__global__ void k_classify_heur(const longlong2* dptr, int64_t nv, int kmin, int group_max,
+                                int bucket_max, int search_max, int warp_max, int wide_max,
+                                int cta_max, uint8_t* var) {
   GRID_STRIDE(r, nv) {
     const longlong2 d = dptr[r];
     const int64_t s = d.y - d.x;
     uint8_t v;
     if (s < kmin) v = VAR_SKIP;
+    else if (s <= group_max) v = VAR_GROUP;
     else if (s <= bucket_max) v = VAR_BUCKET;
     else if (s <= search_max) v = VAR_SEARCH;
     else if (s <= warp_max) v = VAR_WARP;
@@ -59,7 +60,8 @@ __global__ void k_classify_table(const longlong2* dptr, int64_t nv, int kmin, xg
     uint8_t v = VAR_SKIP;
     if (s >= kmin) {
       v = tab.variant[degree_bucket(s)];
-      if (v > VAR_BUCKET) v = VAR_SPLIT;
+      if (v > VAR_GROUP) v = VAR_SPLIT;
+      if (v == VAR_GROUP && s > kGroupCap) v = VAR_WARP;
       if ((v == VAR_SEARCH || v == VAR_BUCKET) && s > kWarpCap) v = VAR_WIDE;
       if (v == VAR_WARP && s > kWarpCap) v = VAR_WIDE;
       if (v == VAR_WIDE && s > kWideCap) v = VAR_CTA;
@@ -67,26 +69,6 @@ __global__ void k_classify_table(const longlong2* dptr, int64_t nv, int kmin, xg
     }
     var[r] = v;
   }
-}
-
-__global__ void k_flag_eq(const uint8_t* var, int64_t nv, uint8_t x, uint8_t* flag) {
-  GRID_STRIDE(r, nv) flag[r] = var[r] == x;
-}
-
-__global__ void k_scatter(const uint8_t* flag, const int64_t* pos, int64_t nv, int32_t* out) {
-  GRID_STRIDE(r, nv) if (flag[r]) out[pos[r]] = (int32_t)r;
-}
-
-__global__ void k_hub_weights(const uint8_t* var, const longlong2* dptr, int64_t nv, int64_t* w) {
-  GRID_STRIDE(r, nv) {
-    const longlong2 d = dptr[r];
-    w[r] = var[r] == VAR_SPLIT ? (d.y - d.x) : 0;
-  }
-}
-
-__global__ void k_hub_offsets(const uint8_t* var, const int64_t* pos, const int64_t* w, int64_t nv,
-                              int64_t* split_off) {
-  GRID_STRIDE(r, nv) if (var[r] == VAR_SPLIT) split_off[pos[r]] = w[r];
 }
 
 __global__ void k_hub_tail(const int64_t* n, int64_t* split_off) {
@@ -124,16 +106,16 @@ __global__ void k_bin_scan(unsigned long long* hist, int64_t* n) {
       hist[v * kBins + b] = run;
       run += c;
     }
-    // var code -> n[] slot: WARP 2, CTA 1, SPLIT 3, WIDE 4, SEARCH 5, BUCKET 6
+    // var code -> n[] slot: WARP 2, CTA 1, SPLIT 3, WIDE 4, SEARCH 5, BUCKET 6, GROUP 7
     n[v == VAR_WARP ? 2 : v == VAR_CTA ? 1 : v == VAR_SPLIT ? 3 : v == VAR_WIDE ? 4
-      : v == VAR_SEARCH ? 5 : 6] = (int64_t)run;
+      : v == VAR_SEARCH ? 5 : v == VAR_BUCKET ? 6 : 7] = (int64_t)run;
   }
 }
 
 __global__ void k_bin_scatter(const uint8_t* var, const float* cost, int64_t nv,
                               unsigned long long* cursor, int32_t* warp_l, int32_t* cta_l,
                               int32_t* hub_l, int32_t* wide_l, int32_t* search_l,
-                              int32_t* bucket_l) {
+                              int32_t* bucket_l, int32_t* group_l) {
   GRID_STRIDE(r, nv) {
     const uint8_t v = var[r];
     if (v < kNumVar) {
@@ -143,9 +125,84 @@ __global__ void k_bin_scatter(const uint8_t* var, const float* cost, int64_t nv,
                      : v == VAR_SPLIT ? hub_l
                      : v == VAR_WIDE  ? wide_l
                      : v == VAR_SEARCH ? search_l
-                                      : bucket_l;
+                     : v == VAR_BUCKET ? bucket_l
+                                      : group_l;
       out[p] = (int32_t)r;
     }
+  }
+}
+
+// ---- natural-order lists in one pass: per-tile code counts, one scan, stable scatter
+constexpr int kCompactThreads = 256;
+constexpr int kCompactItems = 16;
+constexpr int kCompactTile = kCompactThreads * kCompactItems;
+
+__global__ void __launch_bounds__(kCompactThreads) k_compact_count(const uint8_t* var, int64_t nv,
+                                                                   int64_t tiles, int64_t* cnt) {
+  __shared__ int c_sm[kNumVar];
+  if (threadIdx.x < kNumVar) c_sm[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kCompactTile;
+#pragma unroll 4
+  for (int j = 0; j < kCompactItems; ++j) {
+    const int64_t i = base + j * kCompactThreads + threadIdx.x;
+    const int v = i < nv ? var[i] : kNumVar;
+    const unsigned peers = __match_any_sync(0xffffffffu, v);
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    if (v < kNumVar && (peers & lt) == 0u) atomicAdd(&c_sm[v], __popc(peers));
+  }
+  __syncthreads();
+  if (threadIdx.x < kNumVar) cnt[threadIdx.x * tiles + blockIdx.x] = c_sm[threadIdx.x];
+}
+
+struct ListOuts {
+  int32_t* p[kNumVar];  // output list per variant code
+};
+
+// cnt holds the exclusive scan of [code][tile] counts (cnt[kNumVar * tiles] = total):
+// an element's slot in its code's list = cnt[c][tile] - cnt[c][0] + rank in the tile.
+__global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(
+    const uint8_t* var, int64_t nv, int64_t tiles, const int64_t* cnt, ListOuts outs) {
+  __shared__ int64_t run[kNumVar];
+  __shared__ int wcnt[kCompactThreads / 32][kNumVar];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < kNumVar)
+    run[threadIdx.x] = cnt[threadIdx.x * tiles + blockIdx.x] - cnt[threadIdx.x * tiles];
+  const int64_t base = (int64_t)blockIdx.x * kCompactTile;
+  for (int j = 0; j < kCompactItems; ++j) {
+    if (lane < kNumVar) wcnt[warp][lane] = 0;
+    __syncthreads();
+    const int64_t i = base + j * kCompactThreads + threadIdx.x;
+    const int v = i < nv ? var[i] : kNumVar;
+    const unsigned peers = __match_any_sync(0xffffffffu, v);
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    const int rank = __popc(peers & lt);
+    if (v < kNumVar && rank == 0) wcnt[warp][v] = __popc(peers);
+    __syncthreads();
+    if (v < kNumVar) {
+      int64_t pos = run[v] + rank;
+      for (int w = 0; w < warp; ++w) pos += wcnt[w][v];
+      outs.p[v][pos] = (int32_t)i;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumVar) {
+      int t = 0;
+      for (int w = 0; w < kCompactThreads / 32; ++w) t += wcnt[w][threadIdx.x];
+      run[threadIdx.x] += t;
+    }
+    __syncthreads();
+  }
+}
+
+// List sizes into n[] (code -> slot as in k_bin_scan).
+__global__ void k_compact_sizes(const int64_t* cnt, int64_t tiles, int64_t* n) {
+  if (threadIdx.x < kNumVar) {
+    const int v = threadIdx.x;
+    const int64_t sz = cnt[(v + 1) * tiles] - cnt[v * tiles];
+    n[v == VAR_WARP ? 2 : v == VAR_CTA ? 1 : v == VAR_SPLIT ? 3 : v == VAR_WIDE ? 4
+      : v == VAR_SEARCH ? 5 : v == VAR_BUCKET ? 6 : 7] = sz;
   }
 }
 
@@ -179,6 +236,7 @@ TaskLists TaskBuf::lists(bool with_log) const {
   t.wide = wide;
   t.search = search;
   t.bucket = bucket;
+  t.group = group;
   t.split_v = split_v;
   t.split_off = split_off;
   t.n = n;
@@ -188,7 +246,8 @@ TaskLists TaskBuf::lists(bool with_log) const {
     t.log_wide = log + 2 * cap_v;
     t.log_search = log + 3 * cap_v;
     t.log_bucket = log + 4 * cap_v;
-    t.log_split = log + 5 * cap_v;
+    t.log_group = log + 5 * cap_v;
+    t.log_split = log + 6 * cap_v;
   }
   return t;
 }
@@ -202,38 +261,39 @@ cudaError_t taskbuf_reserve(TaskBuf& tb, int64_t nv, cudaStream_t s) {
   TRY(dalloc(&tb.wide, c, s));
   TRY(dalloc(&tb.search, c, s));
   TRY(dalloc(&tb.bucket, c, s));
+  TRY(dalloc(&tb.group, c, s));
   TRY(dalloc(&tb.split_v, c, s));
   TRY(dalloc(&tb.split_off, c + 1, s));
   TRY(dalloc(&tb.n, 8, s));
   TRY(dalloc(&tb.var, c, s));
-  TRY(dalloc(&tb.flag, c, s));
-  TRY(dalloc(&tb.pos, c, s));
   TRY(dalloc(&tb.w, c, s));
   TRY(dalloc(&tb.cost, c, s));
-  TRY(dalloc(&tb.tmp, c, s));
   tb.cap_v = c;
   return cudaSuccess;
 }
 
 void taskbuf_free(TaskBuf& tb, cudaStream_t s) {
-  void* ps[] = {tb.cta, tb.warp, tb.wide, tb.search, tb.bucket, tb.split_v, tb.split_off, tb.n, tb.var,
-                tb.flag, tb.pos, tb.w, tb.cost, tb.tmp, tb.log};
+  void* ps[] = {tb.cta, tb.warp, tb.wide, tb.search, tb.bucket, tb.group, tb.split_v, tb.split_off, tb.n, tb.var,
+                tb.w, tb.cost, tb.log};
   for (void* p : ps)
     if (p) cudaFreeAsync(p, s);
   tb = TaskBuf{};
 }
 
 cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int wide_max, int cta_max,
-                               TaskBuf& tb, cudaStream_t s, int search_max, int bucket_max) {
+                               TaskBuf& tb, cudaStream_t s, int search_max, int bucket_max,
+                               int group_max) {
   if (search_max > kWarpCap) search_max = kWarpCap;
   if (bucket_max > kWarpCap) bucket_max = kWarpCap;
+  if (group_max > kGroupCap) group_max = kGroupCap;
   if (warp_max > kWarpCap) warp_max = kWarpCap;
   if (wide_max > kWideCap) wide_max = kWideCap;
   if (k < 2) k = 2;
   if (cta_max > kCtaCap) cta_max = kCtaCap;
   if (g.nv == 0) return cudaSuccess;
-  k_classify_heur<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, k - 1, bucket_max, search_max,
-                                                      warp_max, wide_max, cta_max, tb.var);
+  k_classify_heur<<<grid_for(g.nv), kThreads, 0, s>>>(g.dptr, g.nv, k - 1, group_max, bucket_max,
+                                                      search_max, warp_max, wide_max, cta_max,
+                                                      tb.var);
   return cudaGetLastError();
 }
 
@@ -249,19 +309,27 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
   TRY(cudaMemsetAsync(tb.n, 0, 8 * sizeof(int64_t), s));
   if (nv == 0) return cudaMemsetAsync(tb.split_off, 0, sizeof(int64_t), s);
   if (!order) {
-    // the hub pass goes last: its positions are reused for the hub offsets below
-    const uint8_t codes[6] = {VAR_CTA, VAR_WARP, VAR_WIDE, VAR_SEARCH, VAR_BUCKET, VAR_SPLIT};
-    int32_t* outs[6] = {tb.cta, tb.warp, tb.wide, tb.search, tb.bucket, tb.split_v};
-    int64_t* cnts[6] = {tb.n + 1, tb.n + 2, tb.n + 4, tb.n + 5, tb.n + 6, tb.n + 3};
-    for (int x = 0; x < 6; ++x) {
-      k_flag_eq<<<grid_for(nv), kThreads, 0, s>>>(tb.var, nv, codes[x], tb.flag);
-      TRY(scan_excl(tb.flag, tb.pos, nv, cnts[x], s));
-      k_scatter<<<grid_for(nv), kThreads, 0, s>>>(tb.flag, tb.pos, nv, outs[x]);
-    }
-    // tb.pos still holds the hub positions (last pass)
-    k_hub_weights<<<grid_for(nv), kThreads, 0, s>>>(tb.var, g.dptr, nv, tb.w);
-    TRY(scan_excl(tb.w, tb.w, nv, tb.n + 0, s));
-    k_hub_offsets<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.pos, tb.w, nv, tb.split_off);
+    const int64_t tiles = (nv + kCompactTile - 1) / kCompactTile;
+    int64_t* cnt = nullptr;
+    TRY(dalloc(&cnt, kNumVar * tiles + 1, s));
+    ListOuts outs;
+    outs.p[VAR_WARP] = tb.warp;
+    outs.p[VAR_CTA] = tb.cta;
+    outs.p[VAR_SPLIT] = tb.split_v;
+    outs.p[VAR_WIDE] = tb.wide;
+    outs.p[VAR_SEARCH] = tb.search;
+    outs.p[VAR_BUCKET] = tb.bucket;
+    outs.p[VAR_GROUP] = tb.group;
+    k_compact_count<<<(unsigned)tiles, kCompactThreads, 0, s>>>(tb.var, nv, tiles, cnt);
+    TRY(scan_excl(cnt, cnt, kNumVar * tiles, cnt + kNumVar * tiles, s));
+    k_compact_scatter<<<(unsigned)tiles, kCompactThreads, 0, s>>>(tb.var, nv, tiles, cnt, outs);
+    k_compact_sizes<<<1, 32, 0, s>>>(cnt, tiles, tb.n);
+    cudaFreeAsync(cnt, s);
+    // hub offsets in hub-list order (at most nv hubs; the rest of w stays zero)
+    TRY(cudaMemsetAsync(tb.w, 0, sizeof(int64_t) * nv, s));
+    k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, tb.w);
+    TRY(cudaGetLastError());
+    TRY(scan_excl(tb.w, tb.split_off, nv, tb.n + 0, s));
   } else {
     unsigned long long* hist = nullptr;
     TRY(dalloc(&hist, kNumVar * kBins, s));
@@ -269,7 +337,8 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
     k_bin_hist<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.cost, nv, hist);
     k_bin_scan<<<1, 32, 0, s>>>(hist, tb.n);
     k_bin_scatter<<<grid_for(nv), kThreads, 0, s>>>(tb.var, tb.cost, nv, hist, tb.warp, tb.cta,
-                                                    tb.split_v, tb.wide, tb.search, tb.bucket);
+                                                    tb.split_v, tb.wide, tb.search, tb.bucket,
+                                                    tb.group);
     cudaFreeAsync(hist, s);
     // hub offsets follow the ordered hub list (at most nv hubs; the unused tail of w
     // is zero so the scan total is the number of hub sub-tasks)

@@ -8,9 +8,9 @@ namespace xgm {
 // Variant codes per vertex task (var[]).
 enum : uint8_t {
   VAR_WARP = 0, VAR_CTA = 1, VAR_SPLIT = 2, VAR_WIDE = 3, VAR_SEARCH = 4, VAR_BUCKET = 5,
-  VAR_SKIP = 6
+  VAR_GROUP = 6, VAR_SKIP = 7
 };
-constexpr int kNumVar = 6;
+constexpr int kNumVar = 7;
 
 // Device buffers of one schedule; sized for a graph's vertex count and reused.
 struct TaskBuf {
@@ -20,16 +20,14 @@ struct TaskBuf {
   int32_t* wide = nullptr;
   int32_t* search = nullptr;
   int32_t* bucket = nullptr;
+  int32_t* group = nullptr;
   int32_t* split_v = nullptr;
   int64_t* split_off = nullptr;
-  int64_t* n = nullptr;       // [8] see TaskLists (7 used)
+  int64_t* n = nullptr;       // [8] see TaskLists
   uint8_t* var = nullptr;     // [cap_v] variant per vertex
-  uint8_t* flag = nullptr;    // [cap_v] scratch
-  int64_t* pos = nullptr;     // [cap_v] scratch
   int64_t* w = nullptr;       // [cap_v] scratch
   float* cost = nullptr;      // [cap_v] predicted log-cost (learned policy)
-  int32_t* tmp = nullptr;     // [cap_v] scratch for ordering
-  long long* log = nullptr;   // [5 * cap_v + split cap] per-task timing log (optional)
+  long long* log = nullptr;   // [6 * cap_v + split cap] per-task timing log (optional)
   int64_t log_cap = 0;
 
   TaskLists lists(bool with_log) const;
@@ -41,12 +39,13 @@ void taskbuf_free(TaskBuf& tb, cudaStream_t s);
 // Plain degree-threshold heuristic (the role of WARP_LIMIT / BLOCK_LIMIT,
 // xgminer/include/glumin/common.h:114-116, and the |W| <= 32 switch of
 // clique5_warp_edge_taskallocate.cuh:26): out-degree s < k-1 -> skip,
-// s <= bucket_max -> BUCKET, s <= search_max -> SEARCH, s <= warp_max -> WARP,
-// s <= wide_max -> WIDE, s <= cta_max -> CTA, else SPLIT (bucket_max and search_max
-// are 0 in the plain heuristic).  Lists keep vertex order.
+// s <= group_max -> GROUP, s <= bucket_max -> BUCKET, s <= search_max -> SEARCH,
+// s <= warp_max -> WARP, s <= wide_max -> WIDE, s <= cta_max -> CTA, else SPLIT
+// (group_max, bucket_max and search_max are 0 in the plain heuristic).  Lists keep
+// vertex order.
 cudaError_t classify_heuristic(const DevGraph& g, int k, int warp_max, int wide_max, int cta_max,
                                TaskBuf& tb, cudaStream_t s, int search_max = 0,
-                               int bucket_max = 0);
+                               int bucket_max = 0, int group_max = 0);
 
 // Variant per out-degree bucket (XGM_SCHED_TUNED); roots with out-degree < kmin skip.
 cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& tab, TaskBuf& tb,

@@ -59,8 +59,7 @@ def main():
         g = ctx.graph_from_edges(nv, s, d)
         del s, d
         for pat in PATTERNS:
-            for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_BUCKET, xgm.VAR_WIDE, xgm.VAR_CTA,
-                        xgm.VAR_SPLIT):
+            for var in xgm.ALL_VARIANTS:
                 X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
                 if len(y) > args.rows:  # uniform subsample
                     idx = np.random.default_rng(scale * 7 + var).choice(len(y), args.rows,
@@ -77,7 +76,7 @@ def main():
     vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=6)
     g = ctx.graph_from_edges(int(vo[-1]), s, d)
     for pat in ["triangle", "4-clique", "diamond"]:
-        for var in (xgm.VAR_WARP, xgm.VAR_SEARCH, xgm.VAR_BUCKET, xgm.VAR_WIDE, xgm.VAR_CTA):
+        for var in xgm.ALL_VARIANTS:
             X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
             if len(y) > args.rows:
                 idx = np.random.default_rng(17 + var).choice(len(y), args.rows, replace=False)
@@ -136,6 +135,7 @@ def main():
     b.close()
     spec = {"params": [float(v) for v in model.params()],
             "features": xgm.MODEL_FEATURES, "hidden": xgm.MODEL_HIDDEN,
+            "variants": xgm.NUM_VARIANTS,
             "target": "log2(clock64 cycles x warps occupied) per vertex task and variant",
             "train": {"graphs": [f"rmat s{s} ef16 seed {10 + i}" for i, s in enumerate(args.scales)],
                       "patterns": PATTERNS, "rows": int(len(y)), "mse_initial": loss0,

@@ -47,6 +47,9 @@ def main() -> None:
     kw = {}
     if args.policy == "learned":
         spec = json.load(open(os.path.join(HERE, "costmodel.json")))
+        if spec.get("variants") != xgm.NUM_VARIANTS or spec.get("features") != xgm.MODEL_FEATURES:
+            raise SystemExit("costmodel.json was trained for another feature layout; retrain it "
+                             "with x-gminer_gb300/train_costmodel.py")
         import numpy as np
 
         m = xgm.Model(ctx)
