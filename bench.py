@@ -163,19 +163,21 @@ def load_engine():
 
 
 def load_model(xgm, ctx):
-    """The trained cost model (x-gminer_gb300/costmodel.json) and its queue order."""
+    """The trained cost model (x-gminer_gb300/costmodel.json) and its schedule settings
+    (queue order, margin) as count() keyword arguments."""
     if not os.path.exists(COSTMODEL):
-        return None, 1
+        return None, {}
     with open(COSTMODEL) as f:
         spec = json.load(f)
     if (spec.get("features") != xgm.MODEL_FEATURES or spec.get("variants") != xgm.NUM_VARIANTS
             or len(spec["params"]) != xgm.MODEL_PARAMS):
-        return None, 1  # trained for another feature layout: fall back to the heuristic
+        return None, {}  # trained for another feature layout: fall back to the heuristic
     import numpy as np
 
     m = xgm.Model(ctx)
     m.set_params(np.asarray(spec["params"], dtype=np.float32))
-    return m, int(spec.get("order_by_cost", 1))
+    return m, {"order_by_cost": int(spec.get("order_by_cost", 1)),
+               "margin": float(spec.get("margin", 0.0))}
 
 
 def measured_peaks() -> dict:
@@ -236,9 +238,9 @@ def engine_arm(args, dist: Dist) -> None:
     g = ctx.graph_from_edges(nv, src, dst)
     del src, dst
     info = g.info()
-    model, order = load_model(xgm, ctx) if args.policy == "learned" else (None, 1)
+    model, mkw = load_model(xgm, ctx) if args.policy == "learned" else (None, {})
     policy = xgm.SCHED_LEARNED if model is not None else xgm.SCHED_HEURISTIC
-    kw = {"policy": policy, "model": model, "order_by_cost": order}
+    kw = {"policy": policy, "model": model, **mkw}
 
     def run(n, **k):
         prep, kern, cnt = [], [], None
@@ -376,11 +378,11 @@ def batch_arm(args, dist: Dist) -> None:
     ctx = xgm.Context(dist.local)
     vo, eo, src, dst = xgm.gen_ba_batch(args.graphs, 100, 5000, 3, 8, seed=5)
     b = ctx.batch_from_edges(vo, src, dst)
-    model, order = load_model(xgm, ctx)
+    model, mkw = load_model(xgm, ctx)
     tune = ctx.autotune(b, BATCH_PATTERNS, reps=3)
     runs = {"heuristic": {}, "tuned": {"policy": xgm.SCHED_TUNED, "table": tune["table"]}}
     if model is not None:
-        runs["learned"] = {"policy": xgm.SCHED_LEARNED, "model": model, "order_by_cost": order}
+        runs["learned"] = {"policy": xgm.SCHED_LEARNED, "model": model, **mkw}
     res, ref = {}, None
     for name, kw in runs.items():
         for _ in range(args.warmup):

@@ -212,6 +212,8 @@ typedef struct {
   int search_max;         /* heuristic: out-degree <= search_max -> SEARCH (0: none) */
   int bucket_max;         /* heuristic: out-degree <= bucket_max -> BUCKET (0: none) */
   int group_max;          /* heuristic: out-degree <= group_max -> GROUP (0: none; <= 8) */
+  float margin;           /* learned: predicted log2-cost saving a task needs to leave the
+                             heuristic's variant (0: default 0.2) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };

@@ -86,7 +86,8 @@ class Sched(C.Structure):
     _fields_ = [("policy", C.c_int), ("variant", C.c_int), ("model", C.c_void_p),
                 ("warp_max", C.c_int), ("cta_max", C.c_int), ("order_by_cost", C.c_int),
                 ("table", C.c_void_p), ("flags", C.c_int), ("wide_max", C.c_int),
-                ("search_max", C.c_int), ("bucket_max", C.c_int), ("group_max", C.c_int)]
+                ("search_max", C.c_int), ("bucket_max", C.c_int), ("group_max", C.c_int),
+                ("margin", C.c_float)]
 
 
 class TuneResult(C.Structure):
@@ -258,10 +259,10 @@ class Context:
     @staticmethod
     def _sched(policy=SCHED_HEURISTIC, variant=0, model=None, warp_max=0, cta_max=0,
                order_by_cost=1, table=None, flags=0, wide_max=0, search_max=0, bucket_max=0,
-               group_max=0):
+               group_max=0, margin=0.0):
         sp = Sched(policy, variant, model._h if model is not None else None, warp_max, cta_max,
                    order_by_cost, C.cast(C.pointer(table), C.c_void_p) if table is not None
-                   else None, flags, wide_max, search_max, bucket_max, group_max)
+                   else None, flags, wide_max, search_max, bucket_max, group_max, margin)
         sp._keep = table  # keep the table alive with the struct
         return sp
 
@@ -269,11 +270,11 @@ class Context:
               model: Optional["Model"] = None, warp_max: int = 0, cta_max: int = 0,
               order_by_cost: int = 1, table: Optional[TuneTable] = None,
               wide_max: int = 0, search_max: int = 0, bucket_max: int = 0,
-              group_max: int = 0, with_stats: bool = False):
+              group_max: int = 0, margin: float = 0.0, with_stats: bool = False):
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
         sp = self._sched(policy, variant, model, warp_max, cta_max, order_by_cost, table,
                          wide_max=wide_max, search_max=search_max, bucket_max=bucket_max,
-                         group_max=group_max)
+                         group_max=group_max, margin=margin)
         out = C.c_uint64()
         st = Stats()
         _check(lib().xgm_count(self._h, graph._h, plan._h, C.byref(sp), C.byref(out),
@@ -293,9 +294,10 @@ class Context:
         return (res, st.as_dict()) if with_stats else res
 
     def count_kernels(self, graph: "Graph", pattern, policy: int = SCHED_HEURISTIC,
-                      model: Optional["Model"] = None, order_by_cost: int = 1) -> int:
+                      model: Optional["Model"] = None, order_by_cost: int = 1,
+                      margin: float = 0.0) -> int:
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
-        sp = self._sched(policy, 0, model, 0, 0, order_by_cost)
+        sp = self._sched(policy, 0, model, 0, 0, order_by_cost, margin=margin)
         n = C.c_int()
         _check(lib().xgm_count_kernels(self._h, graph._h, plan._h, C.byref(sp), C.byref(n)), self)
         return int(n.value)
@@ -325,11 +327,12 @@ class Context:
 
     def count_batched(self, batch: "Batch", patterns, policy: int = SCHED_HEURISTIC,
                       model: Optional["Model"] = None, table: Optional[TuneTable] = None,
-                      use_graph: bool = True, order_by_cost: int = 1, with_stats: bool = False):
+                      use_graph: bool = True, order_by_cost: int = 1, margin: float = 0.0,
+                      with_stats: bool = False):
         plans = [p if isinstance(p, Plan) else self.plan(p) for p in patterns]
         arr = (C.c_void_p * len(plans))(*[p._h.value for p in plans])
         sp = self._sched(policy, 0, model, 0, 0, order_by_cost, table,
-                         0 if use_graph else SCHED_NO_GRAPH)
+                         0 if use_graph else SCHED_NO_GRAPH, margin=margin)
         out = np.empty(batch.num_graphs * len(plans), dtype=np.uint64)
         st = Stats()
         _check(lib().xgm_count_batched(self._h, batch._h, C.cast(arr, C.c_void_p), len(plans),

@@ -279,8 +279,9 @@ std::string sched_key(const Slots& sl, const xgm_sched& sp) {
   k.append(reinterpret_cast<const char*>(&sp.policy), sizeof(int) * 2);
   k.append(reinterpret_cast<const char*>(&sp.model), sizeof(void*));
   k.append(reinterpret_cast<const char*>(&sp.warp_max), sizeof(int) * 3);
-  const int more[3] = {sp.wide_max, sp.search_max, sp.bucket_max};
+  const int more[4] = {sp.wide_max, sp.search_max, sp.bucket_max, sp.group_max};
   k.append(reinterpret_cast<const char*>(more), sizeof(more));
+  k.append(reinterpret_cast<const char*>(&sp.margin), sizeof(float));
   if (sp.table) k.append(reinterpret_cast<const char*>(sp.table), sizeof(xgm_tune_table));
   return k;
 }

@@ -23,8 +23,9 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// A task leaves the heuristic's variant only for a predicted saving of at least 0.2 in
-// log2 warp-cycles (~15%): near-ties are where the model is least reliable.
+// By default a task leaves the heuristic's variant only for a predicted saving of at
+// least 0.2 in log2 warp-cycles (~15%): near-ties are where the model is least
+// reliable.  xgm_sched.margin overrides it (the trainer picks it on held-out graphs).
 constexpr float kLearnedMargin = 0.2f;
 
 inline unsigned grid_for(int64_t n) {
@@ -97,7 +98,7 @@ __device__ __forceinline__ void mlp_variants(const float* P, const float* f, con
 }
 
 __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* var, float* cost,
-                                   int need_cost) {
+                                   int need_cost, float margin) {
   __shared__ float P[kParams];
   load_params(wh, P);
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < g.nv;
@@ -138,8 +139,8 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
     uint8_t bv = hv;
     float best = pred[hv];
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
-      if (pred[v] < best - (v == hv ? 0.0f : kLearnedMargin)) {
-        best = pred[v] + kLearnedMargin;  // later candidates must beat the incumbent too
+      if (pred[v] < best - (v == hv ? 0.0f : margin)) {
+        best = pred[v] + margin;  // later candidates must beat the incumbent too
         bv = (uint8_t)v;
       }
     var[r] = bv;
@@ -268,10 +269,11 @@ int clique_k(int pattern) {
 }  // namespace
 
 cudaError_t classify_learned(const DevGraph& g, int k, const xgm_model& m, TaskBuf& tb,
-                             bool need_cost, cudaStream_t s) {
+                             bool need_cost, float margin, cudaStream_t s) {
   if (g.nv == 0) return cudaSuccess;
   k_classify_learned<<<grid_for(g.nv), kThreads, 0, s>>>(g.view(), k, m.wh, tb.var, tb.cost,
-                                                         need_cost ? 1 : 0);
+                                                         need_cost ? 1 : 0,
+                                                         margin > 0.0f ? margin : kLearnedMargin);
   return cudaGetLastError();
 }
 

@@ -32,7 +32,8 @@ namespace xgm {
 // Learned schedule: per vertex task the features, the MLP's predicted log2 warp-cycles
 // for each variant the task fits, the chosen variant (tb.var) and its cost (tb.cost).
 // Without need_cost (no cost ordering) tasks that fit one variant skip the model.
+// margin <= 0: the default margin.
 cudaError_t classify_learned(const DevGraph& g, int k, const xgm_model& m, TaskBuf& tb,
-                             bool need_cost, cudaStream_t s);
+                             bool need_cost, float margin, cudaStream_t s);
 
 }  // namespace xgm

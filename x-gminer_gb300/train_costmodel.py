@@ -93,6 +93,43 @@ def main():
     loss = model.train(X, y, epochs=max(1, args.epochs // 4), batch=4096, lr=5e-4, seed=2)
     print(f"trained on {len(y)} rows: mse {loss0:.3f} -> {loss:.3f}", flush=True)
 
+    pats_b = ["triangle", "4-clique", "diamond"]
+
+    def time_batch(b, **kw):
+        for _ in range(3):
+            ctx.count_batched(b, pats_b, **kw)
+        best, out = None, None
+        for _ in range(5):
+            out, st = ctx.count_batched(b, pats_b, with_stats=True, **kw)
+            best = st["kernel_ms"] if best is None else min(best, st["kernel_ms"])
+        return out, best
+
+    # margin (the predicted saving a task needs to leave the heuristic's variant), chosen
+    # on validation graphs that neither training nor the evaluation below uses: R-MAT
+    # scale 21 seed 98 and a 4096-graph BA batch with seed 7
+    nv, s, d = xgm.gen_rmat(21, 16, seed=98)
+    gv = ctx.graph_from_edges(nv, s, d)
+    vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=7)
+    bv = ctx.batch_from_edges(vo, s, d)
+    del s, d
+    base = {p: timed_count(ctx, gv, p, 3)[1] for p in pats_b}
+    _, base_b = time_batch(bv)
+    sweep = {}
+    for margin in (0.1, 0.2, 0.35, 0.5, 0.75):
+        logs = []
+        for p in pats_b:
+            t = timed_count(ctx, gv, p, 3, policy=xgm.SCHED_LEARNED, model=model,
+                            order_by_cost=0, margin=margin)[1]
+            logs.append(np.log(base[p] / t))
+        _, tb_ = time_batch(bv, policy=xgm.SCHED_LEARNED, model=model, order_by_cost=0,
+                            margin=margin)
+        logs.append(np.log(base_b / tb_))
+        sweep[margin] = float(np.exp(np.mean(logs)))
+        print("margin", margin, "validation geomean speedup", round(sweep[margin], 4), flush=True)
+    margin = max(sweep, key=sweep.get)
+    gv.close()
+    bv.close()
+
     # held-out evaluation: learned vs plain heuristic, identical counts
     nv, s, d = xgm.gen_rmat(args.eval_scale, 16, seed=99)
     g = ctx.graph_from_edges(nv, s, d)
@@ -103,7 +140,7 @@ def main():
         res = {"count": c_h, "heuristic_ms": t_h, "heuristic_variants": v_h}
         for order in (1, 0):
             c_l, t_l, v_l = timed_count(ctx, g, pat, 3, policy=xgm.SCHED_LEARNED, model=model,
-                                        order_by_cost=order)
+                                        order_by_cost=order, margin=margin)
             assert c_h == c_l, (pat, c_h, c_l)
             res[f"learned_ms_order{order}"] = t_l
             res["learned_variants"] = v_l
@@ -116,19 +153,9 @@ def main():
     # batched form: the benchmark's 4096 BA graphs, triangle + 4-clique + diamond
     vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=5)
     b = ctx.batch_from_edges(vo, s, d)
-    pats = ["triangle", "4-clique", "diamond"]
-
-    def tb(**kw):
-        for _ in range(3):
-            ctx.count_batched(b, pats, **kw)
-        best, out = None, None
-        for _ in range(5):
-            out, st = ctx.count_batched(b, pats, with_stats=True, **kw)
-            best = st["kernel_ms"] if best is None else min(best, st["kernel_ms"])
-        return out, best
-
-    ob, th = tb()
-    ol, tl = tb(policy=xgm.SCHED_LEARNED, model=model, order_by_cost=1 if order_gain > 0 else 0)
+    ob, th = time_batch(b)
+    ol, tl = time_batch(b, policy=xgm.SCHED_LEARNED, model=model,
+                        order_by_cost=1 if order_gain > 0 else 0, margin=margin)
     assert np.array_equal(ob, ol)
     evals["batch_ba4096"] = {"heuristic_ms": th, "learned_ms": tl, "speedup": th / tl}
     print("batch", evals["batch_ba4096"], flush=True)
@@ -141,6 +168,8 @@ def main():
                       "patterns": PATTERNS, "rows": int(len(y)), "mse_initial": loss0,
                       "mse_final": loss, "epochs": args.epochs, "parts": meta},
             "order_by_cost": 1 if order_gain > 0 else 0,
+            "margin": margin,
+            "margin_sweep": {str(k): v for k, v in sweep.items()},
             "eval": {"graph": f"rmat s{args.eval_scale} ef16 seed 99", "results": evals}}
     with open(args.out, "w") as f:
         json.dump(spec, f, indent=1)

@@ -54,7 +54,9 @@ def main() -> None:
 
         m = xgm.Model(ctx)
         m.set_params(np.asarray(spec["params"], dtype=np.float32))
-        kw = {"policy": xgm.SCHED_LEARNED, "model": m}
+        kw = {"policy": xgm.SCHED_LEARNED, "model": m,
+              "order_by_cost": int(spec.get("order_by_cost", 1)),
+              "margin": float(spec.get("margin", 0.0))}
     for _ in range(args.repeat):
         count, st = ctx.count(g, pattern, with_stats=True, **kw)
         print(json.dumps({"pattern": pattern, "count": count, "graph": g.info(), **st}))
