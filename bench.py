@@ -383,7 +383,7 @@ def batch_arm(args, dist: Dist) -> None:
     runs = {"heuristic": {}, "tuned": {"policy": xgm.SCHED_TUNED, "table": tune["table"]}}
     if model is not None:
         runs["learned"] = {"policy": xgm.SCHED_LEARNED, "model": model, **mkw}
-    res, ref = {}, None
+    res, ref, kernels = {}, None, {}
     for name, kw in runs.items():
         for _ in range(args.warmup):
             ctx.count_batched(b, BATCH_PATTERNS, **kw)
@@ -392,6 +392,7 @@ def batch_arm(args, dist: Dist) -> None:
         for _ in range(args.steps):
             out, st = ctx.count_batched(b, BATCH_PATTERNS, with_stats=True, **kw)
             ms.append(st["kernel_ms"])
+            kernels[name] = st["launches"]  # kernel nodes of the replayed CUDA graph
         if ref is None:
             ref = out
         assert np.array_equal(out, ref), f"{name} schedule changed a count"
@@ -425,7 +426,7 @@ def batch_arm(args, dist: Dist) -> None:
             "schedules_ms": res, "tuned_variants": tune["variants"],
             "per_graph_calls_ms_estimate": loop_ms_full,
             "speedup_vs_per_graph_calls": loop_ms_full / res[best],
-            "count_total": int(total), "gpu_launches": None}
+            "count_total": int(total), "gpu_launches": kernels[best] * args.steps}
     print(json.dumps(line), flush=True)
     ctx.close()
 

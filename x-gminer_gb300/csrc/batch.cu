@@ -27,6 +27,7 @@ namespace {
 struct CachedExec {
   std::string key;
   cudaGraphExec_t exec = nullptr;
+  int kernels = 0;  // kernel nodes of the captured graph
 };
 
 }  // namespace
@@ -301,7 +302,10 @@ xgm_status count_batched_impl(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const*
     const std::string key = sched_key(sl, sp);
     cudaGraphExec_t exec = nullptr;
     for (auto& c : b->cache)
-      if (c.key == key) exec = c.exec;
+      if (c.key == key) {
+        exec = c.exec;
+        st.launches = c.kernels;
+      }
     if (!exec) {
       XGM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       r = batch_sequence(ctx, b, sl, P, sp);
@@ -312,10 +316,22 @@ xgm_status count_batched_impl(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const*
         return r;
       }
       XGM_CUDA_TRY(e);
+      size_t nn = 0;
+      int kern = 0;
+      if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn) {
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess)
+          for (size_t i = 0; i < nn; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+              ++kern;
+          }
+      }
       const cudaError_t e2 = cudaGraphInstantiate(&exec, graph, 0);
       cudaGraphDestroy(graph);
       XGM_CUDA_TRY(e2);
-      b->cache.push_back(CachedExec{key, exec});
+      b->cache.push_back(CachedExec{key, exec, kern});
+      st.launches = kern;
       XGM_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
     }
     XGM_CUDA_TRY(cudaGraphLaunch(exec, s));

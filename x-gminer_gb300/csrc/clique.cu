@@ -20,10 +20,13 @@
 //    k = 3: number of local edges (no bitmap needed)
 //    k = 4: sum_i sum_{j in row i} popc(row_i & row_j)
 //    k = 5: sum_i sum_{j in row i} sum_{l in row_i & row_j} popc(row_i & row_j & row_l)
+//    k = 6, 7: the same walk one or two levels deeper
 // Hub vertices (s above the CTA capacity) are split into edge sub-tasks (v0, v1) whose
 // local set is N+(v0) & N+(v1) and which count (k-2)-cliques of it the same way.
-// One persistent kernel runs three queues in order: hub edge sub-tasks, CTA vertex
-// tasks, then warp vertex tasks (s <= 32, one-word rows), each fed by an atomic head.
+// One persistent kernel runs seven queues in order, each fed by an atomic head: hub
+// edge sub-tasks, CTA tasks, wide-warp tasks (s <= 128), binary-search warp tasks,
+// eight-lane group tasks (s <= 8, four per warp), bucket-filtered search tasks, and
+// streaming warp tasks (s <= 32).
 #include "clique.cuh"
 
 namespace xgm {

@@ -3,7 +3,7 @@
 // The reference sizes one grid per launch and grid-strides over the COO edge list
 // (clique4_warp_edge.cuh:14) or splits vertices by degree thresholds into warp / block
 // / per-hub launches (xgminer/src/glumin/glumin_GM_solver.cu:324-346, 490-503).  Here
-// one persistent launch consumes three device-built queues (clique.cu), and the
+// one persistent launch consumes seven device-built queues (clique.cu), and the
 // schedule is only the content and order of those queues; it never changes a count.
 #include "prim.cuh"
 #include "sched.cuh"
