@@ -193,6 +193,101 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
   return acc;
 }
 
+// The same counts (Q = 3, 4, unweighted) with two rows per warp where rows are short:
+// rows of one 32-row block share their word range, and once a block's rows span at most
+// 16 words (nwi <= 16) the two half-warps each take one row (rows 32q + warp and
+// 32q + warp + 16), so no lane idles on words past the row's end.  Longer rows keep the
+// full-warp walk of cta_count_rows.  The loops run while either half has work
+// (__any_sync) and every shuffle stays inside its half.
+template <int Q>
+__device__ uint64_t cta_count_rows_paired(const uint32_t* rows, int s, const int32_t* roff) {
+  static_assert(Q == 3 || Q == 4, "paired rows cover the 4- and 5-clique count phases");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int W = (s + 31) >> 5;
+  const int h = lane >> 4, sub = lane & 15;
+  uint64_t acc = 0;
+  for (int q = 0; q < W; ++q) {
+    const int nwi = W - q;
+    const int r1 = (q << 5) + warp, r2 = r1 + kCtaWarps;
+    if (nwi > 16) {  // full-warp rows
+      for (int t = 0; t < 2; ++t) {
+        const int i = t ? r2 : r1;
+        if (i >= s) break;
+        const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
+        const int w = q + lane;
+        unsigned nz = __ballot_sync(kFull, wi != 0u);
+        while (nz) {
+          const int src = __ffs(nz) - 1;
+          nz &= nz - 1;
+          uint32_t bits = __shfl_sync(kFull, wi, src);
+          while (bits) {
+            const int j = ((q + src) << 5) + __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int qj = j >> 5;
+            const uint32_t m = (lane < nwi && w >= qj) ? (wi & rows[roff[j] + (w - qj)]) : 0u;
+            if (Q == 3) {
+              acc += __popc(m);
+            } else {
+              unsigned nz2 = __ballot_sync(kFull, m != 0u);
+              while (nz2) {
+                const int src2 = __ffs(nz2) - 1;
+                nz2 &= nz2 - 1;
+                uint32_t bits2 = __shfl_sync(kFull, m, src2);
+                while (bits2) {
+                  const int l = ((q + src2) << 5) + __ffs(bits2) - 1;
+                  bits2 &= bits2 - 1;
+                  const int ql = l >> 5;
+                  if (w >= ql && m) acc += __popc(m & rows[roff[l] + (w - ql)]);
+                }
+              }
+            }
+          }
+        }
+      }
+      continue;
+    }
+    // half-warp rows: half h takes row r1 or r2, lane sub holds word q + sub
+    const int i = h ? r2 : r1;
+    const uint32_t wi = (i < s && sub < nwi) ? rows[roff[i] + sub] : 0u;
+    const int w = q + sub;
+    unsigned nz = (__ballot_sync(kFull, wi != 0u) >> (h << 4)) & 0xFFFFu;
+    while (__any_sync(kFull, nz != 0u)) {
+      const bool had = nz != 0u;
+      const int src = had ? __ffs(nz) - 1 : 0;
+      if (had) nz &= nz - 1;
+      uint32_t bits = __shfl_sync(kFull, wi, (h << 4) + src);
+      if (!had) bits = 0u;
+      while (__any_sync(kFull, bits != 0u)) {
+        const bool hb = bits != 0u;
+        const int j = hb ? ((q + src) << 5) + __ffs(bits) - 1 : 0;
+        if (hb) bits &= bits - 1;
+        const int qj = j >> 5;
+        const uint32_t m = (hb && sub < nwi && w >= qj) ? (wi & rows[roff[j] + (w - qj)]) : 0u;
+        if (Q == 3) {
+          acc += __popc(m);
+        } else {
+          unsigned nz2 = (__ballot_sync(kFull, m != 0u) >> (h << 4)) & 0xFFFFu;
+          while (__any_sync(kFull, nz2 != 0u)) {
+            const bool had2 = nz2 != 0u;
+            const int src2 = had2 ? __ffs(nz2) - 1 : 0;
+            if (had2) nz2 &= nz2 - 1;
+            uint32_t bits2 = __shfl_sync(kFull, m, (h << 4) + src2);
+            if (!had2) bits2 = 0u;
+            while (__any_sync(kFull, bits2 != 0u)) {
+              const bool hb2 = bits2 != 0u;
+              const int l = hb2 ? ((q + src2) << 5) + __ffs(bits2) - 1 : 0;
+              if (hb2) bits2 &= bits2 - 1;
+              const int ql = l >> 5;
+              if (hb2 && m && w >= ql) acc += __popc(m & rows[roff[l] + (w - ql)]);
+            }
+          }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
 // D-cliques of the local DAG inside a candidate set, for the 6- and 7-clique plans
 // (local clique depth 5 and 6).  The set is warp-distributed: this lane holds word w;
 // every candidate l > i, so the walk of cta_count_rows carries over level by level:
@@ -426,8 +521,9 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
         atomicAdd(&part.e[sbase + i], cnt[i]);
       }
   }
-  if (Q == 3) acc = cta_count_rows<3, WGT>(rows, s, pre, roff);
-  if (Q == 4) acc = cta_count_rows<4, false>(rows, s, pre, roff);
+  if (Q == 3) acc = WGT ? cta_count_rows<3, true>(rows, s, pre, roff)
+                        : cta_count_rows_paired<3>(rows, s, roff);
+  if (Q == 4) acc = cta_count_rows_paired<4>(rows, s, roff);
   if constexpr (Q >= 5) acc = cta_count_deep<Q>(rows, s, roff);
   return acc;
 }
