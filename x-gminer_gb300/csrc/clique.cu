@@ -139,11 +139,13 @@ enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 
 // Count of (q)-cliques in the local DAG held by the CTA (q >= 3 uses the bitmap).  WGT
 // (Q == 3 only) weights each clique by d+ of its top member, d+(S[l]) = pre[l+1]-pre[l].
+// rows [0, n) are walked; W (default: from n) is the word count of the whole set.
 template <int Q, bool WGT>
-__device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, const int32_t* pre,
-                                                   const int32_t* roff) {
+__device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, const int32_t* pre,
+                                                   const int32_t* roff, int W = 0) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int W = (s + 31) >> 5;
+  const int s = n;
+  if (W == 0) W = (n + 31) >> 5;
   uint64_t acc = 0;
   for (int i = warp; i < s; i += kCtaWarps) {
     const int qi = i >> 5, nwi = W - qi;
@@ -193,89 +195,51 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int s, 
   return acc;
 }
 
-// The same counts (Q = 3, 4, unweighted) with two rows per warp where rows are short:
-// rows of one 32-row block share their word range, and once a block's rows span at most
-// 16 words (nwi <= 16) the two half-warps each take one row (rows 32q + warp and
-// 32q + warp + 16), so no lane idles on words past the row's end.  Longer rows keep the
-// full-warp walk of cta_count_rows.  The loops run while either half has work
-// (__any_sync) and every shuffle stays inside its half.
-template <int Q>
-__device__ uint64_t cta_count_rows_paired(const uint32_t* rows, int s, const int32_t* roff) {
-  static_assert(Q == 3 || Q == 4, "paired rows cover the 4- and 5-clique count phases");
+// Rows [row_lo, row_hi) of the local DAG whose rows span at most G words, G lanes per
+// row (32 / G rows per warp): lane sub of a group holds word qi + sub of its row, every
+// ballot / shuffle stays inside the group, and the loops run while any group of the
+// warp has work (__any_sync), so all 32 lanes meet at every warp-synchronous call.
+template <int Q, int G>
+__device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff, int W,
+                                       int row_lo, int row_hi) {
+  static_assert(Q == 3 || Q == 4, "grouped rows cover the 4- and 5-clique count phases");
+  constexpr unsigned kGMask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
+  constexpr int kGroups = 32 / G;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int W = (s + 31) >> 5;
-  const int h = lane >> 4, sub = lane & 15;
+  const int sub = lane % G, gbase = lane - sub;
   uint64_t acc = 0;
-  for (int q = 0; q < W; ++q) {
-    const int nwi = W - q;
-    const int r1 = (q << 5) + warp, r2 = r1 + kCtaWarps;
-    if (nwi > 16) {  // full-warp rows
-      for (int t = 0; t < 2; ++t) {
-        const int i = t ? r2 : r1;
-        if (i >= s) break;
-        const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
-        const int w = q + lane;
-        unsigned nz = __ballot_sync(kFull, wi != 0u);
-        while (nz) {
-          const int src = __ffs(nz) - 1;
-          nz &= nz - 1;
-          uint32_t bits = __shfl_sync(kFull, wi, src);
-          while (bits) {
-            const int j = ((q + src) << 5) + __ffs(bits) - 1;
-            bits &= bits - 1;
-            const int qj = j >> 5;
-            const uint32_t m = (lane < nwi && w >= qj) ? (wi & rows[roff[j] + (w - qj)]) : 0u;
-            if (Q == 3) {
-              acc += __popc(m);
-            } else {
-              unsigned nz2 = __ballot_sync(kFull, m != 0u);
-              while (nz2) {
-                const int src2 = __ffs(nz2) - 1;
-                nz2 &= nz2 - 1;
-                uint32_t bits2 = __shfl_sync(kFull, m, src2);
-                while (bits2) {
-                  const int l = ((q + src2) << 5) + __ffs(bits2) - 1;
-                  bits2 &= bits2 - 1;
-                  const int ql = l >> 5;
-                  if (w >= ql && m) acc += __popc(m & rows[roff[l] + (w - ql)]);
-                }
-              }
-            }
-          }
-        }
-      }
-      continue;
-    }
-    // half-warp rows: half h takes row r1 or r2, lane sub holds word q + sub
-    const int i = h ? r2 : r1;
-    const uint32_t wi = (i < s && sub < nwi) ? rows[roff[i] + sub] : 0u;
-    const int w = q + sub;
-    unsigned nz = (__ballot_sync(kFull, wi != 0u) >> (h << 4)) & 0xFFFFu;
+  for (int i0 = row_lo + warp * kGroups; i0 < row_hi; i0 += kCtaWarps * kGroups) {
+    const int i = i0 + lane / G;
+    const bool live = i < row_hi;
+    const int qi = live ? (i >> 5) : 0, nwi = W - qi;
+    const uint32_t wi = (live && sub < nwi) ? rows[roff[i] + sub] : 0u;
+    const int w = qi + sub;
+    unsigned nz = (__ballot_sync(kFull, wi != 0u) >> gbase) & kGMask;
     while (__any_sync(kFull, nz != 0u)) {
       const bool had = nz != 0u;
       const int src = had ? __ffs(nz) - 1 : 0;
       if (had) nz &= nz - 1;
-      uint32_t bits = __shfl_sync(kFull, wi, (h << 4) + src);
+      uint32_t bits = __shfl_sync(kFull, wi, gbase + src);
       if (!had) bits = 0u;
       while (__any_sync(kFull, bits != 0u)) {
         const bool hb = bits != 0u;
-        const int j = hb ? ((q + src) << 5) + __ffs(bits) - 1 : 0;
+        const int j = hb ? ((qi + src) << 5) + __ffs(bits) - 1 : 0;
         if (hb) bits &= bits - 1;
         const int qj = j >> 5;
         const uint32_t m = (hb && sub < nwi && w >= qj) ? (wi & rows[roff[j] + (w - qj)]) : 0u;
         if (Q == 3) {
           acc += __popc(m);
         } else {
-          unsigned nz2 = (__ballot_sync(kFull, m != 0u) >> (h << 4)) & 0xFFFFu;
+          unsigned nz2 = (__ballot_sync(kFull, m != 0u) >> gbase) & kGMask;
           while (__any_sync(kFull, nz2 != 0u)) {
             const bool had2 = nz2 != 0u;
             const int src2 = had2 ? __ffs(nz2) - 1 : 0;
             if (had2) nz2 &= nz2 - 1;
-            uint32_t bits2 = __shfl_sync(kFull, m, (h << 4) + src2);
+            uint32_t bits2 = __shfl_sync(kFull, m, gbase + src2);
             if (!had2) bits2 = 0u;
             while (__any_sync(kFull, bits2 != 0u)) {
               const bool hb2 = bits2 != 0u;
-              const int l = hb2 ? ((q + src2) << 5) + __ffs(bits2) - 1 : 0;
+              const int l = hb2 ? ((qi + src2) << 5) + __ffs(bits2) - 1 : 0;
               if (hb2) bits2 &= bits2 - 1;
               const int ql = l >> 5;
               if (hb2 && m && w >= ql) acc += __popc(m & rows[roff[l] + (w - ql)]);
@@ -285,6 +249,25 @@ __device__ uint64_t cta_count_rows_paired(const uint32_t* rows, int s, const int
       }
     }
   }
+  return acc;
+}
+
+// The 4- and 5-clique count phases (unweighted) with the rows split into tiers by how
+// many words they span (row i spans W - floor(i/32)): rows spanning more than 16 words
+// keep the full-warp walk of cta_count_rows, the others run 2, 4 or 8 to a warp
+// (count_rows_grouped) so no lane idles on words past its row's end.
+template <int Q>
+__device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int32_t* pre,
+                                          const int32_t* roff) {
+  const int W = (s + 31) >> 5;
+  // first row spanning at most t words: 32 * (W - t), clamped to [0, s]
+  auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
+  const int r16 = first(16), r8 = first(8), r4 = first(4);
+  uint64_t acc = 0;
+  if (r16 > 0) acc += cta_count_rows<Q, false>(rows, r16, pre, roff, W);
+  acc += count_rows_grouped<Q, 16>(rows, roff, W, r16, r8);
+  acc += count_rows_grouped<Q, 8>(rows, roff, W, r8, r4);
+  acc += count_rows_grouped<Q, 4>(rows, roff, W, r4, s);
   return acc;
 }
 
@@ -522,8 +505,8 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
       }
   }
   if (Q == 3) acc = WGT ? cta_count_rows<3, true>(rows, s, pre, roff)
-                        : cta_count_rows_paired<3>(rows, s, roff);
-  if (Q == 4) acc = cta_count_rows_paired<4>(rows, s, roff);
+                        : cta_count_rows_tiered<3>(rows, s, pre, roff);
+  if (Q == 4) acc = cta_count_rows_tiered<4>(rows, s, pre, roff);
   if constexpr (Q >= 5) acc = cta_count_deep<Q>(rows, s, roff);
   return acc;
 }
