@@ -298,16 +298,69 @@ __device__ uint64_t rows_deep(const uint32_t* rows, const int32_t* roff, uint32_
   }
 }
 
+// rows_deep with G lanes per candidate set (32 / G sets per warp, one per group): group
+// ballots and shuffles, loops while any group has work.
+template <int D, int G>
+__device__ uint64_t rows_deep_grouped(const uint32_t* rows, const int32_t* roff, uint32_t m, int w,
+                                      int qi, int gbase) {
+  if constexpr (D == 1) {
+    return (uint64_t)__popc(m);
+  } else {
+    constexpr unsigned kGMask = (1u << G) - 1u;
+    uint64_t acc = 0;
+    unsigned nz = (__ballot_sync(kFull, m != 0u) >> gbase) & kGMask;
+    while (__any_sync(kFull, nz != 0u)) {
+      const bool had = nz != 0u;
+      const int src = had ? __ffs(nz) - 1 : 0;
+      if (had) nz &= nz - 1;
+      uint32_t bits = __shfl_sync(kFull, m, gbase + src);
+      if (!had) bits = 0u;
+      while (__any_sync(kFull, bits != 0u)) {
+        const bool hb = bits != 0u;
+        const int l = hb ? ((qi + src) << 5) + __ffs(bits) - 1 : 0;
+        if (hb) bits &= bits - 1;
+        const int ql = l >> 5;
+        const uint32_t m2 = (hb && m && w >= ql) ? (m & rows[roff[l] + (w - ql)]) : 0u;
+        acc += rows_deep_grouped<D - 1, G>(rows, roff, m2, w, qi, gbase);
+      }
+    }
+    return acc;
+  }
+}
+
+template <int Q, int G>
+__device__ uint64_t count_deep_grouped(const uint32_t* rows, const int32_t* roff, int W,
+                                       int row_lo, int row_hi) {
+  constexpr int kGroups = 32 / G;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane % G, gbase = lane - sub;
+  uint64_t acc = 0;
+  for (int i0 = row_lo + warp * kGroups; i0 < row_hi; i0 += kCtaWarps * kGroups) {
+    const int i = i0 + lane / G;
+    const bool live = i < row_hi;
+    const int qi = live ? (i >> 5) : 0, nwi = W - qi;
+    const uint32_t wi = (live && sub < nwi) ? rows[roff[i] + sub] : 0u;
+    acc += rows_deep_grouped<Q - 1, G>(rows, roff, wi, qi + sub, qi, gbase);
+  }
+  return acc;
+}
+
+// Q-cliques for Q >= 5, rows tiered by the words they span as in cta_count_rows_tiered.
 template <int Q>
 __device__ uint64_t cta_count_deep(const uint32_t* rows, int s, const int32_t* roff) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = (s + 31) >> 5;
+  auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
+  const int r16 = first(16), r8 = first(8), r4 = first(4);
   uint64_t acc = 0;
-  for (int i = warp; i < s; i += kCtaWarps) {
+  for (int i = warp; i < r16; i += kCtaWarps) {
     const int qi = i >> 5, nwi = W - qi;
     const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
     acc += rows_deep<Q - 1>(rows, roff, wi, qi + lane, qi);
   }
+  acc += count_deep_grouped<Q, 16>(rows, roff, W, r16, r8);
+  acc += count_deep_grouped<Q, 8>(rows, roff, W, r8, r4);
+  acc += count_deep_grouped<Q, 4>(rows, roff, W, r4, s);
   return acc;
 }
 
