@@ -97,13 +97,15 @@ typedef struct {
 
 /* Uploads an undirected CSR (as Graph_V2 loads it) and builds on the GPU the degree
  * orientation (graph_v2.cpp:243-289), the vertex ranking used by the kernels and the
- * task lists.  flags: XGM_BUILD_VALIDATE checks the input on the GPU; XGM_BUILD_CLEAN
- * bits re-run the CSR build over the given entries. */
+ * task lists.  The CSR must be symmetric with sorted rows (as the reference's inputs
+ * are); flags: XGM_BUILD_VALIDATE checks that on the GPU; XGM_BUILD_CLEAN bits re-run
+ * the CSR build over the given entries (symmetrising them). */
 xgm_status xgm_graph_upload(xgm_ctx* ctx, const xgm_csr_host* csr, int flags,
                             xgm_graph** out);
 /* Builds the CSR on the GPU from raw edge samples (the offline step of
  * scripts/graph_format_conversion.py:20-44 plus dedupe and self-loop removal),
- * then the same as xgm_graph_upload.  Ids must lie in [0, num_vertices). */
+ * then the same as xgm_graph_upload.  Ids must lie in [0, num_vertices); without
+ * XGM_BUILD_SYMMETRIZE the samples must already hold both directions of every edge. */
 xgm_status xgm_graph_build_from_edges(xgm_ctx* ctx, int64_t num_vertices,
                                       const int32_t* src, const int32_t* dst,
                                       int64_t num_samples, int flags, xgm_graph** out);

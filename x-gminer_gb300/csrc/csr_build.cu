@@ -140,15 +140,21 @@ __global__ void k_rank_from_sorted(const uint64_t* keys, const int32_t* deg, int
   }
 }
 
-// Warp per original row: rank-space key of every entry, stored at the entry's index.
+// Warp per original row x: its entries y as keys (rank[y] << vb) | rank[x], written at
+// row rank[x] of the rank-space layout, so the key sequence is ordered by rank[x].  By
+// symmetry these are all the rank-space entries with row and column swapped; a stable
+// sort on the row bits alone (bits [vb, 2 vb)) then leaves every row's columns sorted —
+// half the radix passes of sorting (row, column) keys from scratch.
 __global__ void k_rank_entry_keys(const int64_t* rowptr_o, const int32_t* col_o,
-                                  const int32_t* rank, int64_t nv, int vb, uint64_t* keys) {
+                                  const int32_t* rank, const int64_t* rowptr_r, int64_t nv, int vb,
+                                  uint64_t* keys) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < nv; u += warps) {
-    const uint64_t ru = (uint64_t)rank[u] << vb;
-    for (int64_t e = rowptr_o[u] + lane; e < rowptr_o[u + 1]; e += 32)
-      keys[e] = ru | (uint64_t)rank[col_o[e]];
+  for (int64_t x = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; x < nv; x += warps) {
+    const int32_t rx = rank[x];
+    const int64_t src = rowptr_o[x], dst = rowptr_r[rx];
+    for (int64_t e = src + lane; e < rowptr_o[x + 1]; e += 32)
+      keys[dst + (e - src)] = ((uint64_t)rank[col_o[e]] << vb) | (uint64_t)rx;
   }
 }
 
@@ -370,11 +376,11 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
   }
   TRY(scan_excl(degp, g.rowptr, nv, g.rowptr + nv, s));
   if (nv > 0) {
-    k_rank_entry_keys<<<grid_for(nv * 32), kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.rank, nv, vb,
-                                                             keys);
+    k_rank_entry_keys<<<grid_for(nv * 32), kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.rank,
+                                                             g.rowptr, nv, vb, keys);
     TRY(cudaGetLastError());
   }
-  TRY(radix_sort_u64(keys, tmp, ne, 2 * vb, s));
+  TRY(radix_sort_u64(keys, tmp, ne, vb, s, vb));
   if (ne > 0) {
     k_extract_col<<<grid_for(ne), kThreads, 0, s>>>(keys, ne, vb, g.col);
     TRY(cudaGetLastError());

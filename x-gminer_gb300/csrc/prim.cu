@@ -206,14 +206,15 @@ cudaError_t scan_excl(const uint8_t* in, int64_t* out, int64_t n, int64_t* total
   return scan_impl<uint8_t>(in, out, n, total, s);
 }
 
-cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, int64_t n, int bits, cudaStream_t st) {
+cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, int64_t n, int bits, cudaStream_t st,
+                           int shift0) {
   if (n <= 1 || bits <= 0) return cudaSuccess;
   int64_t tiles = (n + kSortTile - 1) / kSortTile;
   int64_t* counts = nullptr;
   cudaError_t e = cudaMallocAsync(&counts, sizeof(int64_t) * kRadix * tiles, st);
   if (e != cudaSuccess) return e;
   uint64_t *a = keys, *b = tmp;
-  for (int shift = 0; shift < bits && e == cudaSuccess; shift += 8) {
+  for (int shift = shift0; shift < shift0 + bits && e == cudaSuccess; shift += 8) {
     k_radix_hist<<<(unsigned)tiles, kSortWarps * 32, 0, st>>>(a, n, shift, counts, tiles);
     e = scan_impl<int64_t>(counts, counts, kRadix * tiles, nullptr, st);
     if (e != cudaSuccess) break;
