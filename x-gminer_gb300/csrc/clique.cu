@@ -488,13 +488,16 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   for (int c = warp; c * 256 < total; c += kCtaWarps) {
     const int kb = c * 256 + lane;
     int i;
-    {  // first segment: largest i with pre[i] <= kb
-      int lo = 0, hi = s;
-      while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (pre[mid] <= kb) lo = mid; else hi = mid;
-      }
-      i = lo;
+    {  // segment of the chunk start (largest i < s with pre[i] <= c * 256): a two-round
+       // 32-way search by the warp (s <= 1024), then each lane steps to its own segment
+      const int k0 = c * 256;
+      const int c1 = lane << 5;
+      const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
+      const int r1 = 31 - __clz(b1);  // b1 has bit 0: pre[0] = 0 <= k0
+      const int c2 = (r1 << 5) + lane;
+      const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
+      i = (r1 << 5) + 31 - __clz(b2);
+      while (i + 1 < s && pre[i + 1] <= kb) ++i;  // stays below s past the end
     }
     int seg_end = pre[i + 1];
     long long seg_base = lb[i] - pre[i];
