@@ -55,8 +55,11 @@ constexpr int kClipMin = 96;  // lists longer than this are clipped at max(S)
 // Wide-warp region (one warp, s <= kWideCap, 4-word rows), aliased over the CTA region
 // once the CTA queues drain; the warp regions follow all wide regions so a warp in the
 // last phase never overlaps a warp still in the wide phase.
+constexpr int kWideBloomWords = 64;  // 2048-bit filter: ~6 % false positives at s = 128
+constexpr int kWarpBloomWords = 32;  // 1024-bit filter: ~3 % false positives at s = 32
+
 struct WideSmem {
-  uint32_t bloom[16];  // 512-bit membership pre-filter of S
+  uint32_t bloom[kWideBloomWords];  // membership pre-filter of S
   long long lb[kWideCap];
   int32_t S[kWideCap];
   int32_t pre[kWideCap + 4];
@@ -67,7 +70,7 @@ constexpr int kOffWarpRegion = kCtaWarps * (int)sizeof(WideSmem);
 
 // Warp region: one per warp (s <= 32, one-word rows).
 struct WarpSmem {
-  uint32_t bloom[8];  // 256-bit membership pre-filter of S
+  uint32_t bloom[kWarpBloomWords];  // membership pre-filter of S
   long long lb[kWarpCap];
   int32_t S[kWarpCap];
   int32_t pre[kWarpCap + 2];
@@ -76,13 +79,14 @@ struct WarpSmem {
 };
 static_assert(kOffWarpRegion + sizeof(WarpSmem) * kCtaWarps <= kCtaSmem, "warp regions fit");
 static_assert(sizeof(WideSmem) % 16 == 0, "wide regions stay 16-byte aligned");
+static_assert(kWarpBloomWords == 32 && kWideBloomWords == 64, "filters are cleared lane-wise");
 
 __device__ __forceinline__ uint32_t hash_slot(int32_t x) {
   return ((uint32_t)x * 2654435761u) >> (32 - 11);  // kHashSize = 2^11
 }
 
 // Bloom bit of x (independent of hash_slot's multiplier): 14 bits for the CTA filter,
-// the top 8 of them for the warp filter.
+// the top 11 / 10 of them for the wide / warp filters.
 __device__ __forceinline__ uint32_t bloom_bit(int32_t x) {
   return ((uint32_t)x * 0x85EBCA6Bu) >> 18;
 }
@@ -668,10 +672,10 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   if (lane == 31) w.pre[32] = inc;
   w.rows[lane] = 0u;
   w.cnt[lane] = 0u;
-  if (lane < 8) w.bloom[lane] = 0u;
+  w.bloom[lane] = 0u;  // kWarpBloomWords == 32
   __syncwarp();
   if (lane < s) {
-    const uint32_t b = bloom_bit(xs) >> 6;  // 8 bits
+    const uint32_t b = bloom_bit(xs) >> 4;  // 10 bits
     atomicOr(&w.bloom[b >> 5], 1u << (b & 31));
   }
   __syncwarp();  // pre[s] is the total: lanes >= s contributed length 0
@@ -705,7 +709,7 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
     for (int t = 0; t < 4; ++t) {
       const int32_t x = xv[t];
       if (x > smax) continue;
-      const uint32_t b = bloom_bit(x) >> 6;
+      const uint32_t b = bloom_bit(x) >> 4;
       if (!((w.bloom[b >> 5] >> (b & 31)) & 1u)) continue;
       const int j = warp_bsearch(w.S, s, x);
       if (j < 0) continue;
@@ -1069,12 +1073,13 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
   if (lane == 31) w.pre[kWideCap] = inc;  // total when s == kWideCap
   for (int x = lane; x < kWideCap * kWideWords; x += 32) w.rows[x] = 0u;
   for (int x = lane; x < kWideCap; x += 32) w.cnt[x] = 0u;
-  if (lane < 16) w.bloom[lane] = 0u;
+  w.bloom[lane] = 0u;  // kWideBloomWords == 64
+  w.bloom[lane + 32] = 0u;
   __syncwarp();
 #pragma unroll
   for (int t = 0; t < 4; ++t)
     if (4 * lane + t < s) {
-      const uint32_t b = bloom_bit(xs[t]) >> 5;  // 9 bits
+      const uint32_t b = bloom_bit(xs[t]) >> 3;  // 11 bits
       atomicOr(&w.bloom[b >> 5], 1u << (b & 31));
     }
   __syncwarp();
@@ -1108,7 +1113,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
     for (int t = 0; t < 4; ++t) {
       const int32_t x = xv[t];
       if (x > smax) continue;
-      const uint32_t b = bloom_bit(x) >> 5;
+      const uint32_t b = bloom_bit(x) >> 3;
       if (!((w.bloom[b >> 5] >> (b & 31)) & 1u)) continue;
       const int j = warp_bsearch(w.S, s, x);
       if (j < 0) continue;
