@@ -476,7 +476,9 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   for (int i = tid; i < s; i += kCtaThreads) {
     const int32_t x = S[i];
     uint32_t slot = hash_slot(x);
-    while (atomicCAS(&hkey[slot], -1, x) != -1) slot = (slot + 1) & (kHashSize - 1);
+    // s <= kCtaCap < kHashSize members: an empty slot always exists
+    for (int probe = 0; probe < kHashSize && atomicCAS(&hkey[slot], -1, x) != -1; ++probe)
+      slot = (slot + 1) & (kHashSize - 1);
     hval[slot] = (uint16_t)i;
     const uint32_t b = bloom_bit(x);
     atomicOr(&bloom[b >> 5], 1u << (b & 31));
