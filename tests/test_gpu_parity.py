@@ -214,3 +214,17 @@ def test_algo_bytes_match_oracle(xgm, ctx, orc):
     rr, rc = relabel_by_degree(rowptr, col)
     assert ctx.algo_bytes(g, "rectangle") == orc.algo_bytes("cycle4", rr, rc)
     assert orc.count("cycle4", rr, rc) == orc.count("cycle4", rowptr, col)
+
+
+@pytest.mark.parametrize("n", [3, 5, 8, 9, 10, 12, 33, 40])
+def test_complete_graphs_every_variant(xgm, ctx, n):
+    # K_n: out-degrees 0..n-1, so every task-size boundary of the variants (GROUP <= 8,
+    # WARP / SEARCH / BUCKET <= 32, WIDE <= 128) is crossed; counts have closed forms
+    from math import comb
+    iu = np.triu_indices(n, 1)
+    g = ctx.graph_from_edges(n, iu[0].astype(np.int32), iu[1].astype(np.int32))
+    for var in xgm.ALL_VARIANTS:
+        for k, pat in ((3, "triangle"), (4, "4-clique"), (5, "5-clique"), (6, "6-clique")):
+            assert ctx.count(g, pat, policy=xgm.SCHED_FIXED, variant=var) == comb(n, k), (n, var, k)
+        assert ctx.count(g, "diamond", policy=xgm.SCHED_FIXED, variant=var) == 6 * comb(n, 4)
+    g.close()
