@@ -150,11 +150,14 @@ xgm_status ensure_c4(xgm_ctx* ctx, const DevGraph& g) {
 
 namespace {
 
-// Large 4-cycle tasks whose wedges are at least a quarter of their id range (v2 < v0)
-// and numerous are counted a group at a time with L2-resident counters
-// (launch_c4_dense_walk); the others stay in the persistent kernel's list.  Reads the
-// large list back, rewrites it without the dense tasks, and launches the groups.
+// Large 4-cycle tasks with at least 1/16 wedge per id of their range (v2 < v0) and
+// numerous wedges are counted a group at a time with L2-resident counters
+// (launch_c4_dense_walk); the others stay in the persistent kernel's list, whose large
+// tasks pay two DRAM atomics per wedge.  A group's counters are reset by a memset of
+// its ranges when they hold fewer than 8 counters per wedge, else by a second walk.
+// Reads the large list back, rewrites it without the grouped tasks, and launches them.
 constexpr int64_t kC4DenseMinWedges = int64_t(1) << 16;
+constexpr int64_t kC4DenseRangePerWedge = 16;
 
 xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
   cudaStream_t s = ctx->stream;
@@ -175,7 +178,8 @@ xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
   std::vector<int32_t> sparse, dense;
   for (int64_t t = 0; t < nl; ++t) {
     const int64_t w = info[2 * t], v0 = list[t];
-    if (w >= kC4DenseMinWedges && 4 * w >= v0 && v0 <= kC4GroupCounters) dense.push_back((int32_t)t);
+    if (w >= kC4DenseMinWedges && kC4DenseRangePerWedge * w >= v0 && v0 <= kC4GroupCounters)
+      dense.push_back((int32_t)t);
     else sparse.push_back(list[t]);
   }
   if (dense.empty()) return XGM_OK;
@@ -183,17 +187,18 @@ xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
   // groups: consecutive dense tasks whose ranges fit the counter array
   std::vector<int32_t> tv0;
   std::vector<int64_t> ttab;
-  struct Group { int64_t t0, m, tab, nseg, ncnt; };
+  struct Group { int64_t t0, m, tab, nseg, ncnt, wedges; };
   std::vector<Group> groups;
   int64_t max_seg = 0;
   for (size_t i = 0; i < dense.size();) {
-    Group gr{(int64_t)tv0.size(), 0, (int64_t)ttab.size(), 0, 0};
+    Group gr{(int64_t)tv0.size(), 0, (int64_t)ttab.size(), 0, 0, 0};
     std::vector<int64_t> tseg{0}, tcnt;
     while (i < dense.size() && (gr.m == 0 || gr.ncnt + list[dense[i]] <= kC4GroupCounters)) {
       const int32_t t = dense[i++];
       tv0.push_back(list[t]);
       tcnt.push_back(gr.ncnt);
       gr.ncnt += list[t];
+      gr.wedges += info[2 * t];
       tseg.push_back(tseg.back() + info[2 * t + 1]);
       ++gr.m;
     }
@@ -246,7 +251,12 @@ xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
     XGM_CUDA_TRY(scan_excl(ctx->c4_seg_pre, ctx->c4_seg_pre, gr.nseg, ctx->c4_seg_pre + gr.nseg, s));
     XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre, ctx->c4_seg_base, ctx->c4_seg_cnt,
                                       gr.nseg, ctx->c4_counters, &ctx->d_sc->count, grid, s));
-    XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_counters, 0, sizeof(uint32_t) * gr.ncnt, s));
+    if (gr.ncnt <= 8 * gr.wedges)
+      XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_counters, 0, sizeof(uint32_t) * gr.ncnt, s));
+    else
+      XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre, ctx->c4_seg_base,
+                                        ctx->c4_seg_cnt, gr.nseg, ctx->c4_counters, nullptr,
+                                        grid, s, true));
     *launches += 3;
   }
   return XGM_OK;

@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(kThreads) k_c4_dense_walk(const int32_t* col,
                                                             const int64_t* seg_base,
                                                             const int32_t* seg_cnt, int64_t nseg,
                                                             uint32_t* counters,
-                                                            unsigned long long* out) {
+                                                            unsigned long long* out, int clear) {
   const int lane = threadIdx.x & 31;
   const int64_t total = seg_pre[nseg];
   const int64_t tile = 32 * kC4TileIters;
@@ -389,7 +389,8 @@ __global__ void __launch_bounds__(kThreads) k_c4_dense_walk(const int32_t* col,
         seg_end = seg_pre[e + 1];
       }
       const int32_t v2 = ldg_i32(col + seg_base[e] + (k - seg_pre[e]));
-      acc += atomicAdd(&counters[(int64_t)seg_cnt[e] + v2], 1u);
+      if (clear) counters[(int64_t)seg_cnt[e] + v2] = 0u;  // second walk: reset what it touched
+      else acc += atomicAdd(&counters[(int64_t)seg_cnt[e] + v2], 1u);
     }
   }
   acc = warp_sum_u64(acc);
@@ -504,9 +505,10 @@ cudaError_t launch_c4_task_info(const GView& g, const int32_t* list, int64_t n,
 cudaError_t launch_c4_dense_walk(const int32_t* col, const int64_t* seg_pre,
                                  const int64_t* seg_base, const int32_t* seg_cnt, int64_t nseg,
                                  uint32_t* counters, unsigned long long* out, int grid,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, bool clear) {
   if (nseg == 0) return cudaSuccess;
-  k_c4_dense_walk<<<grid, kThreads, 0, s>>>(col, seg_pre, seg_base, seg_cnt, nseg, counters, out);
+  k_c4_dense_walk<<<grid, kThreads, 0, s>>>(col, seg_pre, seg_base, seg_cnt, nseg, counters, out,
+                                            clear ? 1 : 0);
   return cudaGetLastError();
 }
 

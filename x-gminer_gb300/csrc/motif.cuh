@@ -37,10 +37,11 @@ constexpr int64_t kC4GroupCounters = int64_t(16) << 20;  // 64 MB of counters pe
 cudaError_t launch_c4_segments(const GView& g, const int32_t* tv0, const int64_t* tseg,
                                const int64_t* tcnt, int m, int64_t nseg, int64_t* seg_base,
                                int64_t* seg_len, int32_t* seg_cnt, cudaStream_t s);
+// clear: walk again and reset the counters the first walk touched (instead of counting)
 cudaError_t launch_c4_dense_walk(const int32_t* col, const int64_t* seg_pre,
                                  const int64_t* seg_base, const int32_t* seg_cnt, int64_t nseg,
                                  uint32_t* counters, unsigned long long* out, int grid,
-                                 cudaStream_t s);
+                                 cudaStream_t s, bool clear = false);
 // wedges and lower degree of each listed task: info[2t] = wedges, info[2t+1] = lower degree
 cudaError_t launch_c4_task_info(const GView& g, const int32_t* list, int64_t n,
                                 const long long* wedges, int64_t* info, cudaStream_t s);
