@@ -188,11 +188,13 @@ xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
   std::vector<int32_t> tv0;
   std::vector<int64_t> ttab;
   struct Group { int64_t t0, m, tab, nseg, ncnt, wedges; };
+  // groups: consecutive tasks whose ranges fit the counter array.  Segments (one per
+  // task and lower neighbour) are numbered across all groups, so one segment launch and
+  // one scan serve every group; a group is a segment range.
   std::vector<Group> groups;
-  int64_t max_seg = 0;
+  std::vector<int64_t> tseg{0}, tcnt;
   for (size_t i = 0; i < dense.size();) {
-    Group gr{(int64_t)tv0.size(), 0, (int64_t)ttab.size(), 0, 0, 0};
-    std::vector<int64_t> tseg{0}, tcnt;
+    Group gr{(int64_t)tv0.size(), 0, tseg.back(), 0, 0, 0};
     while (i < dense.size() && (gr.m == 0 || gr.ncnt + list[dense[i]] <= kC4GroupCounters)) {
       const int32_t t = dense[i++];
       tv0.push_back(list[t]);
@@ -202,27 +204,28 @@ xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
       tseg.push_back(tseg.back() + info[2 * t + 1]);
       ++gr.m;
     }
-    gr.nseg = tseg.back();
-    max_seg = std::max(max_seg, gr.nseg);
-    ttab.insert(ttab.end(), tseg.begin(), tseg.end());
-    ttab.insert(ttab.end(), tcnt.begin(), tcnt.end());
+    gr.nseg = tseg.back() - gr.tab;  // tab: first segment of the group
     groups.push_back(gr);
   }
+  const int64_t nseg_all = tseg.back();
+  const int64_t m_all = (int64_t)tv0.size();
+  ttab = tseg;
+  ttab.insert(ttab.end(), tcnt.begin(), tcnt.end());
   if (!ctx->c4_counters) {
     XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_counters, sizeof(uint32_t) * kC4GroupCounters, s));
     XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_counters, 0, sizeof(uint32_t) * kC4GroupCounters, s));
   }
-  if (ctx->c4_seg_cap < max_seg) {
+  if (ctx->c4_seg_cap < nseg_all) {
     void* ps[] = {ctx->c4_seg_base, ctx->c4_seg_pre, ctx->c4_seg_cnt};
     for (void* p : ps)
       if (p) cudaFreeAsync(p, s);
     ctx->c4_seg_cap = 0;
-    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_base, sizeof(int64_t) * max_seg, s));
-    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_pre, sizeof(int64_t) * (max_seg + 1), s));
-    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_cnt, sizeof(int32_t) * max_seg, s));
-    ctx->c4_seg_cap = max_seg;
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_base, sizeof(int64_t) * nseg_all, s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_pre, sizeof(int64_t) * (nseg_all + 1), s));
+    XGM_CUDA_TRY(cudaMallocAsync(&ctx->c4_seg_cnt, sizeof(int32_t) * nseg_all, s));
+    ctx->c4_seg_cap = nseg_all;
   }
-  const int64_t need = std::max<int64_t>((int64_t)tv0.size(), (int64_t)ttab.size());
+  const int64_t need = std::max<int64_t>(m_all, (int64_t)ttab.size());
   if (ctx->c4_task_cap < need) {
     if (ctx->c4_tv0) cudaFreeAsync(ctx->c4_tv0, s);
     if (ctx->c4_ttab) cudaFreeAsync(ctx->c4_ttab, s);
@@ -236,28 +239,31 @@ xgm_status cycle4_dense_groups(xgm_ctx* ctx, const DevGraph& g, int* launches) {
   if (ns) XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_large, sparse.data(), sizeof(int32_t) * ns,
                                       cudaMemcpyHostToDevice, s));
   XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_n, &ns, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-  XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_tv0, tv0.data(), sizeof(int32_t) * tv0.size(),
+  XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_tv0, tv0.data(), sizeof(int32_t) * m_all,
                                cudaMemcpyHostToDevice, s));
   XGM_CUDA_TRY(cudaMemcpyAsync(ctx->c4_ttab, ttab.data(), sizeof(int64_t) * ttab.size(),
                                cudaMemcpyHostToDevice, s));
   XGM_CUDA_TRY(cudaStreamSynchronize(s));  // host tables are freed on return
   const GView view = g.view();
   const int grid = 4 * ctx->num_sms;
+  XGM_CUDA_TRY(launch_c4_segments(view, ctx->c4_tv0, ctx->c4_ttab, ctx->c4_ttab + m_all + 1,
+                                  (int)m_all, nseg_all, ctx->c4_seg_base, ctx->c4_seg_pre,
+                                  ctx->c4_seg_cnt, s));
+  XGM_CUDA_TRY(scan_excl(ctx->c4_seg_pre, ctx->c4_seg_pre, nseg_all, ctx->c4_seg_pre + nseg_all,
+                         s));
+  *launches += 2;
   for (const Group& gr : groups) {
-    const int64_t* tseg = ctx->c4_ttab + gr.tab;
-    const int64_t* tcnt = tseg + gr.m + 1;
-    XGM_CUDA_TRY(launch_c4_segments(view, ctx->c4_tv0 + gr.t0, tseg, tcnt, (int)gr.m, gr.nseg,
-                                    ctx->c4_seg_base, ctx->c4_seg_pre, ctx->c4_seg_cnt, s));
-    XGM_CUDA_TRY(scan_excl(ctx->c4_seg_pre, ctx->c4_seg_pre, gr.nseg, ctx->c4_seg_pre + gr.nseg, s));
-    XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre, ctx->c4_seg_base, ctx->c4_seg_cnt,
-                                      gr.nseg, ctx->c4_counters, &ctx->d_sc->count, grid, s));
+    const int64_t e0 = gr.tab;
+    XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre + e0, ctx->c4_seg_base + e0,
+                                      ctx->c4_seg_cnt + e0, gr.nseg, ctx->c4_counters,
+                                      &ctx->d_sc->count, grid, s));
     if (gr.ncnt <= 8 * gr.wedges)
       XGM_CUDA_TRY(cudaMemsetAsync(ctx->c4_counters, 0, sizeof(uint32_t) * gr.ncnt, s));
     else
-      XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre, ctx->c4_seg_base,
-                                        ctx->c4_seg_cnt, gr.nseg, ctx->c4_counters, nullptr,
+      XGM_CUDA_TRY(launch_c4_dense_walk(g.col, ctx->c4_seg_pre + e0, ctx->c4_seg_base + e0,
+                                        ctx->c4_seg_cnt + e0, gr.nseg, ctx->c4_counters, nullptr,
                                         grid, s, true));
-    *launches += 3;
+    *launches += 2;
   }
   return XGM_OK;
 }

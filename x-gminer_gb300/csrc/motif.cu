@@ -363,7 +363,10 @@ __global__ void __launch_bounds__(kThreads) k_c4_dense_walk(const int32_t* col,
                                                             uint32_t* counters,
                                                             unsigned long long* out, int clear) {
   const int lane = threadIdx.x & 31;
-  const int64_t total = seg_pre[nseg];
+  // seg_pre holds a prefix over a larger segment set: wedges of this call are
+  // [seg_pre[0], seg_pre[nseg]), indexed here from 0
+  const int64_t base = seg_pre[0];
+  const int64_t total = seg_pre[nseg] - base;
   const int64_t tile = 32 * kC4TileIters;
   const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
   unsigned long long acc = 0;
@@ -372,23 +375,23 @@ __global__ void __launch_bounds__(kThreads) k_c4_dense_walk(const int32_t* col,
     // segment of the tile's first wedge (lane 0 searches, the warp shares it)
     int64_t e = 0;
     if (lane == 0) {
-      int64_t lo = 0, hi = nseg;  // largest e with seg_pre[e] <= t0
+      int64_t lo = 0, hi = nseg;  // largest e with seg_pre[e] - base <= t0
       while (hi - lo > 1) {
         const int64_t mid = (lo + hi) >> 1;
-        if (seg_pre[mid] <= t0) lo = mid; else hi = mid;
+        if (seg_pre[mid] - base <= t0) lo = mid; else hi = mid;
       }
       e = lo;
     }
     e = __shfl_sync(kFull, e, 0);
-    int64_t seg_end = seg_pre[e + 1];
+    int64_t seg_end = seg_pre[e + 1] - base;
     for (int j = 0; j < kC4TileIters; ++j) {
       const int64_t k = t0 + j * 32 + lane;
       if (k >= total) break;
       while (k >= seg_end) {
         ++e;
-        seg_end = seg_pre[e + 1];
+        seg_end = seg_pre[e + 1] - base;
       }
-      const int32_t v2 = ldg_i32(col + seg_base[e] + (k - seg_pre[e]));
+      const int32_t v2 = ldg_i32(col + seg_base[e] + (k - (seg_pre[e] - base)));
       if (clear) counters[(int64_t)seg_cnt[e] + v2] = 0u;  // second walk: reset what it touched
       else acc += atomicAdd(&counters[(int64_t)seg_cnt[e] + v2], 1u);
     }
