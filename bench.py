@@ -268,7 +268,7 @@ def engine_arm(args, dist: Dist) -> None:
     value = total_matches / (ms_per_step / 1e3)
     kern_ms = statistics.mean(kern)
 
-    # plain heuristic schedule on the same graph and steps (the learned schedule's judge)
+    # plain heuristic schedule on the same graph and steps (the baseline of the learned schedule)
     plain = None
     if policy == xgm.SCHED_LEARNED:
         run(1, policy=xgm.SCHED_HEURISTIC)
