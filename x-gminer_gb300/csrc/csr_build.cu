@@ -140,21 +140,22 @@ __global__ void k_rank_from_sorted(const uint64_t* keys, const int32_t* deg, int
   }
 }
 
-// Warp per original row x: its entries y as keys (rank[y] << vb) | rank[x], written at
-// row rank[x] of the rank-space layout, so the key sequence is ordered by rank[x].  By
-// symmetry these are all the rank-space entries with row and column swapped; a stable
-// sort on the row bits alone (bits [vb, 2 vb)) then leaves every row's columns sorted —
-// half the radix passes of sorting (row, column) keys from scratch.
+// Warp per rank-space row r (original row x = perm[r]): the entries y of x as keys
+// (rank[y] << vb) | r, written at row r of the rank-space layout (sequential writes
+// across the grid), so the key sequence is ordered by r.  By symmetry these are all the
+// rank-space entries with row and column swapped; a stable sort on the row bits alone
+// (bits [vb, 2 vb)) then leaves every row's columns sorted — half the radix passes of
+// sorting (row, column) keys from scratch.
 __global__ void k_rank_entry_keys(const int64_t* rowptr_o, const int32_t* col_o,
-                                  const int32_t* rank, const int64_t* rowptr_r, int64_t nv, int vb,
-                                  uint64_t* keys) {
+                                  const int32_t* rank, const int32_t* perm,
+                                  const int64_t* rowptr_r, int64_t nv, int vb, uint64_t* keys) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t x = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; x < nv; x += warps) {
-    const int32_t rx = rank[x];
-    const int64_t src = rowptr_o[x], dst = rowptr_r[rx];
-    for (int64_t e = src + lane; e < rowptr_o[x + 1]; e += 32)
-      keys[dst + (e - src)] = ((uint64_t)rank[col_o[e]] << vb) | (uint64_t)rx;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < nv; r += warps) {
+    const int32_t x = perm[r];
+    const int64_t src = rowptr_o[x], dst = rowptr_r[r], len = rowptr_r[r + 1] - dst;
+    for (int64_t j = lane; j < len; j += 32)
+      keys[dst + j] = ((uint64_t)rank[col_o[src + j]] << vb) | (uint64_t)r;
   }
 }
 
@@ -368,7 +369,9 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
     k_rank_keys<<<grid_for(nv), kThreads, 0, s>>>(deg, group, nv, vb, db, keys);
     TRY(cudaGetLastError());
   }
-  TRY(radix_sort_u64(keys, tmp, nv, vb + db + gb, s));
+  // keys start in id order, so a stable sort on the (group, degree) bits alone gives
+  // (group, degree, id) order
+  TRY(radix_sort_u64(keys, tmp, nv, db + gb, s, vb));
   if (nv > 0) {
     k_rank_from_sorted<<<grid_for(nv), kThreads, 0, s>>>(keys, deg, nv, vb, db, group != nullptr,
                                                          g.perm, g.rank, degp, g.gid);
@@ -377,7 +380,7 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
   TRY(scan_excl(degp, g.rowptr, nv, g.rowptr + nv, s));
   if (nv > 0) {
     k_rank_entry_keys<<<grid_for(nv * 32), kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.rank,
-                                                             g.rowptr, nv, vb, keys);
+                                                             g.perm, g.rowptr, nv, vb, keys);
     TRY(cudaGetLastError());
   }
   TRY(radix_sort_u64(keys, tmp, ne, vb, s, vb));
