@@ -92,8 +92,9 @@ xgm_status count_motifs(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched&
 xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
                          int* n_kernels);
 void motif_buffers_free(xgm_ctx* ctx);
+// k_feat: clique size the learned model's features describe (default k).
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
-                         cudaStream_t s);
+                         cudaStream_t s, int k_feat = 0);
 bool sched_may_bucket(const xgm_sched& sp);  // the policy can assign the BUCKET variant
 int ensure_clique_grid(xgm_ctx* ctx);
 int match_pattern(const xgm_plan_desc* d);  // builtin id, 0 unsupported, -1 malformed

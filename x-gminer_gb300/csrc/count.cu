@@ -63,7 +63,7 @@ bool sched_may_bucket(const xgm_sched& sp) {
 // when the policy can pick BUCKET (outside stream capture: callers that capture call
 // ensure_bucket_index before they begin).
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
-                         cudaStream_t s) {
+                         cudaStream_t s, int k_feat) {
   bool order = false;
   if (sp.policy == XGM_SCHED_LEARNED) {
     if (!sp.model) {
@@ -72,7 +72,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
     }
     order = sp.order_by_cost != 0;
     XGM_CUDA_TRY(ensure_bucket_index(g, s));  // the model may pick BUCKET
-    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, order, sp.margin, s));
+    XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, order, sp.margin, s, k_feat));
   } else if (sp.policy == XGM_SCHED_TUNED) {
     if (!sp.table) {
       set_thread_error("XGM_SCHED_TUNED needs a variant table (xgm_sched.table)");

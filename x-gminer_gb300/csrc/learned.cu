@@ -97,8 +97,8 @@ __device__ __forceinline__ void mlp_variants(const float* P, const float* f, con
   }
 }
 
-__global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* var, float* cost,
-                                   int need_cost, float margin) {
+__global__ void k_classify_learned(GView g, int k, int k_feat, const __half* wh, uint8_t* var,
+                                   float* cost, int need_cost, float margin) {
   __shared__ float P[kParams];
   load_params(wh, P);
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < g.nv;
@@ -131,7 +131,7 @@ __global__ void k_classify_learned(GView g, int k, const __half* wh, uint8_t* va
       continue;
     }
     float f[kFeat];
-    task_features(g, (int32_t)r, k, f);
+    task_features(g, (int32_t)r, k_feat, f);
     float pred[XGM_NUM_VARIANTS];
     mlp_variants(P, f, cand, pred);
     for (int v = 0; v < XGM_NUM_VARIANTS; ++v)
@@ -269,9 +269,10 @@ int clique_k(int pattern) {
 }  // namespace
 
 cudaError_t classify_learned(const DevGraph& g, int k, const xgm_model& m, TaskBuf& tb,
-                             bool need_cost, float margin, cudaStream_t s) {
+                             bool need_cost, float margin, cudaStream_t s, int k_feat) {
   if (g.nv == 0) return cudaSuccess;
-  k_classify_learned<<<grid_for(g.nv), kThreads, 0, s>>>(g.view(), k, m.wh, tb.var, tb.cost,
+  k_classify_learned<<<grid_for(g.nv), kThreads, 0, s>>>(g.view(), k, k_feat > 0 ? k_feat : k,
+                                                         m.wh, tb.var, tb.cost,
                                                          need_cost ? 1 : 0,
                                                          margin > 0.0f ? margin : kLearnedMargin);
   return cudaGetLastError();

@@ -32,8 +32,9 @@ namespace xgm {
 // Learned schedule: per vertex task the features, the MLP's predicted log2 warp-cycles
 // for each variant the task fits, the chosen variant (tb.var) and its cost (tb.cost).
 // Without need_cost (no cost ordering) tasks that fit one variant skip the model.
-// margin <= 0: the default margin.
+// margin <= 0: the default margin.  k sets which tasks are skipped (out-degree < k-1);
+// k_feat (default k) is the clique size the features describe.
 cudaError_t classify_learned(const DevGraph& g, int k, const xgm_model& m, TaskBuf& tb,
-                             bool need_cost, float margin, cudaStream_t s);
+                             bool need_cost, float margin, cudaStream_t s, int k_feat = 0);
 
 }  // namespace xgm
