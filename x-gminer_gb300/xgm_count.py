@@ -21,9 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 xgm = importlib.import_module("x-gminer_gb300")
 
-# GLUMIN patternIDs of the supported patterns (xgminer/include/glumin.h:34-46 maps
-# patternID - 16 to the GLUMIN pattern; 4/5-clique are P4/P5)
-PATTERN_IDS = {20: "4-clique", 21: "5-clique"}
+# xgminer patternIDs of the supported GLUMIN patterns (xgminer/include/glumin.h:34-39
+# maps patternID - 16 to GLUMIN's P-number): P1-P5, P23 (6-clique), P24 (7-clique)
+PATTERN_IDS = {17: "P1", 18: "P2", 19: "P3", 20: "P4", 21: "P5", 39: "P23", 40: "P24"}
 
 
 def main() -> None:
@@ -33,11 +33,15 @@ def main() -> None:
     src.add_argument("--rmat", type=int, metavar="SCALE", help="seeded R-MAT, edge factor 16")
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--pattern", default="4-clique")
-    ap.add_argument("--patternID", type=int, help="reference pattern id (20: 4-clique, 21: 5-clique)")
+    ap.add_argument("--patternID", type=int,
+                    help="xgminer pattern id: 17-21 = GLUMIN P1-P5, 39 / 40 = P23 / P24")
     ap.add_argument("--policy", choices=["heuristic", "learned"], default="heuristic")
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
-    pattern = PATTERN_IDS.get(args.patternID, args.pattern) if args.patternID else args.pattern
+    if args.patternID and args.patternID not in PATTERN_IDS:
+        raise SystemExit(f"patternID {args.patternID} is not a supported plan "
+                         f"(supported: {sorted(PATTERN_IDS)})")
+    pattern = PATTERN_IDS[args.patternID] if args.patternID else args.pattern
     ctx = xgm.Context(0)
     if args.graph:
         g = ctx.load_graph(args.graph)
@@ -58,7 +62,7 @@ def main() -> None:
               "order_by_cost": int(spec.get("order_by_cost", 1)),
               "margin": float(spec.get("margin", 0.0))}
     for _ in range(args.repeat):
-        count, st = ctx.count(g, pattern, with_stats=True, **kw)
+        count, st = ctx.count(g, xgm.plan(pattern), with_stats=True, **kw)
         print(json.dumps({"pattern": pattern, "count": count, "graph": g.info(), **st}))
     ctx.close()
 
