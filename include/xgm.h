@@ -138,12 +138,20 @@ typedef enum {
   XGM_PATTERN_STAR3 = 8,            /* K_{1,3}; GLUMIN 4-star.yml (P1) */
   XGM_PATTERN_PATH4 = 9,            /* 3-edge path; GLUMIN 4-path.yml */
   XGM_PATTERN_CLIQUE6 = 10,         /* GLUMIN P23 (clique6_warp_edge*.cuh) */
-  XGM_PATTERN_CLIQUE7 = 11          /* GLUMIN P24 (clique7_warp_edge*.cuh) */
+  XGM_PATTERN_CLIQUE7 = 11,         /* GLUMIN P24 (clique7_warp_edge*.cuh) */
+  XGM_PATTERN_PROGRAM = 12          /* set-operation program: GLUMIN's P6..P22, or a
+                                       compiled connected pattern of up to 5 vertices */
 } xgm_pattern;
 
+/* Words of a set-operation program in flat form (xgm_plan_program). */
+#define XGM_PROGRAM_WORDS 124
+
 typedef struct {
-  int builtin;            /* xgm_pattern, or 0 to match `adj` */
-  int num_vertices;       /* pattern size when builtin == 0 (3..5) */
+  int builtin;            /* xgm_pattern, or 0 to match `adj`: a builtin when one has this
+                             shape, else a compiled set-operation program (connected
+                             patterns of up to 5 vertices, each occurrence counted once);
+                             XGM_PATTERN_PROGRAM compiles `adj` even where a builtin exists */
+  int num_vertices;       /* pattern size when builtin == 0 (3..5; 6 and 7 for cliques) */
   uint8_t adj[8][8];      /* pattern adjacency when builtin == 0 */
   int induced;            /* 0: edge-induced; 1: vertex-induced (the non-clique motifs are
                              derived from edge-induced counts, the 4-clique count and the
@@ -159,14 +167,26 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* desc, xgm_plan** 
  * pattern ids (codes/GLUMIN/src/G2Miner/main.cc:13-60), vertex-induced: "P1" (4-star),
  * "P2" (4-diamond, reported as GLUMIN does: each diamond once per direction of its
  * shared edge, i.e. twice), "P3" (4-tailed-triangle), "P4"/"P5"/"P23"/"P24"
- * (4/5/6/7-clique). */
+ * (4/5/6/7-clique), and "P6".."P22", GLUMIN's generated 5-vertex plans
+ * (G2Miner/gpu_GM_LUT_kernels/GM_kernels/P*-GM.yml.cuh) run as set-operation
+ * programs with GLUMIN's own set semantics: the count is the reference's, including
+ * the embeddings with a repeated vertex that P12, P13, P19 and P22 admit.  The
+ * 5-vertex .yml names ("5-cycle", "5-double-triangle", "5-house", "5-path",
+ * "5-solid-house", "5-star", "5-tailed-square") give compiled edge-induced programs. */
 xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out);
 /* Plan from a GLUMIN pattern description, the text of one of
  * codes/GLUMIN/codegen/codegen/patterns/*.yml: its `edges: [AB, AC, ...]` list (vertices
- * named by letters) is matched against the builtins.  GLUMIN's plans count
- * vertex-induced embeddings (pass induced = 1 for the same meaning). */
+ * named by letters) is matched against the builtins, else compiled to a set-operation
+ * program (up to 5 vertices).  GLUMIN's plans count vertex-induced embeddings (pass
+ * induced = 1 for the same meaning). */
 xgm_status xgm_plan_from_spec(xgm_ctx* ctx, const char* spec, int induced, xgm_plan** out);
 int xgm_plan_pattern(const xgm_plan* p);
+/* A program plan's flat form: [1, k, slots, flat, v1 < v0 task filter, ops per level
+ * (3), v2 / v3 candidate operands, then 19 operations of six words (out slot, kind 0 intersect /
+ * 1 difference / 2 filter, operand a, operand b, bound mask, exclusion mask); an
+ * operand >= 16 is N(v_(operand-16)), below it a slot].  Returns XGM_PROGRAM_WORDS
+ * (writing words[] when n_words is at least that), 0 for a builtin plan. */
+int xgm_plan_program(const xgm_plan* p, int32_t* words, int n_words);
 int xgm_plan_induced(const xgm_plan* p);
 void xgm_plan_destroy(xgm_plan* p);
 

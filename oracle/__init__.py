@@ -82,6 +82,12 @@ def lib():
         L.orc_motif.argtypes = [C.c_int, I64, P, P, I64, P]
         L.orc_algo_bytes.restype = U64
         L.orc_algo_bytes.argtypes = [C.c_int, I64, P, P, I64]
+        L.orc_glumin5.restype = C.c_int
+        L.orc_glumin5.argtypes = [C.c_int, I64, P, P, I64, P]
+        L.orc_setprog.restype = C.c_int
+        L.orc_setprog.argtypes = [P, C.c_int, I64, P, P, I64, P]
+        L.orc_occurrences.restype = C.c_int
+        L.orc_occurrences.argtypes = [C.c_int, P, C.c_int, I64, P, P, P]
         _lib = L
     return _lib
 
@@ -162,6 +168,42 @@ def motif(k: int, rowptr: np.ndarray, col: np.ndarray) -> list:
     return [int(x) for x in out[: 2 if k == 3 else 6]]
 
 
+def glumin5(pid: int, rowptr: np.ndarray, col: np.ndarray) -> int:
+    """GLUMIN's P<pid> count (6 <= pid <= 22) on the undirected CSR: the generated plan
+    restated as CPU loops, GLUMIN's set semantics included."""
+    nv, rowptr, col = _args(rowptr, col)
+    md = int(np.diff(rowptr).max()) if nv else 0
+    out = np.zeros(1, dtype=np.uint64)
+    if lib().orc_glumin5(pid, nv, rowptr.ctypes.data, col.ctypes.data, md, out.ctypes.data) != 0:
+        raise ValueError("GLUMIN 5-vertex plans are P6 .. P22")
+    return int(out[0])
+
+
+def program(words, rowptr: np.ndarray, col: np.ndarray) -> int:
+    """Runs an engine set-operation program (xgm_plan_program words) on the CPU."""
+    w = np.ascontiguousarray(words, dtype=np.int32)
+    nv, rowptr, col = _args(rowptr, col)
+    md = int(np.diff(rowptr).max()) if nv else 0
+    out = np.zeros(1, dtype=np.uint64)
+    if lib().orc_setprog(w.ctypes.data, len(w), nv, rowptr.ctypes.data, col.ctypes.data, md,
+                         out.ctypes.data) != 0:
+        raise ValueError("malformed program words")
+    return int(out[0])
+
+
+def occurrences(adj, induced: bool, rowptr: np.ndarray, col: np.ndarray) -> int:
+    """Occurrences of a connected pattern (k x k 0/1 adjacency, k <= 6) by brute force:
+    injective embeddings over the automorphism count.  Small graphs only."""
+    a = np.ascontiguousarray(np.asarray(adj, dtype=np.uint8))
+    k = a.shape[0]
+    nv, rowptr, col = _args(rowptr, col)
+    out = np.zeros(1, dtype=np.uint64)
+    if lib().orc_occurrences(k, a.ctypes.data, 1 if induced else 0, nv, rowptr.ctypes.data,
+                             col.ctypes.data, out.ctypes.data) != 0:
+        raise ValueError("pattern must be connected, 2 .. 6 vertices")
+    return int(out[0])
+
+
 def algo_bytes(kind: str, rowptr: np.ndarray, col: np.ndarray) -> int:
     nv, rowptr, col = _args(rowptr, col)
     md = int(np.max(np.diff(rowptr))) if nv else 0
@@ -210,6 +252,27 @@ def run_ref_motif(k: int, prefix: str, threads_: int = 0) -> list:
     if sorted(found) != list(range(n)):
         raise RuntimeError("unexpected reference output:\n" + r.stdout[-800:])
     return [found[i] for i in range(n)]
+
+
+# GLUMIN's 5-vertex CPU plans (codes/GLUMIN/src/pattern/cpu_serials.cc:57-81): the
+# selector of the list form (BS_vertex_*, cpu_kernels/*-BSE.yml.h) and of the LUT form
+# (LUT_*, *-BSV.yml.h) for the P id whose generated GPU plan each restates.
+GLUMIN5_CPU = {10: (4, 3), 15: (6, 5), 7: (8, 7), 13: (10, 9), 20: (12, 11)}
+
+
+def run_ref_glumin5(pid: int, prefix: str, lut: bool = False) -> Tuple[int, float]:
+    """Runs GLUMIN's CPU plan for P<pid> (7, 10, 13, 15, 20) on <prefix>.* graph files;
+    returns (count, seconds)."""
+    sel = GLUMIN5_CPU[pid][1 if lut else 0]
+    cmd = [os.path.join(REF_DIR, "glumin_pattern_cpu"), prefix, str(sel)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd[0]} failed: {r.stderr[-500:]}")
+    m = re.search(r"pattern 0: (\d+)", r.stdout)
+    t = re.search(r"runtime \[omp_base\] = ([0-9.eE+-]+)", r.stdout)
+    if not m:
+        raise RuntimeError("unexpected reference output:\n" + r.stdout[-800:])
+    return int(m.group(1)), float(t.group(1)) if t else float("nan")
 
 
 def write_graph(prefix: str, rowptr: np.ndarray, col: np.ndarray) -> None:

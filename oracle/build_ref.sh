@@ -9,6 +9,8 @@
 #   clique_omp_base <- src/common/{graph,VertexSet}.cc src/clique/{main,omp_base}.cc
 #   count_omp_base  <- + src/common/{pattern,intersect}.cc src/count/{main,omp_base}.cc
 #   motif_omp_formula <- src/common/{graph,VertexSet}.cc src/motif/{main,omp_formula}.cc
+#   glumin_pattern_cpu <- GLUMIN's codes/GLUMIN/src/common/{graph,VertexSet}.cc
+#                         src/pattern/{main,cpu_serials}.cc (the 5-vertex CPU plans)
 #
 # count's intersect.cc uses x86 AVX2 intrinsics and rectangle.h misses <array>
 # under gcc 13, hence -mavx2 and -include array for that binary only; on hosts
@@ -29,13 +31,20 @@ rc=0
 build() {  # name, extra args...
   local name="$1"; shift
   if [ -x "$OUT/$name" ] && [ "$OUT/$name" -nt "$0" ]; then return 0; fi
-  "$CXX" $FLAGS "$@" -o "$OUT/$name" || { echo "build_ref: $name failed"; rc=1; }
+  "$CXX" ${BFLAGS:-$FLAGS} "$@" -o "$OUT/$name" || { echo "build_ref: $name failed"; rc=1; }
 }
 build tc_omp_base $COMMON "$GM/src/triangle/main.cc" "$GM/src/triangle/omp_base.cc" &
 build clique_omp_base -I"$GM/src/clique/cpu_kernels" $COMMON "$GM/src/clique/main.cc" \
   "$GM/src/clique/omp_base.cc" &
 build motif_omp_formula -I"$GM/src/motif/cpu_kernels" $COMMON "$GM/src/motif/main.cc" \
   "$GM/src/motif/omp_formula.cc" &
+GL="$REF/codes/GLUMIN"
+if [ -d "$GL/src/pattern" ]; then
+  BFLAGS="-O3 -fopenmp -std=c++17 -w" build glumin_pattern_cpu -I"$GL/include" \
+    -I"$GL/src/pattern/cpu_kernels" \
+    "$GL/src/common/graph.cc" "$GL/src/common/VertexSet.cc" "$GL/src/pattern/cpu_serials.cc" \
+    "$GL/src/pattern/main.cc" &
+fi
 if [ "$(uname -m)" = "x86_64" ]; then
   build count_omp_base -mavx2 -include array -I"$GM/src/count/cpu_kernels" $COMMON \
     "$GM/src/common/pattern.cc" "$GM/src/common/intersect.cc" "$GM/src/count/main.cc" \

@@ -525,3 +525,429 @@ uint64_t orc_algo_bytes(int kind, int64_t nv, const int64_t* rowptr, const int32
 #undef DEG
   return bytes;
 }
+
+/* ------------------------------------------------ GLUMIN 5-vertex plans (P6-P22)
+ * GLUMIN's generated pattern kernels, codes/GLUMIN/src/G2Miner/gpu_GM_LUT_kernels/
+ * GM_kernels/P<id>-GM.yml.cuh, restated as CPU loops.  A task is every directed
+ * entry (v0, v1) of the undirected CSR (init_edgelist without symmetry breaking,
+ * codes/GLUMIN/src/common/graph.cc:296-340).  The set operations are GLUMIN's
+ * (codegen/include/gpu_kernels/codegen_utils.cuh:256-300, set_intersect.cuh,
+ * set_difference.cuh:44-86,176-232): the elements of the first sorted list below
+ * `up` that are (intersect) or are not (difference) in the second.  Nothing skips
+ * an already matched vertex, so a difference can hand one back (N(v1) \ N(v0) holds
+ * v0); the reference counts those embeddings and so does this restatement. */
+#define NOB INT32_MAX
+static eid_t g_isect(const vid_t* a, eid_t na, const vid_t* b, eid_t nb, vid_t up, vid_t* out) {
+  eid_t n = 0, r = 0;
+  for (eid_t l = 0; l < na && a[l] < up; l++) {
+    while (r < nb && b[r] < a[l]) r++;
+    if (r < nb && b[r] == a[l]) out[n++] = a[l];
+  }
+  return n;
+}
+static eid_t g_diff(const vid_t* a, eid_t na, const vid_t* b, eid_t nb, vid_t up, vid_t* out) {
+  eid_t n = 0, r = 0;
+  for (eid_t l = 0; l < na && a[l] < up; l++) {
+    while (r < nb && b[r] < a[l]) r++;
+    if (r >= nb || b[r] != a[l]) out[n++] = a[l];
+  }
+  return n;
+}
+static uint64_t g_isect_n(const vid_t* a, eid_t na, const vid_t* b, eid_t nb, vid_t up) {
+  uint64_t n = 0;
+  eid_t r = 0;
+  for (eid_t l = 0; l < na && a[l] < up; l++) {
+    while (r < nb && b[r] < a[l]) r++;
+    if (r < nb && b[r] == a[l]) n++;
+  }
+  return n;
+}
+static uint64_t g_diff_n(const vid_t* a, eid_t na, const vid_t* b, eid_t nb, vid_t up) {
+  uint64_t n = 0;
+  eid_t r = 0;
+  for (eid_t l = 0; l < na && a[l] < up; l++) {
+    while (r < nb && b[r] < a[l]) r++;
+    if (r >= nb || b[r] != a[l]) n++;
+  }
+  return n;
+}
+
+#define NB(v) (col + rowptr[v]), (rowptr[(v) + 1] - rowptr[v])
+#define SL(i) s[i], n[i]
+
+/* One task (v0, v1) of plan P<pid>; s[0..4] are slot buffers of max-degree size. */
+static uint64_t glumin5_task(int pid, const int64_t* rowptr, const int32_t* col, vid_t v0,
+                             vid_t v1, vid_t** s) {
+  eid_t n[5] = {0, 0, 0, 0, 0};
+  uint64_t c = 0;
+  switch (pid) {
+    case 6: /* P6-GM.yml.cuh */
+      n[0] = g_isect(NB(v0), NB(v1), v1, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        n[2] = g_diff(SL(1), NB(v2), v1, s[2]);
+        for (eid_t j = 0; j < n[2]; j++) c += g_isect_n(SL(2), NB(s[2][j]), s[2][j]);
+      }
+      break;
+    case 7: /* P7-GM.yml.cuh */
+    case 8: /* P8-GM.yml.cuh */
+      n[0] = g_diff(NB(v1), NB(v0), NOB, s[0]);
+      n[1] = g_isect(NB(v0), NB(v1), NOB, s[1]);
+      n[2] = g_diff(NB(v0), NB(v1), NOB, s[2]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        n[3] = g_diff(SL(1), NB(v2), NOB, s[3]);
+        n[4] = pid == 7 ? g_diff(SL(2), NB(v2), NOB, s[4]) : g_isect(SL(2), NB(v2), NOB, s[4]);
+        for (eid_t j = 0; j < n[3]; j++) c += g_diff_n(SL(4), NB(s[3][j]), NOB);
+      }
+      break;
+    case 9: /* P9-GM.yml.cuh */
+    case 13: /* P13-GM.yml.cuh */
+      n[0] = g_isect(NB(v0), NB(v1), NOB, s[0]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        n[1] = g_diff(SL(0), NB(s[0][i]), NOB, s[1]);
+        for (eid_t j = 0; j < n[1]; j++) {
+          vid_t v3 = s[1][j];
+          c += pid == 9 ? g_isect_n(SL(1), NB(v3), v3) : g_diff_n(SL(1), NB(v3), NOB);
+        }
+      }
+      break;
+    case 10: /* P10-GM.yml.cuh */
+      n[0] = g_diff(NB(v0), NB(v1), v1, s[0]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        n[1] = g_diff(SL(0), NB(v2), v2, s[1]);
+        for (eid_t j = 0; j < n[1]; j++) c += g_diff_n(SL(1), NB(s[1][j]), s[1][j]);
+      }
+      break;
+    case 11: /* P11-GM.yml.cuh */
+      n[0] = g_diff(NB(v1), NB(v0), NOB, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        n[2] = g_diff(SL(1), NB(v2), NOB, s[2]);
+        n[3] = g_isect(SL(1), NB(v2), NOB, s[3]);
+        for (eid_t j = 0; j < n[2]; j++) c += g_diff_n(SL(3), NB(s[2][j]), v1);
+      }
+      break;
+    case 12: /* P12-GM.yml.cuh */
+      n[0] = g_diff(NB(v1), NB(v0), v0, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        n[2] = g_isect(SL(1), NB(s[0][i]), NOB, s[2]);
+        for (eid_t j = 0; j < n[2]; j++) c += g_diff_n(SL(2), NB(s[2][j]), NOB);
+      }
+      break;
+    case 14: /* P14-GM.yml.cuh */
+    case 20: /* P20-GM.yml.cuh */
+    case 17: /* P17-GM.yml.cuh */
+      n[0] = g_isect(NB(v0), NB(v1), NOB, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        if (pid == 14) {
+          n[2] = g_isect(SL(0), NB(v2), v1, s[2]);
+          n[3] = g_diff(SL(1), NB(v2), NOB, s[3]);
+        } else if (pid == 20) {
+          n[2] = g_isect(SL(1), NB(v2), v1, s[2]);
+          n[3] = g_diff(SL(1), NB(v2), NOB, s[3]);
+        } else {
+          n[2] = g_isect(SL(1), NB(v2), NOB, s[2]);
+          n[3] = g_diff(SL(0), NB(v2), NOB, s[3]);
+        }
+        for (eid_t j = 0; j < n[2]; j++) c += g_diff_n(SL(3), NB(s[2][j]), NOB);
+      }
+      break;
+    case 15: /* P15-GM.yml.cuh */
+    case 21: /* P21-GM.yml.cuh */
+      n[0] = g_diff(NB(v1), NB(v0), NOB, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        n[2] = g_diff(SL(1), NB(s[0][i]), NOB, s[2]);
+        for (eid_t j = 0; j < n[2]; j++) {
+          vid_t v3 = s[2][j];
+          c += pid == 15 ? g_diff_n(SL(2), NB(v3), v3) : g_isect_n(SL(2), NB(v3), v3);
+        }
+      }
+      break;
+    case 16: /* P16-GM.yml.cuh */
+      n[0] = g_diff(NB(v1), NB(v0), NOB, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      n[2] = g_isect(NB(v0), NB(v1), NOB, s[2]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        n[3] = g_diff(SL(1), NB(v2), NOB, s[3]);
+        n[4] = g_isect(SL(2), NB(v2), NOB, s[4]);
+        for (eid_t j = 0; j < n[3]; j++) c += g_diff_n(SL(4), NB(s[3][j]), v1);
+      }
+      break;
+    case 18: /* P18-GM.yml.cuh */
+      n[0] = g_isect(NB(v0), NB(v1), v1, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        n[2] = g_diff(SL(1), NB(s[0][i]), NOB, s[2]);
+        for (eid_t j = 0; j < n[2]; j++) c += g_diff_n(SL(2), NB(s[2][j]), s[2][j]);
+      }
+      break;
+    case 19: /* P19-GM.yml.cuh */
+      n[0] = g_isect(NB(v0), NB(v1), v1, s[0]);
+      n[1] = g_diff(NB(v0), NB(v1), NOB, s[1]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        vid_t v2 = s[0][i];
+        n[2] = g_isect(SL(1), NB(v2), v2, s[2]);
+        n[3] = g_diff(SL(0), NB(v2), NOB, s[3]);
+        for (eid_t j = 0; j < n[2]; j++) c += g_isect_n(SL(3), NB(s[2][j]), s[2][j]);
+      }
+      break;
+    case 22: /* P22-GM.yml.cuh (its v1 == v0 skip never fires on a loop-free CSR) */
+      n[0] = g_isect(NB(v0), NB(v1), NOB, s[0]);
+      for (eid_t i = 0; i < n[0]; i++) {
+        n[1] = g_isect(SL(0), NB(s[0][i]), NOB, s[1]);
+        for (eid_t j = 0; j < n[1]; j++) c += g_diff_n(SL(1), NB(s[1][j]), NOB);
+      }
+      break;
+    default:
+      break;
+  }
+  return c;
+}
+
+/* P<pid> count (6 <= pid <= 22); returns 0, or -1 for another id. */
+int orc_glumin5(int pid, int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t max_deg,
+                uint64_t* out) {
+  if (pid < 6 || pid > 22) return -1;
+  uint64_t total = 0;
+  const int64_t md = max_deg > 0 ? max_deg : 1;
+#pragma omp parallel reduction(+ : total)
+  {
+    vid_t* buf = (vid_t*)malloc(sizeof(vid_t) * 5 * (size_t)md);
+    vid_t* s[5];
+    for (int i = 0; i < 5; i++) s[i] = buf + (size_t)i * md;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t v0 = 0; v0 < nv; v0++)
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++)
+        total += glumin5_task(pid, rowptr, col, (vid_t)v0, col[e], s);
+    free(buf);
+  }
+  *out = total;
+  return 0;
+}
+
+/* ------------------------------------------------------ set-operation programs
+ * Interpreter for the engine's program words (see include/xgm.h,
+ * xgm_plan_program): tasks are the directed CSR entries (v0, v1), only v1 < v0 when
+ * the program says so; level l runs after v_0..v_{l+1} are matched; v_{l+2} then runs
+ * over its candidate operand; the last level ends with the counted operation.
+ * Operand >= 16 is N(v_(operand-16)), below it a slot. */
+typedef struct {
+  int k, nslots, flat, v1lt, nops[3], cand[5];
+  int op[3][6][6];
+  int fin[6];
+} prog_t;
+
+typedef struct {
+  const prog_t* p;
+  const int64_t* rowptr;
+  const int32_t* col;
+  vid_t v[5];
+  vid_t* slot[12];
+  eid_t slen[12];
+} pstate_t;
+
+static void p_operand(pstate_t* st, int code, const vid_t** a, eid_t* n) {
+  if (code >= 16) {
+    vid_t v = st->v[code - 16];
+    *a = st->col + st->rowptr[v];
+    *n = st->rowptr[v + 1] - st->rowptr[v];
+  } else {
+    *a = st->slot[code];
+    *n = st->slen[code];
+  }
+}
+
+static int p_member(const vid_t* b, eid_t nb, vid_t x) {
+  eid_t lo = 0, hi = nb;
+  while (lo < hi) {
+    eid_t m = (lo + hi) / 2;
+    if (b[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  return lo < nb && b[lo] == x;
+}
+
+/* Runs one operation; writes its slot, or returns the count when out == NULL. */
+static uint64_t p_apply(pstate_t* st, const int* o, vid_t* out, eid_t* nout) {
+  const vid_t *a, *b = NULL;
+  eid_t na, nb = 0;
+  p_operand(st, o[2], &a, &na);
+  if (o[1] != 2) p_operand(st, o[3], &b, &nb);
+  vid_t up = INT32_MAX;
+  for (int j = 0; j < 5; j++)
+    if ((o[4] >> j) & 1)
+      if (st->v[j] < up) up = st->v[j];
+  uint64_t c = 0;
+  eid_t n = 0;
+  for (eid_t i = 0; i < na && a[i] < up; i++) {
+    vid_t x = a[i];
+    int skip = 0;
+    for (int j = 0; j < 5; j++)
+      if (((o[5] >> j) & 1) && x == st->v[j]) skip = 1;
+    if (skip) continue;
+    if (o[1] != 2 && p_member(b, nb, x) != (o[1] == 0)) continue;
+    if (out) out[n++] = x;
+    else c++;
+  }
+  if (nout) *nout = n;
+  return c;
+}
+
+static uint64_t p_level(pstate_t* st, int l) {
+  const prog_t* p = st->p;
+  for (int i = 0; i < p->nops[l]; i++) {
+    const int* o = p->op[l][i];
+    p_apply(st, o, st->slot[o[0]], &st->slen[o[0]]);
+  }
+  if (l == p->k - 3) return p_apply(st, p->fin, NULL, NULL);
+  const vid_t* c;
+  eid_t nc;
+  p_operand(st, p->cand[l + 2], &c, &nc);
+  uint64_t t = 0;
+  for (eid_t i = 0; i < nc; i++) {
+    st->v[l + 2] = c[i];
+    t += p_level(st, l + 1);
+  }
+  return t;
+}
+
+/* Runs a program over every directed CSR entry; returns 0, or -1 for malformed words. */
+int orc_setprog(const int32_t* w, int nw, int64_t nv, const int64_t* rowptr, const int32_t* col,
+                int64_t max_deg, uint64_t* out) {
+  if (nw < 124 || w[0] != 1) return -1;
+  prog_t p;
+  memset(&p, 0, sizeof(p));
+  p.k = w[1];
+  p.nslots = w[2];
+  p.flat = w[3];
+  p.v1lt = w[4];
+  for (int l = 0; l < 3; l++) p.nops[l] = w[5 + l];
+  p.cand[2] = w[8];
+  p.cand[3] = w[9];
+  if (p.k < 3 || p.k > 5 || p.nslots < 0 || p.nslots > 12) return -1;
+  const int32_t* o = w + 10;
+  for (int l = 0; l < 3; l++)
+    for (int i = 0; i < 6; i++, o += 6) memcpy(p.op[l][i], o, sizeof(int) * 6);
+  memcpy(p.fin, o, sizeof(int) * 6);
+  uint64_t total = 0;
+  const int64_t md = max_deg > 0 ? max_deg : 1;
+#pragma omp parallel reduction(+ : total)
+  {
+    pstate_t st;
+    memset(&st, 0, sizeof(st));
+    st.p = &p;
+    st.rowptr = rowptr;
+    st.col = col;
+    vid_t* buf = (vid_t*)malloc(sizeof(vid_t) * 12 * (size_t)md);
+    for (int i = 0; i < 12; i++) st.slot[i] = buf + (size_t)i * md;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t v0 = 0; v0 < nv; v0++)
+      for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
+        if (p.v1lt && col[e] >= v0) continue;
+        st.v[0] = (vid_t)v0;
+        st.v[1] = col[e];
+        total += p_level(&st, 0);
+      }
+    free(buf);
+  }
+  *out = total;
+  return 0;
+}
+
+/* ---------------------------------------------------- brute-force occurrences
+ * Occurrences of a connected pattern (k <= 6 vertices, adjacency adj[k*k]),
+ * vertex-induced or edge-induced: injective maps that keep every pattern edge (and,
+ * induced, every non-edge), counted by depth-first search in a BFS order of the
+ * pattern and divided by the pattern's automorphism count.  Independent of the
+ * engine's program compiler; for small graphs. */
+typedef struct {
+  int k, induced;
+  const uint8_t* adj;
+  int order[6], parent[6];
+  const int64_t* rowptr;
+  const int32_t* col;
+  vid_t m[6];
+} emb_t;
+
+static int e_adj(const emb_t* e, vid_t a, vid_t b) {
+  return p_member(e->col + e->rowptr[a], e->rowptr[a + 1] - e->rowptr[a], b);
+}
+
+static uint64_t e_dfs(emb_t* e, int i) {
+  if (i == e->k) return 1;
+  const int t = e->order[i];
+  const vid_t pv = e->m[e->parent[i]];
+  uint64_t c = 0;
+  for (int64_t x = e->rowptr[pv]; x < e->rowptr[pv + 1]; x++) {
+    vid_t y = e->col[x];
+    int ok = 1;
+    for (int j = 0; j < i && ok; j++) {
+      const int u = e->order[j];
+      if (e->m[u] == y) ok = 0;
+      else if (e->adj[t * e->k + u]) ok = e_adj(e, y, e->m[u]);
+      else if (e->induced) ok = !e_adj(e, y, e->m[u]);
+    }
+    if (!ok) continue;
+    e->m[t] = y;
+    c += e_dfs(e, i + 1);
+  }
+  return c;
+}
+
+/* Returns 0, or -1 when the pattern is not connected or k is out of range. */
+int orc_occurrences(int k, const uint8_t* adj, int induced, int64_t nv, const int64_t* rowptr,
+                    const int32_t* col, uint64_t* out) {
+  if (k < 2 || k > 6) return -1;
+  emb_t e0;
+  memset(&e0, 0, sizeof(e0));
+  e0.k = k;
+  e0.induced = induced;
+  e0.adj = adj;
+  e0.rowptr = rowptr;
+  e0.col = col;
+  int seen[6] = {1, 0, 0, 0, 0, 0}, n = 1;
+  e0.order[0] = 0;
+  for (int h = 0; h < n; h++)
+    for (int u = 0; u < k; u++)
+      if (!seen[u] && adj[e0.order[h] * k + u]) {
+        seen[u] = 1;
+        e0.parent[n] = e0.order[h];
+        e0.order[n++] = u;
+      }
+  if (n != k) return -1;
+  /* automorphisms */
+  int perm[6], c[6] = {0};
+  for (int i = 0; i < k; i++) perm[i] = i;
+  uint64_t aut = 0;
+  for (int i = 0;;) { /* Heap's algorithm over all k! permutations */
+    int ok = 1;
+    for (int a = 0; a < k && ok; a++)
+      for (int b = 0; b < k && ok; b++) ok = adj[perm[a] * k + perm[b]] == adj[a * k + b];
+    aut += ok;
+    while (i < k && c[i] >= i) c[i++] = 0;
+    if (i >= k) break;
+    int j = (i % 2) ? c[i] : 0, t = perm[j];
+    perm[j] = perm[i];
+    perm[i] = t;
+    c[i]++;
+    i = 1;
+  }
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : total)
+  for (int64_t v = 0; v < nv; v++) {
+    emb_t e = e0;
+    e.m[0] = (vid_t)v;
+    total += e_dfs(&e, 1);
+  }
+  *out = total / aut;
+  return 0;
+}

@@ -6,7 +6,10 @@ CSR build, and every count from the reference's OWN OpenMP binaries (oracle/_ref
 built from the reference sources by oracle/build_ref.sh) run on the graph files:
 tc/clique/count omp_base for the six plans, motif_omp_formula for the k = 3 and k = 4
 vertex-induced motif census ("motif3", "motif4", in the reference's output order).  The
-oracle restatement is cross-checked on the way.  A sha256 of the CSR bytes lets the
+oracle restatement is cross-checked on the way.  On the graphs listed in GLUMIN5_CASES,
+"glumin5" holds GLUMIN's 5-vertex plans P6..P22: P7, P10, P13, P15 and P20 from the
+reference's own CPU plans (glumin_pattern_cpu, list and LUT forms, which must agree
+with the oracle), the others from the oracle's restatement of the generated kernels.  A sha256 of the CSR bytes lets the
 GPU tests confirm they regenerated the same graph.
 
 Run from the repository root (needs the reference tree for oracle/_ref):
@@ -37,6 +40,7 @@ CASES = [
     {"name": "ba_n200_m8", "gen": "ba", "args": [200, 8], "seed": 9},
 ]
 KINDS = ["tc", "clique4", "clique5", "diamond", "cycle4", "tailed"]
+GLUMIN5_CASES = {"rmat_s10_ef16", "er_n4096_m40000", "ba_n3000_m5", "ba_n200_m8"}
 
 
 def samples(case):
@@ -82,6 +86,26 @@ def main() -> None:
             if ref != mine:
                 raise SystemExit(f"{case['name']} motif{k}: reference {ref} != oracle {mine}")
             counts[f"motif{k}"] = ref
+        if case["name"] in GLUMIN5_CASES:
+            g5 = {}
+            for pid in range(6, 23):
+                mine = oracle.glumin5(pid, rowptr, col)
+                if pid in oracle.GLUMIN5_CPU:
+                    for lut in (False, True):
+                        try:
+                            ref, _ = oracle.run_ref_glumin5(pid, prefix, lut)
+                        except RuntimeError:
+                            # the LUT form of P20 (LUT_5anti_tailed_diamond) aborts with
+                            # heap corruption on rmat_s10_ef16; the list form is the pin
+                            if not lut:
+                                raise
+                            print(f"  {case['name']} P{pid}: reference LUT form failed")
+                            continue
+                        if ref != mine:
+                            raise SystemExit(f"{case['name']} P{pid}: reference {ref} != "
+                                             f"oracle {mine}")
+                g5[f"P{pid}"] = mine
+            counts["glumin5"] = g5
         rec = dict(case)
         rec.update({"V": int(nv), "E": int(len(col)), "E_dag": int(len(dcol)),
                     "csr_sha256": csr_digest(rowptr, col), "counts": counts,

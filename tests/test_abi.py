@@ -109,9 +109,20 @@ def test_plan_names_and_ids(xgm):
                            ("P23", xgm.CLIQUE6, 1), ("P24", xgm.CLIQUE7, 1)]:
         p = xgm.plan(name)
         assert (p.pattern, int(p.induced)) == (pat, ind), name
-    with pytest.raises(xgm.XgmError) as e:
-        xgm.plan("P6")
-    assert e.value.status == xgm.ERR_UNSUPPORTED
+    for pid in range(6, 23):  # GLUMIN's generated 5-vertex plans: set-operation programs
+        p = xgm.plan(f"P{pid}")
+        assert (p.pattern, p.induced) == (xgm.PROGRAM, True), pid
+        w = p.program
+        assert w is not None and len(w) == xgm.PROGRAM_WORDS and w[0] == 1 and w[1] == 5
+    for name in xgm.YML5_EDGES:  # GLUMIN's 5-vertex .yml names: compiled, edge-induced
+        p = xgm.plan(name)
+        assert (p.pattern, p.induced) == (xgm.PROGRAM, False), name
+        assert xgm.plan(name, induced=True).induced
+    assert xgm.plan("P5").program is None
+    for bad in ("P25", "P0", "P6x", "6-star"):
+        with pytest.raises(xgm.XgmError) as e:
+            xgm.plan(bad)
+        assert e.value.status == xgm.ERR_UNSUPPORTED, bad
 
 
 def test_plan_from_spec(xgm):
@@ -124,10 +135,13 @@ def test_plan_from_spec(xgm):
         p = xgm.plan_from_spec(_spec(edges))
         assert p.pattern == pat and p.induced, edges
         assert not xgm.plan_from_spec(_spec(edges), induced=False).induced
+    # a 5-vertex pattern without a builtin compiles to a set-operation program
+    p = xgm.plan_from_spec(_spec(["AB", "BC", "CD", "DE", "AE"]))  # 5-cycle
+    assert p.pattern == xgm.PROGRAM and p.induced and p.program is not None
     for bad, st in [(_spec(["AB", "A"]), xgm.ERR_INVALID), (_spec(["AA", "AB"]), xgm.ERR_INVALID),
                     ("pattern:\n  name: x\n", xgm.ERR_INVALID), (_spec([]), xgm.ERR_INVALID),
-                    (_spec(["AB", "BC", "CD", "DE", "AE"]), xgm.ERR_UNSUPPORTED),  # 5-cycle
-                    (_spec(["AB", "CD"]), xgm.ERR_UNSUPPORTED)]:  # disconnected
+                    (_spec(["AB", "CD"]), xgm.ERR_UNSUPPORTED),  # disconnected
+                    (_spec(["AB", "BC", "CD", "DE", "EF"]), xgm.ERR_UNSUPPORTED)]:  # 6-path
         with pytest.raises(xgm.XgmError) as e:
             xgm.plan_from_spec(bad)
         assert e.value.status == st, bad
@@ -142,10 +156,15 @@ def test_reference_pattern_files(xgm):
             "4-cycle": xgm.CYCLE4, "4-diamond": xgm.DIAMOND, "4-path": xgm.PATH4,
             "4-star": xgm.STAR3, "4-tailed-triangle": xgm.TAILED_TRIANGLE,
             "5-clique": xgm.CLIQUE5}
+    want.update({name: xgm.PROGRAM for name in xgm.YML5_EDGES})
     for f in sorted(os.listdir(GLUMIN_PATTERNS)):
         name = f[:-4]
         if name in want:
             assert xgm.plan_from_spec(os.path.join(GLUMIN_PATTERNS, f)).pattern == want[name], f
-        else:  # 5-vertex motifs and the empty template are not plans of this engine
+        else:  # the empty template is not a plan
             with pytest.raises(xgm.XgmError):
                 xgm.plan_from_spec(os.path.join(GLUMIN_PATTERNS, f))
+    # the engine's copies of the 5-vertex edge lists are the files' own
+    for name, edges in xgm.YML5_EDGES.items():
+        text = open(os.path.join(GLUMIN_PATTERNS, name + ".yml")).read()
+        assert "edges: [" + edges + "]" in text, name

@@ -36,6 +36,14 @@ VIEW_UNDIRECTED, VIEW_DAG = 0, 1
 
 TRIANGLE, CLIQUE4, CLIQUE5, DIAMOND, CYCLE4, TAILED_TRIANGLE = 1, 2, 3, 4, 5, 6
 WEDGE, STAR3, PATH4, CLIQUE6, CLIQUE7 = 7, 8, 9, 10, 11
+PROGRAM = 12  # set-operation program: GLUMIN P6..P22 or a compiled 5-vertex pattern
+PROGRAM_WORDS = 124
+GLUMIN5_IDS = [f"P{i}" for i in range(6, 23)]
+# GLUMIN's 5-vertex .yml patterns (codegen/codegen/patterns/5-*.yml), `edges:` lists
+YML5_EDGES = {"5-cycle": "AB, BC, CD, DE, AE", "5-double-triangle": "AB, AC, BC, AD, AE, DE",
+              "5-house": "AB, AC, BC, BD, DE, CE", "5-path": "AB, BC, CD, DE",
+              "5-solid-house": "AB, AC, BC, BD, BE, CD, CE, DE", "5-star": "AB, AC, AD, AE",
+              "5-tailed-square": "AB, BC, CD, AD, AE"}
 PATTERN_NAMES = {"triangle": TRIANGLE, "4-clique": CLIQUE4, "5-clique": CLIQUE5,
                  "diamond": DIAMOND, "rectangle": CYCLE4, "4-cycle": CYCLE4,
                  "tailedtriangle": TAILED_TRIANGLE, "wedge": WEDGE, "3-star": STAR3,
@@ -125,6 +133,7 @@ _SIGS = [
     ("xgm_plan_from_name", _I, [_P, C.c_char_p, C.POINTER(_P)]),
     ("xgm_plan_from_spec", _I, [_P, C.c_char_p, _I, C.POINTER(_P)]),
     ("xgm_plan_pattern", _I, [_P]),
+    ("xgm_plan_program", _I, [_P, _P, _I]),
     ("xgm_plan_induced", _I, [_P]),
     ("xgm_plan_destroy", None, [_P]),
     ("xgm_count", _I, [_P, _P, _P, C.POINTER(Sched), C.POINTER(_U64), C.POINTER(Stats)]),
@@ -249,8 +258,8 @@ class Context:
         return self._adopt(Graph(self, h))
 
     # plans / counting -----------------------------------------------------
-    def plan(self, pattern, induced: bool = False) -> "Plan":
-        return plan(pattern, induced, self)
+    def plan(self, pattern, induced: bool = False, program: bool = False) -> "Plan":
+        return plan(pattern, induced, self, program)
 
     def plan_from_spec(self, spec: str, induced: bool = True) -> "Plan":
         """Plan from a GLUMIN pattern .yml (text or path); GLUMIN counts vertex-induced."""
@@ -363,12 +372,22 @@ class Context:
         return int(out.value)
 
 
-def plan(pattern, induced: bool = False, ctx: Optional["Context"] = None) -> "Plan":
-    """Plan from a name, a builtin id or a pattern adjacency matrix (no GPU needed)."""
+def plan(pattern, induced: bool = False, ctx: Optional["Context"] = None,
+         program: bool = False) -> "Plan":
+    """Plan from a name, a builtin id or a pattern adjacency matrix (no GPU needed);
+    program=True compiles an adjacency matrix to a set-operation program even where a
+    builtin plan exists."""
     h = C.c_void_p()
     ch = ctx._h if ctx is not None else None
     if isinstance(pattern, str):
+        if induced and pattern in YML5_EDGES:
+            return plan_from_spec(f"edges: [{YML5_EDGES[pattern]}]", True, ctx)
         _check(lib().xgm_plan_from_name(ch, pattern.encode(), C.byref(h)), ctx)
+        if induced and lib().xgm_plan_pattern(h) == PROGRAM:
+            if not lib().xgm_plan_induced(h):
+                lib().xgm_plan_destroy(h)
+                raise XgmError(ERR_UNSUPPORTED, f"{pattern}: no vertex-induced form by name")
+            return Plan(h)
         if induced:  # names carry no induced flag: rebuild through the descriptor
             p = lib().xgm_plan_pattern(h)
             lib().xgm_plan_destroy(h)
@@ -380,7 +399,7 @@ def plan(pattern, induced: bool = False, ctx: Optional["Context"] = None) -> "Pl
         d.builtin = pattern
     else:
         adj = np.asarray(pattern, dtype=np.uint8)
-        d.builtin = 0
+        d.builtin = PROGRAM if program else 0
         d.num_vertices = adj.shape[0]
         for i in range(adj.shape[0]):
             for j in range(adj.shape[1]):
@@ -409,6 +428,16 @@ class Plan:
     @property
     def induced(self) -> bool:
         return bool(lib().xgm_plan_induced(self._h))
+
+    @property
+    def program(self) -> Optional[np.ndarray]:
+        """Flat words of a set-operation program plan (None for a builtin)."""
+        n = lib().xgm_plan_program(self._h, None, 0)
+        if n == 0:
+            return None
+        w = np.zeros(n, dtype=np.int32)
+        lib().xgm_plan_program(self._h, w.ctypes.data, n)
+        return w
 
     def __del__(self):
         try:

@@ -140,6 +140,7 @@ void xgm_destroy(xgm_ctx* c) {
   if (c->stream) {
     taskbuf_free(c->tb, c->stream);
     motif_buffers_free(c);
+    program_buffers_free(c);
     cudaStreamSynchronize(c->stream);
   }
   if (c->d_sc) cudaFree(c->d_sc);
@@ -337,13 +338,32 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* d, xgm_plan** out
   if (!d || !out) return XGM_ERR_INVALID;
   *out = nullptr;
   int pat = d->builtin;
-  if (pat == 0) {
+  const bool force_program = pat == XGM_PATTERN_PROGRAM;
+  if (pat == 0 || force_program) {
     pat = match_pattern(d);
-    if (pat <= 0) {
-      set_thread_error(pat == 0 ? "pattern not supported (supported: triangle, 4/5-clique, "
-                                  "diamond, 4-cycle, tailed triangle, wedge, 3-star, 4-path)"
-                                : "pattern adjacency is malformed");
-      return finish_status(ctx, pat == 0 ? XGM_ERR_UNSUPPORTED : XGM_ERR_INVALID);
+    if (pat < 0) {
+      set_thread_error("pattern adjacency is malformed");
+      return finish_status(ctx, XGM_ERR_INVALID);
+    }
+    if (pat == 0 || force_program) {
+      // no builtin: a set-operation program (connected patterns of up to 5 vertices)
+      Prog prog;
+      std::string why;
+      if (d->num_vertices > kProgMaxK) {
+        set_thread_error("pattern not supported (builtins, or any connected pattern of up to "
+                         "5 vertices)");
+        return finish_status(ctx, XGM_ERR_UNSUPPORTED);
+      }
+      if (!prog_compile(d->num_vertices, d->adj, d->induced != 0, &prog, &why)) {
+        set_thread_error("pattern not supported: " + why);
+        return finish_status(ctx, XGM_ERR_UNSUPPORTED);
+      }
+      xgm_plan* p = new xgm_plan();
+      p->pattern = XGM_PATTERN_PROGRAM;
+      p->induced = d->induced ? 1 : 0;
+      p->prog = prog;
+      *out = p;
+      return XGM_OK;
     }
   }
   if (pat < XGM_PATTERN_TRIANGLE || pat > XGM_PATTERN_CLIQUE7) return XGM_ERR_INVALID;
@@ -393,6 +413,35 @@ int xgm_plan_induced(const xgm_plan* p) { return p ? p->induced : 0; }
 
 xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out) {
   if (!name || !out) return XGM_ERR_INVALID;
+  *out = nullptr;
+  // GLUMIN's 5-vertex plans P6..P22, as generated
+  if (name[0] == 'P' && name[1] >= '0' && name[1] <= '9') {
+    char* end = nullptr;
+    const long pid = std::strtol(name + 1, &end, 10);
+    Prog prog;
+    if (end && *end == '\0' && pid >= 6 && pid <= 22 && prog_glumin((int)pid, &prog)) {
+      xgm_plan* p = new xgm_plan();
+      p->pattern = XGM_PATTERN_PROGRAM;
+      p->induced = 1;
+      p->prog = prog;
+      *out = p;
+      return XGM_OK;
+    }
+  }
+  // GLUMIN's 5-vertex .yml names (codegen/codegen/patterns/5-*.yml), edge-induced like
+  // the other .yml names
+  static const struct {
+    const char* name;
+    const char* edges;
+  } kYml5[] = {{"5-cycle", "edges: [AB, BC, CD, DE, AE]"},
+               {"5-double-triangle", "edges: [AB, AC, BC, AD, AE, DE]"},
+               {"5-house", "edges: [AB, AC, BC, BD, DE, CE]"},
+               {"5-path", "edges: [AB, BC, CD, DE]"},
+               {"5-solid-house", "edges: [AB, AC, BC, BD, BE, CD, CE, DE]"},
+               {"5-star", "edges: [AB, AC, AD, AE]"},
+               {"5-tailed-square", "edges: [AB, BC, CD, AD, AE]"}};
+  for (const auto& y : kYml5)
+    if (std::strcmp(name, y.name) == 0) return xgm_plan_from_spec(ctx, y.edges, 0, out);
   int induced = 0;
   uint64_t scale = 1;
   const int pat = pattern_from_name(name, &induced, &scale);
@@ -410,6 +459,13 @@ xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out) {
 }
 
 int xgm_plan_pattern(const xgm_plan* p) { return p ? p->pattern : 0; }
+
+int xgm_plan_program(const xgm_plan* p, int32_t* words, int n_words) {
+  if (!p || p->pattern != XGM_PATTERN_PROGRAM) return 0;
+  static_assert(kProgWords == XGM_PROGRAM_WORDS, "program word count");
+  if (words && n_words >= kProgWords) prog_to_words(p->prog, words);
+  return kProgWords;
+}
 void xgm_plan_destroy(xgm_plan* p) { delete p; }
 
 // ----------------------------------------------------------------- counting
@@ -422,7 +478,9 @@ xgm_status xgm_count(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan, con
   xgm_stats st_local;
   xgm_stats& st = stats ? *stats : st_local;
   std::memset(&st, 0, sizeof(st));
-  xgm_status r = count_plan(ctx, g->g, plan->pattern, plan->induced, sp, out_count, st);
+  xgm_status r = plan->pattern == XGM_PATTERN_PROGRAM
+                     ? count_program(ctx, g->g, plan->prog, out_count, st)
+                     : count_plan(ctx, g->g, plan->pattern, plan->induced, sp, out_count, st);
   if (r == XGM_OK) *out_count *= plan->scale;
   return finish_status(ctx, r);
 }
@@ -445,6 +503,10 @@ xgm_status xgm_motif_count(xgm_ctx* ctx, const xgm_graph* g, int k, const xgm_sc
 xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
                              const xgm_sched* sched, int* n_kernels) {
   if (!ctx || !g || !plan || !n_kernels) return XGM_ERR_INVALID;
+  if (plan->pattern == XGM_PATTERN_PROGRAM) {
+    *n_kernels = plan->prog.k == 3 ? 1 : 2;
+    return XGM_OK;
+  }
   xgm_sched def;
   std::memset(&def, 0, sizeof(def));
   return finish_status(ctx, count_kernels(ctx, g->g, plan->pattern, sched ? *sched : def, n_kernels));
@@ -477,6 +539,10 @@ xgm_status xgm_sc_solver(xgm_ctx* ctx, const xgm_graph* g, const char* pattern, 
 
 xgm_status xgm_algo_bytes(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan, uint64_t* bytes) {
   if (!ctx || !g || !plan || !bytes) return XGM_ERR_INVALID;
+  if (plan->pattern == XGM_PATTERN_PROGRAM) {
+    set_thread_error("algorithmic bytes are defined for the builtin plans only");
+    return finish_status(ctx, XGM_ERR_UNSUPPORTED);
+  }
   return finish_status(ctx, algo_bytes_dispatch(ctx, g->g, plan->pattern, bytes));
 }
 

@@ -5,6 +5,7 @@
 #include "clique.cuh"
 #include "graph.cuh"
 #include "sched.cuh"
+#include "setprog.cuh"
 
 namespace xgm {
 
@@ -61,6 +62,11 @@ struct xgm_ctx {
   int64_t* c4_ttab = nullptr;  // per group: tseg[m+1] then tcnt[m]
   int64_t c4_task_cap = 0;
   int clique_grid = 0;
+  // set-operation programs (setprog.cu): per-warp slot scratch, split records, heads
+  int32_t* prog_scratch = nullptr;
+  int64_t prog_scratch_cap = 0;
+  void* prog_split = nullptr;
+  unsigned long long* prog_heads = nullptr;
 };
 
 struct xgm_graph {
@@ -72,6 +78,7 @@ struct xgm_plan {
   int pattern = 0;
   int induced = 0;     // vertex-induced motif counts (via the motif identities)
   uint64_t scale = 1;  // embeddings per match in the caller's convention (GLUMIN P2: 2)
+  xgm::Prog prog;      // XGM_PATTERN_PROGRAM: the set-operation program
 };
 
 namespace xgm {
@@ -92,6 +99,10 @@ xgm_status count_motifs(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched&
 xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm_sched& sp,
                          int* n_kernels);
 void motif_buffers_free(xgm_ctx* ctx);
+// setprog.cu
+xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_t* out,
+                         xgm_stats& st);
+void program_buffers_free(xgm_ctx* ctx);
 // k_feat: clique size the learned model's features describe (default k).
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
                          cudaStream_t s, int k_feat = 0);

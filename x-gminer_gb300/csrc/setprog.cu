@@ -1,0 +1,447 @@
+// Interpreter for set-operation programs (setprog.cuh) on the undirected CSR in
+// original ids.
+//
+// One warp per task; a task is one directed CSR entry (v0, v1), as GLUMIN's
+// edge-parallel kernels walk the full edge list (G2Miner/gpu_GM_LUT.cu:78-95,
+// GM_kernels/P*-GM.yml.cuh: `for eid ... g.get_src(eid), g.get_dst(eid)`).  Warps
+// claim chunks of entries from an atomic head; the row of a chunk's first entry is
+// found by binary search over rowptr and then advanced entry by entry.
+//
+// A set operation streams its first list through the warp (coalesced, 32 elements a
+// step), tests each element against the second list by binary search, and compacts
+// the survivors with a ballot into the warp's slot; a bound stops the stream at the
+// first element at or above it (the lists are sorted).  The last vertex is never
+// enumerated: the final count runs flat over every (v_{k-2}, x) pair of the last
+// candidate list and the counted operand, so a warp keeps all 32 lanes busy when the
+// lists are short, which they mostly are on sparse graphs.  A task whose v2
+// candidate list is long keeps its first kSplitLen candidates and queues the rest as
+// split records; a second launch runs those (each record recomputes the level-0
+// slots, O(d(v0) + d(v1)) per record, against O(d^2) work per record).
+//
+// Slots live in a per-warp global scratch area (slot count x max degree ints), which
+// stays in L1/L2: a slot is written once per level and read by every later step.
+#include <algorithm>
+#include <climits>
+#include <cstring>
+
+#include "api_internal.h"
+#include "graph.cuh"
+#include "setprog.cuh"
+
+namespace xgm {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 8;       // CSR entries claimed per queue step
+constexpr int kSplitMin = 96;   // v2 candidates above which a task is split
+constexpr int kSplitLen = 32;   // v2 candidates per split record
+constexpr int64_t kSplitCap = int64_t(1) << 22;  // records (64 MB)
+
+struct SplitRec {
+  int32_t e_lo, e_hi;  // CSR entry
+  int32_t lo, hi;      // v2 candidate range
+};
+
+struct ProgArgs {
+  const int64_t* rowptr;
+  const int32_t* col;
+  int64_t nv, ne;
+  int32_t* scratch;
+  int64_t slot_cap;   // ints per slot
+  int nslots;
+  unsigned long long* heads;  // [0] entry head, [1] split tail, [2] split head
+  SplitRec* split;
+  int64_t split_cap;
+  unsigned long long* total;
+  int split_mode;
+};
+
+struct WarpState {
+  int v[kProgMaxK];
+  int vl[kProgMaxK];
+  long long vb[kProgMaxK];
+  int slen[kProgMaxSlots];
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Binary search for x in the sorted list b[0, len).
+__device__ __forceinline__ bool member(const int32_t* b, int len, int x) {
+  int lo = 0, n = len;
+  while (n > 0) {
+    const int h = n >> 1;
+    if (__ldg(b + lo + h) < x) {
+      lo += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return lo < len && __ldg(b + lo) == x;
+}
+
+struct Operand {
+  const int32_t* p;
+  int n;
+};
+
+__device__ __forceinline__ Operand operand(const WarpState& w, int code, const ProgArgs& a,
+                                           const int32_t* slots) {
+  if (code >= kOpList) {
+    const int j = code - kOpList;
+    return Operand{a.col + w.vb[j], w.vl[j]};
+  }
+  return Operand{slots + (int64_t)code * a.slot_cap, w.slen[code]};
+}
+
+__device__ __forceinline__ int bound_of(const WarpState& w, unsigned mask) {
+  int b = INT_MAX;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j)
+    if ((mask >> j) & 1u) b = min(b, w.v[j]);
+  return b;
+}
+
+struct Excl {
+  int e[kProgMaxK];
+  __device__ __forceinline__ bool hit(int x) const {
+    bool h = false;
+#pragma unroll
+    for (int j = 0; j < kProgMaxK; ++j) h |= x == e[j];
+    return h;
+  }
+};
+
+__device__ __forceinline__ Excl excl_of(const WarpState& w, unsigned mask) {
+  Excl r;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j) r.e[j] = ((mask >> j) & 1u) ? w.v[j] : -1;
+  return r;
+}
+
+__device__ __forceinline__ void set_vertex(WarpState& w, int j, int x, const ProgArgs& a, int lane) {
+  if (lane == 0) {
+    const long long b = a.rowptr[x];
+    w.v[j] = x;
+    w.vb[j] = b;
+    w.vl[j] = (int)(a.rowptr[x + 1] - b);
+  }
+  __syncwarp();
+}
+
+// out slot <- op(a, b); warp-wide.
+__device__ void run_op(const ProgOp& o, WarpState& w, const ProgArgs& a, int32_t* slots, int lane) {
+  const Operand A = operand(w, o.a, a, slots);
+  const Operand B = o.kind == OP_FILTER ? Operand{nullptr, 0} : operand(w, o.b, a, slots);
+  const int bnd = bound_of(w, o.bound);
+  const Excl ex = excl_of(w, o.excl);
+  int32_t* out = slots + (int64_t)o.out * a.slot_cap;
+  int written = 0;
+  for (int base = 0; base < A.n; base += 32) {
+    const int i = base + lane;
+    const bool in = i < A.n;
+    const int x = in ? A.p[i] : INT_MAX;
+    const bool below = in && x < bnd;
+    bool keep = below && !ex.hit(x);
+    if (keep && o.kind != OP_FILTER) keep = member(B.p, B.n, x) == (o.kind == OP_INTERSECT);
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) out[written + __popc(m & lanemask_lt())] = x;
+    written += __popc(m);
+    if (__ballot_sync(0xffffffffu, in && !below)) break;
+  }
+  if (lane == 0) w.slen[o.out] = written;
+  __syncwarp();
+}
+
+// |op(a, b)| for the counted vertex; per-lane partial.
+__device__ unsigned long long count_op(const ProgOp& o, const WarpState& w, const ProgArgs& a,
+                                       const int32_t* slots, int lane) {
+  const Operand A = operand(w, o.a, a, slots);
+  const Operand B = o.kind == OP_FILTER ? Operand{nullptr, 0} : operand(w, o.b, a, slots);
+  const int bnd = bound_of(w, o.bound);
+  const Excl ex = excl_of(w, o.excl);
+  unsigned long long c = 0;
+  for (int base = 0; base < A.n; base += 32) {
+    const int i = base + lane;
+    const bool in = i < A.n;
+    const int x = in ? A.p[i] : INT_MAX;
+    const bool below = in && x < bnd;
+    bool keep = below && !ex.hit(x);
+    if (keep && o.kind != OP_FILTER) keep = member(B.p, B.n, x) == (o.kind == OP_INTERSECT);
+    c += keep ? 1 : 0;
+    if (__ballot_sync(0xffffffffu, in && !below)) break;
+  }
+  return c;
+}
+
+// Final count merged with the loop over v_iv (iv = k-2) running over C[lo, hi):
+// one item per (candidate u, element x of the counted operand).
+__device__ unsigned long long count_flat(const ProgOp& o, const WarpState& w, int iv, Operand C,
+                                         int lo, int hi, const ProgArgs& a, const int32_t* slots,
+                                         int lane) {
+  const Operand A = operand(w, o.a, a, slots);
+  const unsigned ivbit = 1u << iv;
+  const int sbnd = bound_of(w, o.bound & ~ivbit);
+  const bool ubnd = (o.bound & ivbit) != 0;
+  const Excl ex = excl_of(w, o.excl & ~ivbit);
+  const bool uex = (o.excl & ivbit) != 0;
+  const bool filter = o.kind == OP_FILTER;
+  const bool b_u = !filter && o.b == kOpList + iv;
+  const Operand Bf = (filter || b_u) ? Operand{nullptr, 0} : operand(w, o.b, a, slots);
+  const bool want = o.kind == OP_INTERSECT;
+  const int n = hi - lo;
+  unsigned long long c = 0;
+  if (A.n == 0 || n <= 0) return 0;
+  int ci = lane / A.n, ai = lane - ci * A.n;
+  while (ci < n) {
+    const int u = C.p[lo + ci];
+    const int x = A.p[ai];
+    const int bnd = ubnd ? min(sbnd, u) : sbnd;
+    if (x < bnd && !ex.hit(x) && !(uex && x == u)) {
+      if (filter) {
+        ++c;
+      } else if (b_u) {
+        const long long rb = a.rowptr[u];
+        c += member(a.col + rb, (int)(a.rowptr[u + 1] - rb), x) == want ? 1 : 0;
+      } else {
+        c += member(Bf.p, Bf.n, x) == want ? 1 : 0;
+      }
+    }
+    ai += 32;
+    while (ai >= A.n) {
+      ai -= A.n;
+      ++ci;
+    }
+  }
+  return c;
+}
+
+template <int K>
+__device__ unsigned long long run_task(const Prog& p, WarpState& w, const ProgArgs& a,
+                                       int32_t* slots, int v0, int v1, long long e, int lo, int hi,
+                                       bool may_split, int lane) {
+  set_vertex(w, 0, v0, a, lane);
+  set_vertex(w, 1, v1, a, lane);
+  for (int i = 0; i < p.nops[0]; ++i) run_op(p.ops[0][i], w, a, slots, lane);
+  if (K == 3) return count_op(p.fin, w, a, slots, lane);
+  const Operand C2 = operand(w, p.cand[2], a, slots);
+  if (hi < 0 || hi > C2.n) hi = C2.n;
+  if (may_split && C2.n > kSplitMin) {
+    const int nrec = (C2.n - kSplitLen + kSplitLen - 1) / kSplitLen;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(a.heads + 1, (unsigned long long)nrec);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const bool fits = base + nrec <= (unsigned long long)a.split_cap;
+    for (int r = lane; r < nrec; r += 32) {
+      // a claim that crosses the capacity leaves empty records below it; the task
+      // then runs all of its candidates itself
+      if (base + r >= (unsigned long long)a.split_cap) break;
+      const int rlo = kSplitLen * (r + 1);
+      a.split[base + r] = fits ? SplitRec{(int32_t)(e & 0xffffffffLL), (int32_t)(e >> 32), rlo,
+                                          min(rlo + kSplitLen, C2.n)}
+                               : SplitRec{0, 0, 0, 0};
+    }
+    if (fits) hi = kSplitLen;
+  }
+  unsigned long long c = 0;
+  if (K == 4) {
+    if (p.flat) return count_flat(p.fin, w, 2, C2, lo, hi, a, slots, lane);
+    for (int i2 = lo; i2 < hi; ++i2) {
+      set_vertex(w, 2, C2.p[i2], a, lane);
+      for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
+      c += count_op(p.fin, w, a, slots, lane);
+    }
+    return c;
+  }
+  for (int i2 = lo; i2 < hi; ++i2) {
+    set_vertex(w, 2, C2.p[i2], a, lane);
+    for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
+    const Operand C3 = operand(w, p.cand[3], a, slots);
+    if (p.flat) {
+      c += count_flat(p.fin, w, 3, C3, 0, C3.n, a, slots, lane);
+    } else {
+      for (int i3 = 0; i3 < C3.n; ++i3) {
+        set_vertex(w, 3, C3.p[i3], a, lane);
+        for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
+        c += count_op(p.fin, w, a, slots, lane);
+      }
+    }
+  }
+  return c;
+}
+
+__device__ __forceinline__ int row_of(const int64_t* rowptr, int64_t nv, long long e) {
+  int64_t lo = 0, n = nv + 1;  // first index with rowptr[idx] > e, minus one
+  while (n > 0) {
+    const int64_t h = n >> 1;
+    if (rowptr[lo + h] <= e) {
+      lo += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return (int)(lo - 1);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_setprog(Prog prog, ProgArgs a) {
+  __shared__ Prog p;
+  __shared__ WarpState ws[kWarps];
+  if (threadIdx.x == 0) p = prog;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  WarpState& w = ws[wib];
+  int32_t* slots = a.scratch + ((int64_t)blockIdx.x * kWarps + wib) * a.nslots * a.slot_cap;
+  unsigned long long c = 0;
+  if (!a.split_mode) {
+    for (;;) {
+      unsigned long long e0 = 0;
+      if (lane == 0) e0 = atomicAdd(a.heads, (unsigned long long)kChunk);
+      e0 = __shfl_sync(0xffffffffu, e0, 0);
+      if ((long long)e0 >= a.ne) break;
+      const long long e1 = min((long long)e0 + kChunk, (long long)a.ne);
+      int v0 = 0;
+      if (lane == 0) v0 = row_of(a.rowptr, a.nv, (long long)e0);
+      v0 = __shfl_sync(0xffffffffu, v0, 0);
+      for (long long e = (long long)e0; e < e1; ++e) {
+        while (a.rowptr[v0 + 1] <= e) ++v0;
+        const int v1 = a.col[e];
+        if (p.v1lt && v1 >= v0) continue;
+        c += run_task<K>(p, w, a, slots, v0, v1, e, 0, -1, true, lane);
+      }
+    }
+  } else {
+    const unsigned long long nrec = min(*(volatile unsigned long long*)(a.heads + 1),
+                                        (unsigned long long)a.split_cap);
+    for (;;) {
+      unsigned long long r = 0;
+      if (lane == 0) r = atomicAdd(a.heads + 2, 1ull);
+      r = __shfl_sync(0xffffffffu, r, 0);
+      if (r >= nrec) break;
+      const SplitRec rec = a.split[r];
+      if (rec.lo >= rec.hi) continue;
+      const long long e = (long long)(uint32_t)rec.e_lo | ((long long)rec.e_hi << 32);
+      int v0 = 0;
+      if (lane == 0) v0 = row_of(a.rowptr, a.nv, e);
+      v0 = __shfl_sync(0xffffffffu, v0, 0);
+      c += run_task<K>(p, w, a, slots, v0, a.col[e], e, rec.lo, rec.hi, false, lane);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0 && c) atomicAdd(a.total, c);
+}
+
+template <int K>
+cudaError_t launch_k(const Prog& p, const ProgArgs& a, int grid, cudaStream_t s) {
+  ProgArgs b = a;
+  b.split_mode = 0;
+  k_setprog<K><<<grid, kThreads, 0, s>>>(p, b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || K == 3) return e;
+  b.split_mode = 1;
+  k_setprog<K><<<grid, kThreads, 0, s>>>(p, b);
+  return cudaGetLastError();
+}
+
+int occupancy(int k) {
+  int n = 0;
+  cudaError_t e = k == 3   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<3>, kThreads, 0)
+                  : k == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<4>, kThreads, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<5>, kThreads, 0);
+  return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
+}  // namespace
+
+xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_t* out,
+                         xgm_stats& st) {
+  std::string why;
+  if (!prog_check(p, &why)) {
+    set_thread_error("invalid set-operation program: " + why);
+    return XGM_ERR_INVALID;
+  }
+  cudaStream_t s = ctx->stream;
+  XGM_CUDA_TRY(cudaSetDevice(ctx->device));
+  XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  const int nslots = p.nslots > 0 ? p.nslots : 1;
+  const int64_t slot_cap = g.max_deg > 0 ? g.max_deg : 1;
+  // resident warps, fewer when the scratch would pass 8 GB
+  int grid = ctx->num_sms * occupancy(p.k);
+  const int64_t per_block = (int64_t)kWarps * nslots * slot_cap * (int64_t)sizeof(int32_t);
+  const int64_t budget = int64_t(8) << 30;
+  if ((int64_t)grid * per_block > budget)
+    grid = (int)std::max<int64_t>(ctx->num_sms, budget / per_block);
+  const int64_t need = (int64_t)grid * kWarps * nslots * slot_cap;
+  if (need > ctx->prog_scratch_cap) {
+    if (ctx->prog_scratch) XGM_CUDA_TRY(cudaFreeAsync(ctx->prog_scratch, s));
+    ctx->prog_scratch = nullptr;
+    ctx->prog_scratch_cap = 0;
+    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_scratch, sizeof(int32_t) * need, s));
+    ctx->prog_scratch_cap = need;
+  }
+  if (!ctx->prog_split) {
+    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_split, sizeof(SplitRec) * kSplitCap, s));
+    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_heads, sizeof(unsigned long long) * 4, s));
+  }
+  XGM_CUDA_TRY(cudaMemsetAsync(ctx->prog_heads, 0, sizeof(unsigned long long) * 4, s));
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  ProgArgs a;
+  a.rowptr = g.rowptr_o;
+  a.col = g.col_o;
+  a.nv = g.nv;
+  a.ne = g.ne;
+  a.scratch = ctx->prog_scratch;
+  a.slot_cap = slot_cap;
+  a.nslots = nslots;
+  a.heads = (unsigned long long*)ctx->prog_heads;
+  a.split = (SplitRec*)ctx->prog_split;
+  a.split_cap = kSplitCap;
+  a.total = &ctx->d_sc->count;
+  a.split_mode = 0;
+  int launches = 0;
+  if (g.ne > 0) {
+    cudaError_t e = p.k == 3   ? launch_k<3>(p, a, grid, s)
+                    : p.k == 4 ? launch_k<4>(p, a, grid, s)
+                               : launch_k<5>(p, a, grid, s);
+    if (e != cudaSuccess) return cuda_fail(e, "k_setprog", __FILE__, __LINE__);
+    launches = p.k == 3 ? 1 : 2;
+  }
+  XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+  XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->prog_heads + 1, sizeof(int64_t),
+                               cudaMemcpyDeviceToDevice, s));
+  xgm_status r = ctx_sync_scalars(ctx);
+  if (r != XGM_OK) return r;
+  float prep = 0, kern = 0;
+  cudaEventElapsedTime(&prep, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&kern, ctx->ev[1], ctx->ev[2]);
+  std::memset(&st, 0, sizeof(st));
+  st.prep_ms = prep;
+  st.kernel_ms = kern;
+  st.launches = launches;
+  st.tasks = g.ne;
+  st.variant_tasks[XGM_VAR_SPLIT] = std::min<int64_t>(ctx->h_sc->n[0], kSplitCap);
+  *out = ctx->h_sc->count;
+  return XGM_OK;
+}
+
+void program_buffers_free(xgm_ctx* ctx) {
+  cudaStream_t s = ctx->stream;
+  if (ctx->prog_scratch) cudaFreeAsync(ctx->prog_scratch, s);
+  if (ctx->prog_split) cudaFreeAsync(ctx->prog_split, s);
+  if (ctx->prog_heads) cudaFreeAsync(ctx->prog_heads, s);
+  ctx->prog_scratch = nullptr;
+  ctx->prog_split = nullptr;
+  ctx->prog_heads = nullptr;
+  ctx->prog_scratch_cap = 0;
+}
+
+}  // namespace xgm
