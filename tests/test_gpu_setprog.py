@@ -47,10 +47,10 @@ def test_glumin5_golden(xgm, ctx, golden):
 
 
 def test_glumin5_vs_oracle_and_split(xgm, ctx, orc):
+    split = 0
     for rowptr, col in (_hub_graph(400, 0.02, 5), _random_graph(300, 0.05, 6),
                         _random_graph(120, 0.2, 7)):
         g = ctx.graph_from_csr(rowptr, col)
-        split = 0
         for pid in range(6, 23):
             got, st = ctx.count(g, f"P{pid}", with_stats=True)
             assert got == orc.glumin5(pid, rowptr, col), pid

@@ -13,13 +13,15 @@
 // first element at or above it (the lists are sorted).  The last vertex is never
 // enumerated: the final count runs flat over every (v_{k-2}, x) pair of the last
 // candidate list and the counted operand, so a warp keeps all 32 lanes busy when the
-// lists are short, which they mostly are on sparse graphs.  A task whose v2
-// candidate list is long keeps its first kSplitLen candidates and queues the rest as
-// split records; a second launch runs those (each record recomputes the level-0
-// slots, O(d(v0) + d(v1)) per record, against O(d^2) work per record).
+// lists are short, which they mostly are on sparse graphs.  A task whose estimated
+// work (v2 candidates x the cost of one v2 step, from the lengths of the level-0
+// slots the later steps read) passes kSplitWork keeps its first v2 candidates and
+// queues the rest as split records of about kSplitWork each; a second launch runs
+// those (each record recomputes the level-0 slots, O(d(v0) + d(v1)) lane-steps / 32,
+// a few percent of a record).
 //
-// Slots live in a per-warp global scratch area (slot count x max degree ints), which
-// stays in L1/L2: a slot is written once per level and read by every later step.
+// Slots live in a per-warp global scratch area ((slot count + 1) x max degree ints),
+// which stays in L1/L2: a slot is written once per level and read by every later step.
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -35,8 +37,10 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 8;       // CSR entries claimed per queue step
-constexpr int kSplitMin = 96;   // v2 candidates above which a task is split
-constexpr int kSplitLen = 32;   // v2 candidates per split record
+// Work of a task in lane-steps (one binary search of one lane): a task above kSplitWork
+// runs its first v2 candidates itself and queues the others as records of about
+// kSplitWork each (about a millisecond of one warp).
+constexpr long long kSplitWork = 4096;
 constexpr int64_t kSplitCap = int64_t(1) << 22;  // records (64 MB)
 
 struct SplitRec {
@@ -180,11 +184,57 @@ __device__ unsigned long long count_op(const ProgOp& o, const WarpState& w, cons
   return c;
 }
 
+// First index of sorted A[0, n) at or above x.
+__device__ __forceinline__ int lower_index(const int32_t* A, int n, int x) {
+  int lo = 0;
+  while (n > 0) {
+    const int h = n >> 1;
+    if (A[lo + h] < x) {
+      lo += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return lo;
+}
+
+// One lane's count for a candidate u whose list N(u) (du entries from rb) is short
+// next to A: each y in N(u) is searched in A instead of each x of A in N(u).  The
+// difference count is the number of A's elements that pass the bound and the
+// exclusions, minus the intersection.
+__device__ unsigned long long count_short(const Operand& A, int u, long long rb, int du, int sbnd,
+                                          bool ubnd, const Excl& ex, bool uex, bool want,
+                                          const int32_t* col) {
+  const int bnd = ubnd ? min(sbnd, u) : sbnd;
+  const int m = lower_index(A.p, A.n, bnd);
+  unsigned long long inter = 0;
+  for (int i = 0; i < du; ++i) {
+    const int y = col[rb + i];
+    if (y >= bnd) break;
+    if (ex.hit(y)) continue;  // y == u cannot occur: no self-loops
+    inter += member(A.p, m, y) ? 1 : 0;
+  }
+  if (want) return inter;
+  long long pass = m;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j) {
+    bool dup = false;
+#pragma unroll
+    for (int i = 0; i < j; ++i) dup |= ex.e[i] == ex.e[j];
+    if (ex.e[j] >= 0 && !dup && member(A.p, m, ex.e[j])) --pass;
+  }
+  if (uex && !ex.hit(u) && member(A.p, m, u)) --pass;
+  return (unsigned long long)(pass - (long long)inter);
+}
+
 // Final count merged with the loop over v_iv (iv = k-2) running over C[lo, hi):
-// one item per (candidate u, element x of the counted operand).
+// one item per (candidate u, element x of the counted operand).  When the second
+// operand is N(u) and A is long, candidates with short lists are counted one per lane
+// by count_short, and only the others (gathered into `big`) take the item walk.
 __device__ unsigned long long count_flat(const ProgOp& o, const WarpState& w, int iv, Operand C,
                                          int lo, int hi, const ProgArgs& a, const int32_t* slots,
-                                         int lane) {
+                                         int32_t* big, int lane) {
   const Operand A = operand(w, o.a, a, slots);
   const unsigned ivbit = 1u << iv;
   const int sbnd = bound_of(w, o.bound & ~ivbit);
@@ -195,9 +245,29 @@ __device__ unsigned long long count_flat(const ProgOp& o, const WarpState& w, in
   const bool b_u = !filter && o.b == kOpList + iv;
   const Operand Bf = (filter || b_u) ? Operand{nullptr, 0} : operand(w, o.b, a, slots);
   const bool want = o.kind == OP_INTERSECT;
-  const int n = hi - lo;
+  int n = hi - lo;
   unsigned long long c = 0;
   if (A.n == 0 || n <= 0) return 0;
+  if (b_u && A.n >= 64) {
+    int nbig = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int ci = base + lane;
+      const bool in = ci < n;
+      const int u = in ? C.p[lo + ci] : 0;
+      const long long rb = in ? a.rowptr[u] : 0;
+      const int du = in ? (int)(a.rowptr[u + 1] - rb) : 0;
+      const bool small = in && 4 * du <= A.n;
+      if (small) c += count_short(A, u, rb, du, sbnd, ubnd, ex, uex, want, a.col);
+      const unsigned mb = __ballot_sync(0xffffffffu, in && !small);
+      if (in && !small) big[nbig + __popc(mb & lanemask_lt())] = u;
+      nbig += __popc(mb);
+    }
+    __syncwarp();
+    C = Operand{big, nbig};
+    lo = 0;
+    n = nbig;
+    if (n == 0) return c;
+  }
   int ci = lane / A.n, ai = lane - ci * A.n;
   while (ci < n) {
     const int u = C.p[lo + ci];
@@ -222,36 +292,72 @@ __device__ unsigned long long count_flat(const ProgOp& o, const WarpState& w, in
   return c;
 }
 
+// Operands whose lengths bound the work of one v2 step: the level-0 slots (bit = slot)
+// and the lists N(v0), N(v1) (bits 16, 17) that every operand read after level 0
+// descends from.
+__device__ unsigned step_roots(const Prog& p) {
+  bool deep[kProgMaxSlots] = {};
+  int8_t from[kProgMaxSlots] = {};
+  for (int l = 1; l < kProgLevels; ++l)
+    for (int i = 0; i < p.nops[l]; ++i) {
+      deep[p.ops[l][i].out] = true;
+      from[p.ops[l][i].out] = p.ops[l][i].a;
+    }
+  unsigned m = 0;
+  auto add = [&](int c) {
+    while (c < kOpList && deep[c]) c = from[c];  // operands are defined before use
+    if (c < kOpList) m |= 1u << c;
+    else if (c - kOpList <= 1) m |= 1u << (16 + c - kOpList);
+  };
+  for (int l = 1; l < kProgLevels; ++l)
+    for (int i = 0; i < p.nops[l]; ++i) add(p.ops[l][i].a);
+  add(p.fin.a);
+  if (p.k == 5) add(p.cand[3]);
+  return m;
+}
+
 template <int K>
-__device__ unsigned long long run_task(const Prog& p, WarpState& w, const ProgArgs& a,
-                                       int32_t* slots, int v0, int v1, long long e, int lo, int hi,
-                                       bool may_split, int lane) {
+__device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState& w,
+                                       const ProgArgs& a, int32_t* slots, int v0, int v1,
+                                       long long e, int lo, int hi, bool may_split, int lane) {
+  int32_t* big = slots + (int64_t)a.nslots * a.slot_cap;  // count_flat's long-list candidates
   set_vertex(w, 0, v0, a, lane);
   set_vertex(w, 1, v1, a, lane);
   for (int i = 0; i < p.nops[0]; ++i) run_op(p.ops[0][i], w, a, slots, lane);
   if (K == 3) return count_op(p.fin, w, a, slots, lane);
   const Operand C2 = operand(w, p.cand[2], a, slots);
   if (hi < 0 || hi > C2.n) hi = C2.n;
-  if (may_split && C2.n > kSplitMin) {
-    const int nrec = (C2.n - kSplitLen + kSplitLen - 1) / kSplitLen;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(a.heads + 1, (unsigned long long)nrec);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    const bool fits = base + nrec <= (unsigned long long)a.split_cap;
-    for (int r = lane; r < nrec; r += 32) {
-      // a claim that crosses the capacity leaves empty records below it; the task
-      // then runs all of its candidates itself
-      if (base + r >= (unsigned long long)a.split_cap) break;
-      const int rlo = kSplitLen * (r + 1);
-      a.split[base + r] = fits ? SplitRec{(int32_t)(e & 0xffffffffLL), (int32_t)(e >> 32), rlo,
-                                          min(rlo + kSplitLen, C2.n)}
-                               : SplitRec{0, 0, 0, 0};
+  if (may_split && C2.n > 1) {
+    // lane-steps of one v2 step: the streams of the level-1 operations, then the
+    // final count over (v3, x) pairs (5 vertices) or over x (4 vertices)
+    int len = 0;
+    for (int j = 0; j < kProgMaxSlots; ++j)
+      if ((roots >> j) & 1u) len = max(len, w.slen[j]);
+    if ((roots >> 16) & 1u) len = max(len, w.vl[0]);
+    if ((roots >> 17) & 1u) len = max(len, w.vl[1]);
+    const long long step = 1 + len / 32 + (K == 5 ? (long long)len * len / 64 : 0);
+    if ((long long)C2.n * step > kSplitWork) {
+      const int per = (int)max(1LL, min((long long)C2.n, kSplitWork / step));
+      const int nrec = (C2.n - per + per - 1) / per;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(a.heads + 1, (unsigned long long)nrec);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const bool fits = base + nrec <= (unsigned long long)a.split_cap;
+      for (int r = lane; r < nrec; r += 32) {
+        // a claim that crosses the capacity leaves empty records below it; the task
+        // then runs all of its candidates itself
+        if (base + r >= (unsigned long long)a.split_cap) break;
+        const int rlo = per * (r + 1);
+        a.split[base + r] = fits ? SplitRec{(int32_t)(e & 0xffffffffLL), (int32_t)(e >> 32), rlo,
+                                            min(rlo + per, C2.n)}
+                                 : SplitRec{0, 0, 0, 0};
+      }
+      if (fits) hi = per;
     }
-    if (fits) hi = kSplitLen;
   }
   unsigned long long c = 0;
   if (K == 4) {
-    if (p.flat) return count_flat(p.fin, w, 2, C2, lo, hi, a, slots, lane);
+    if (p.flat) return count_flat(p.fin, w, 2, C2, lo, hi, a, slots, big, lane);
     for (int i2 = lo; i2 < hi; ++i2) {
       set_vertex(w, 2, C2.p[i2], a, lane);
       for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
@@ -264,7 +370,7 @@ __device__ unsigned long long run_task(const Prog& p, WarpState& w, const ProgAr
     for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
     const Operand C3 = operand(w, p.cand[3], a, slots);
     if (p.flat) {
-      c += count_flat(p.fin, w, 3, C3, 0, C3.n, a, slots, lane);
+      c += count_flat(p.fin, w, 3, C3, 0, C3.n, a, slots, big, lane);
     } else {
       for (int i3 = 0; i3 < C3.n; ++i3) {
         set_vertex(w, 3, C3.p[i3], a, lane);
@@ -293,12 +399,16 @@ __device__ __forceinline__ int row_of(const int64_t* rowptr, int64_t nv, long lo
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_setprog(Prog prog, ProgArgs a) {
   __shared__ Prog p;
+  __shared__ unsigned roots;
   __shared__ WarpState ws[kWarps];
-  if (threadIdx.x == 0) p = prog;
+  if (threadIdx.x == 0) {
+    p = prog;
+    roots = step_roots(prog);
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   WarpState& w = ws[wib];
-  int32_t* slots = a.scratch + ((int64_t)blockIdx.x * kWarps + wib) * a.nslots * a.slot_cap;
+  int32_t* slots = a.scratch + ((int64_t)blockIdx.x * kWarps + wib) * (a.nslots + 1) * a.slot_cap;
   unsigned long long c = 0;
   if (!a.split_mode) {
     for (;;) {
@@ -314,7 +424,7 @@ __global__ void __launch_bounds__(kThreads) k_setprog(Prog prog, ProgArgs a) {
         while (a.rowptr[v0 + 1] <= e) ++v0;
         const int v1 = a.col[e];
         if (p.v1lt && v1 >= v0) continue;
-        c += run_task<K>(p, w, a, slots, v0, v1, e, 0, -1, true, lane);
+        c += run_task<K>(p, roots, w, a, slots, v0, v1, e, 0, -1, true, lane);
       }
     }
   } else {
@@ -331,7 +441,7 @@ __global__ void __launch_bounds__(kThreads) k_setprog(Prog prog, ProgArgs a) {
       int v0 = 0;
       if (lane == 0) v0 = row_of(a.rowptr, a.nv, e);
       v0 = __shfl_sync(0xffffffffu, v0, 0);
-      c += run_task<K>(p, w, a, slots, v0, a.col[e], e, rec.lo, rec.hi, false, lane);
+      c += run_task<K>(p, roots, w, a, slots, v0, a.col[e], e, rec.lo, rec.hi, false, lane);
     }
   }
 #pragma unroll
@@ -376,11 +486,12 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   const int64_t slot_cap = g.max_deg > 0 ? g.max_deg : 1;
   // resident warps, fewer when the scratch would pass 8 GB
   int grid = ctx->num_sms * occupancy(p.k);
-  const int64_t per_block = (int64_t)kWarps * nslots * slot_cap * (int64_t)sizeof(int32_t);
+  // per warp: the program's slots and one list of candidates for count_flat
+  const int64_t per_block = (int64_t)kWarps * (nslots + 1) * slot_cap * (int64_t)sizeof(int32_t);
   const int64_t budget = int64_t(8) << 30;
   if ((int64_t)grid * per_block > budget)
     grid = (int)std::max<int64_t>(ctx->num_sms, budget / per_block);
-  const int64_t need = (int64_t)grid * kWarps * nslots * slot_cap;
+  const int64_t need = (int64_t)grid * kWarps * (nslots + 1) * slot_cap;
   if (need > ctx->prog_scratch_cap) {
     if (ctx->prog_scratch) XGM_CUDA_TRY(cudaFreeAsync(ctx->prog_scratch, s));
     ctx->prog_scratch = nullptr;
