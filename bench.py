@@ -52,9 +52,11 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="clique", choices=["clique", "batch", "motifs"],
+    p.add_argument("--workload", default="clique",
+                   choices=["clique", "batch", "motifs", "patterns5"],
                    help="clique: k-clique counting on R-MAT s22; batch: 4096 BA graphs; "
-                        "motifs: edge-induced 4-vertex motifs on ER and Chung-Lu 2^21")
+                        "motifs: edge-induced 4-vertex motifs on ER and Chung-Lu 2^21; "
+                        "patterns5: GLUMIN's 5-vertex plans P6-P22 on R-MAT s12 and ER 2^16")
     p.add_argument("--graphs", type=int, default=4096)
     return p.parse_args()
 
@@ -520,6 +522,63 @@ def motifs_arm(args, dist: Dist) -> None:
     ctx.close()
 
 
+def patterns5_arm(args, dist: Dist) -> None:
+    """GLUMIN's vertex-induced 5-vertex plans P6..P22 (set-operation programs) on an
+    R-MAT graph (scale 12, edge factor 8, seed 3; maximum degree 941) and an Erdos-Renyi
+    G(n = 2^16, average degree 16), seeded.  One step counts all 17 plans on both graphs;
+    matches/s = total count / total device time.  CPU baseline: the oracle's restatement
+    of the same plans on the host cores, every plan on the ER graph."""
+    import torch
+
+    xgm = load_engine()
+    torch.cuda.set_device(dist.local)
+    ctx = xgm.Context(dist.local)
+    graphs = {"rmat_s12_ef8": xgm.gen_rmat(12, 8, seed=3),
+              "er_2^16_deg16": xgm.gen_er(1 << 16, 1 << 19, seed=3)}
+    per, total_ms, total_matches, info, launches = {}, 0.0, 0, {}, 0
+    for gname, (nv, src, dst) in graphs.items():
+        g = ctx.graph_from_edges(nv, src, dst)
+        info[gname] = g.info()
+        for pid in range(6, 23):
+            pat = f"P{pid}"
+            for _ in range(args.warmup):
+                ctx.count(g, pat)
+            _sync()
+            ms, cnt = [], 0
+            for _ in range(args.steps):
+                cnt, st = ctx.count(g, pat, with_stats=True)
+                ms.append(st["kernel_ms"] + st["prep_ms"])
+                launches += st["launches"]
+            per[f"{gname}/{pat}"] = {"count": cnt, "ms": statistics.mean(ms)}
+            total_ms += statistics.mean(ms)
+            total_matches += cnt
+        g.close()
+    line = {"metric": "matches_per_sec", "value": total_matches / (total_ms / 1e3),
+            "unit": "matches/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32 ids / uint64 counts",
+            "data": "synthetic (seeded R-MAT and Erdos-Renyi)",
+            "config": {"workload": "GLUMIN P6-P22 (vertex-induced 5-vertex plans), R-MAT s12 "
+                                   "ef8 and ER 2^16 deg 16", "graphs": info},
+            "gpu_launches": launches // max(1, args.steps), "per_pattern": per}
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        import oracle
+
+        nv, src, dst = graphs["er_2^16_deg16"]
+        rowptr, col = oracle.build_csr(nv, src, dst)
+        cores = oracle.threads()
+        t0 = time.perf_counter()
+        c = sum(oracle.glumin5(pid, rowptr, col) for pid in range(6, 23))
+        dt = time.perf_counter() - t0
+        gpu_ms = sum(v["ms"] for k, v in per.items() if k.startswith("er_"))
+        line["cpu_baseline"] = {"value": c / dt, "unit": "matches/s", "cores": cores,
+                                "kind": "port",
+                                "sample": f"P6-P22 on the ER graph ({c} matches in {dt:.2f} s, "
+                                          f"OpenMP oracle port; the GPU took {gpu_ms:.1f} ms)"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -530,6 +589,8 @@ def main():
             batch_arm(args, dist)
         elif args.workload == "motifs":
             motifs_arm(args, dist)
+        elif args.workload == "patterns5":
+            patterns5_arm(args, dist)
         else:
             engine_arm(args, dist)
     finally:

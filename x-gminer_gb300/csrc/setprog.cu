@@ -15,9 +15,8 @@
 // candidate list and the counted operand, so a warp keeps all 32 lanes busy when the
 // lists are short, which they mostly are on sparse graphs.  A task whose estimated
 // work (v2 candidates x the cost of one v2 step, from the lengths of the level-0
-// slots the later steps read) passes kSplitWork keeps its first v2 candidates and
-// queues the rest as split records of about kSplitWork each; a second launch runs
-// those (each record recomputes the level-0 slots, O(d(v0) + d(v1)) lane-steps / 32,
+// slots the later steps read) passes kSplitWork queues its v2 candidates as split
+// records of about kSplitWork each; a second launch runs those (each record recomputes the level-0 slots, O(d(v0) + d(v1)) lane-steps / 32,
 // a few percent of a record).
 //
 // Slots live in a per-warp global scratch area ((slot count + 1) x max degree ints),
@@ -38,8 +37,8 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 8;       // CSR entries claimed per queue step
 // Work of a task in lane-steps (one binary search of one lane): a task above kSplitWork
-// runs its first v2 candidates itself and queues the others as records of about
-// kSplitWork each (about a millisecond of one warp).
+// queues its v2 candidates as records of about kSplitWork each (about a millisecond
+// of one warp).
 constexpr long long kSplitWork = 4096;
 constexpr int64_t kSplitCap = int64_t(1) << 22;  // records (64 MB)
 
@@ -337,8 +336,10 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
     if ((roots >> 17) & 1u) len = max(len, w.vl[1]);
     const long long step = 1 + len / 32 + (K == 5 ? (long long)len * len / 64 : 0);
     if ((long long)C2.n * step > kSplitWork) {
+      // every candidate goes to the records, so a warp that claims a chunk of heavy
+      // tasks only builds their level-0 slots
       const int per = (int)max(1LL, min((long long)C2.n, kSplitWork / step));
-      const int nrec = (C2.n - per + per - 1) / per;
+      const int nrec = (C2.n + per - 1) / per;
       unsigned long long base = 0;
       if (lane == 0) base = atomicAdd(a.heads + 1, (unsigned long long)nrec);
       base = __shfl_sync(0xffffffffu, base, 0);
@@ -347,12 +348,12 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
         // a claim that crosses the capacity leaves empty records below it; the task
         // then runs all of its candidates itself
         if (base + r >= (unsigned long long)a.split_cap) break;
-        const int rlo = per * (r + 1);
+        const int rlo = per * r;
         a.split[base + r] = fits ? SplitRec{(int32_t)(e & 0xffffffffLL), (int32_t)(e >> 32), rlo,
                                             min(rlo + per, C2.n)}
                                  : SplitRec{0, 0, 0, 0};
       }
-      if (fits) hi = per;
+      if (fits) return 0;
     }
   }
   unsigned long long c = 0;
@@ -397,7 +398,7 @@ __device__ __forceinline__ int row_of(const int64_t* rowptr, int64_t nv, long lo
 }
 
 template <int K>
-__global__ void __launch_bounds__(kThreads) k_setprog(Prog prog, ProgArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) {
   __shared__ Prog p;
   __shared__ unsigned roots;
   __shared__ WarpState ws[kWarps];

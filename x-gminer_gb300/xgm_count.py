@@ -21,9 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 xgm = importlib.import_module("x-gminer_gb300")
 
-# xgminer patternIDs of the supported GLUMIN patterns (xgminer/include/glumin.h:34-39
-# maps patternID - 16 to GLUMIN's P-number): P1-P5, P23 (6-clique), P24 (7-clique)
-PATTERN_IDS = {17: "P1", 18: "P2", 19: "P3", 20: "P4", 21: "P5", 39: "P23", 40: "P24"}
+# xgminer patternIDs of the GLUMIN patterns (xgminer/include/glumin.h:34-39 maps
+# patternID - 16 to GLUMIN's P-number): every one of P1-P24
+PATTERN_IDS = {i: f"P{i - 16}" for i in range(17, 41)}
 
 
 def main() -> None:
@@ -34,7 +34,7 @@ def main() -> None:
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--pattern", default="4-clique")
     ap.add_argument("--patternID", type=int,
-                    help="xgminer pattern id: 17-21 = GLUMIN P1-P5, 39 / 40 = P23 / P24")
+                    help="xgminer pattern id: 17-40 = GLUMIN P1-P24")
     ap.add_argument("--policy", choices=["heuristic", "learned"], default="heuristic")
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
