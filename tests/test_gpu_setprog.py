@@ -54,7 +54,9 @@ def test_glumin5_vs_oracle_and_split(xgm, ctx, orc):
         for pid in range(6, 23):
             got, st = ctx.count(g, f"P{pid}", with_stats=True)
             assert got == orc.glumin5(pid, rowptr, col), pid
-            assert st["launches"] == 2 and st["tasks"] == len(col)
+            # bitmap launch (small-degree v0) where the plan allows it, task launch, split
+            # launch
+            assert st["launches"] in (2, 3) and st["tasks"] == len(col)
             split += st["variant_tasks"][xgm.VAR_SPLIT]
         g.close()
     assert split > 0  # the hub graph's long candidate lists went through split records

@@ -243,6 +243,50 @@ bool prog_compile(int k, const uint8_t adj[8][8], bool induced, Prog* out, std::
   return true;
 }
 
+// GLUMIN's LUT kernels (GM_LUT_kernels/P*.yml.cuh with codegen_LUT.cuh) run the
+// same plans on a bitmap of the adjacency among N(v0); this decides whether a program
+// has that shape.
+bool prog_lut(const Prog& p, ProgLut* out) {
+  ProgLut r;
+  if (p.k < 4 || p.k > 5) return *out = r, false;
+  // space of each slot: 1 = subset of N(v0) (bitmap), 2 = the N(v1) \ N(v0) stream
+  int8_t space[kProgMaxSlots] = {};
+  auto n0 = [&](int code) { return code == G(0) || (code < kOpList && space[code] == 1); };
+  for (int i = 0; i < p.nops[0]; ++i) {
+    const ProgOp& o = p.ops[0][i];
+    if (n0(o.a) || (o.a == G(1) && o.b == G(0) && o.kind == OP_INTERSECT)) {
+      space[o.out] = 1;
+    } else if (o.a == G(1) && o.b == G(0) && o.kind == OP_DIFFERENCE && o.out == p.cand[2] &&
+               r.stream < 0) {
+      space[o.out] = 2;
+      r.stream = (int8_t)i;
+    } else {
+      return *out = ProgLut{}, false;
+    }
+  }
+  // the stream feeds the v2 loop only
+  auto uses = [&](int code) {
+    for (int l = 1; l < kProgLevels; ++l)
+      for (int i = 0; i < p.nops[l]; ++i)
+        if (p.ops[l][i].a == code) return true;
+    return p.fin.a == code || (p.k == 5 && p.cand[3] == code);
+  };
+  if (r.stream >= 0 && uses(p.ops[0][r.stream].out)) return *out = ProgLut{}, false;
+  if (!(n0(p.cand[2]) || (p.cand[2] < kOpList && space[p.cand[2]] == 2)))
+    return *out = ProgLut{}, false;
+  for (int l = 1; l <= p.k - 3; ++l)
+    for (int i = 0; i < p.nops[l]; ++i) {
+      const ProgOp& o = p.ops[l][i];
+      if (!n0(o.a)) return *out = ProgLut{}, false;
+      space[o.out] = 1;
+    }
+  if (p.k == 5 && !n0(p.cand[3])) return *out = ProgLut{}, false;
+  if (!n0(p.fin.a)) return *out = ProgLut{}, false;
+  r.ok = 1;
+  *out = r;
+  return true;
+}
+
 bool prog_check(const Prog& p, std::string* why) {
   if (p.k < 3 || p.k > kProgMaxK) return fail(why, "k out of range"), false;
   if (p.nslots < 0 || p.nslots > kProgMaxSlots) return fail(why, "slot count out of range"), false;

@@ -54,12 +54,23 @@ struct ProgArgs {
   int32_t* scratch;
   int64_t slot_cap;   // ints per slot
   int nslots;
-  unsigned long long* heads;  // [0] entry head, [1] split tail, [2] split head
+  unsigned long long* heads;  // [0] entry head, [1] split tail, [2] split head, [3] v0 head (bitmap form)
   SplitRec* split;
   int64_t split_cap;
   unsigned long long* total;
   int split_mode;
+  int lut_ok;      // the bitmap kernel takes the tasks with small v0 (ProgLut)
+  int lut_stream;  // its stream operation, or -1
 };
+
+// Bitmap form: a v0 of degree up to kLutDeg runs in k_setlut, one lane per (v0, v1)
+// task; for stream programs only while d(v1) <= kLutStream (the lane walks N(v1)).
+constexpr int kLutDeg = 32;
+constexpr int kLutStream = 32;
+
+__device__ __forceinline__ bool lut_task_taken(const ProgArgs& a, int d0, int d1) {
+  return a.lut_ok && d0 <= kLutDeg && (a.lut_stream < 0 || d1 <= kLutStream);
+}
 
 struct WarpState {
   int v[kProgMaxK];
@@ -425,6 +436,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) 
         while (a.rowptr[v0 + 1] <= e) ++v0;
         const int v1 = a.col[e];
         if (p.v1lt && v1 >= v0) continue;
+        if (a.lut_ok && lut_task_taken(a, (int)(a.rowptr[v0 + 1] - a.rowptr[v0]),
+                                       (int)(a.rowptr[v1 + 1] - a.rowptr[v1])))
+          continue;
         c += run_task<K>(p, roots, w, a, slots, v0, v1, e, 0, -1, true, lane);
       }
     }
@@ -450,10 +464,203 @@ __global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) 
   if (lane == 0 && c) atomicAdd(a.total, c);
 }
 
+// ------------------------------------------------------------------ bitmap form
+// GLUMIN's LUT kernels (GM_LUT_kernels/P*.yml.cuh, codegen_LUT.cuh) keep the adjacency
+// among N(v0) as bit rows and run the plan on them.  Here a warp takes one v0 of
+// degree <= 32: N(v0) and its 32-bit rows (row i = the N(v0) indices adjacent to
+// N(v0)[i]) sit in shared memory, and each lane runs one task (v0, v1) on 32-bit masks
+// in N(v0) index space: an intersection is an AND with a row, a difference an AND with
+// its complement, a bound (x < v_j) a prefix mask (N(v0) is sorted), an exclusion one
+// cleared bit, and the count a popc.  The row of v0 is all of N(v0); a v2 from the
+// stream N(v1) \ N(v0) is not in that space and gets its row built on the fly.
+
+// Bits of N(v0) (n0[0, d0), sorted) adjacent to y: a merge when N(y) is short, else a
+// binary search of each N(v0) element in N(y).
+__device__ uint32_t row_over(const int32_t* n0, int d0, int y, const ProgArgs& a) {
+  const long long rb = a.rowptr[y];
+  const int dy = (int)(a.rowptr[y + 1] - rb);
+  uint32_t r = 0;
+  if (dy <= 8 * d0) {
+    int i = 0;
+    for (int j = 0; j < dy && i < d0; ++j) {
+      const int z = a.col[rb + j];
+      while (i < d0 && n0[i] < z) ++i;
+      if (i < d0 && n0[i] == z) r |= 1u << i;
+    }
+  } else {
+    for (int i = 0; i < d0; ++i)
+      if (member(a.col + rb, dy, n0[i])) r |= 1u << i;
+  }
+  return r;
+}
+
+struct LutLane {
+  int v[kProgMaxK];    // matched ids
+  int idx[kProgMaxK];  // index in N(v0), or -1
+  int pre[kProgMaxK];  // elements of N(v0) below v_j
+  uint32_t row[kProgMaxK];
+};
+
+__device__ __forceinline__ uint32_t row_of_code(const LutLane& L, int code) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j)
+    if (code == kOpList + j) r = L.row[j];
+  return r;
+}
+
+// prefix mask of the bound (x < min v_j) and the exclusion mask, over matched vertices
+__device__ __forceinline__ uint32_t keep_mask(const LutLane& L, const ProgOp& o, uint32_t valid) {
+  int pb = 32;
+  uint32_t ex = 0;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j) {
+    if ((o.bound >> j) & 1u) pb = min(pb, L.pre[j]);
+    if (((o.excl >> j) & 1u) && L.idx[j] >= 0) ex |= 1u << L.idx[j];
+  }
+  const uint32_t pm = pb >= 32 ? 0xffffffffu : ((1u << pb) - 1u);
+  return valid & pm & ~ex;
+}
+
+__device__ __forceinline__ uint32_t lut_apply(const LutLane& L, const ProgOp& o, uint32_t A,
+                                              uint32_t valid) {
+  uint32_t r = A;
+  if (o.kind == OP_INTERSECT) r &= row_of_code(L, o.b);
+  else if (o.kind == OP_DIFFERENCE) r &= ~row_of_code(L, o.b);
+  return r & keep_mask(L, o, valid);
+}
+
+__device__ __forceinline__ uint32_t lut_operand(const LutLane& L, int code, const uint32_t* sl,
+                                                uint32_t valid) {
+  if (code == kOpList) return valid;               // N(v0)
+  if (code == kOpList + 1) return L.row[1];        // N(v1) n N(v0), the only use of N(v1)
+  return sl[code * 32];
+}
+
+__device__ __forceinline__ void lut_set(LutLane& L, int j, int x, int i, const int32_t* n0, int d0) {
+  L.v[j] = x;
+  L.idx[j] = i;
+  L.pre[j] = i >= 0 ? i : lower_index(n0, d0, x);
+}
+
+template <int K>
+__device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, uint32_t* sl,
+                                        uint32_t valid) {
+  for (int i = 0; i < p.nops[l]; ++i) {
+    const ProgOp& o = p.ops[l][i];
+    sl[o.out * 32] = lut_apply(L, o, lut_operand(L, o.a, sl, valid), valid);
+  }
+  if (l == K - 3) return (unsigned long long)__popc(lut_apply(L, p.fin, lut_operand(L, p.fin.a, sl, valid), valid));
+  return 0;
+}
+
+// One (v0, v1) task on masks; sl = this lane's slots (stride 32).
+template <int K>
+__device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0, int i1, int d0,
+                                       const int32_t* n0, const uint32_t* lut, uint32_t* sl) {
+  const int v1 = n0[i1];
+  if (p.v1lt && v1 >= v0) return 0;
+  const long long rb1 = a.rowptr[v1];
+  const int d1 = (int)(a.rowptr[v1 + 1] - rb1);
+  if (!lut_task_taken(a, d0, d1)) return 0;  // the list kernel runs it
+  const uint32_t valid = d0 >= 32 ? 0xffffffffu : ((1u << d0) - 1u);
+  LutLane L;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j) L.v[j] = -1, L.idx[j] = -1, L.pre[j] = 0, L.row[j] = 0;
+  lut_set(L, 0, v0, -1, n0, d0);
+  L.row[0] = valid;
+  lut_set(L, 1, v1, i1, n0, d0);
+  L.row[1] = lut[i1];
+  for (int i = 0; i < p.nops[0]; ++i) {
+    if (i == a.lut_stream) continue;
+    const ProgOp& o = p.ops[0][i];
+    sl[o.out * 32] = lut_apply(L, o, lut_operand(L, o.a, sl, valid), valid);
+  }
+  unsigned long long c = 0;
+  auto step2 = [&]() {
+    if (K == 4) {
+      c += lut_level<K>(p, 1, L, sl, valid);
+      return;
+    }
+    lut_level<K>(p, 1, L, sl, valid);
+    for (uint32_t m = lut_operand(L, p.cand[3], sl, valid); m; m &= m - 1) {
+      const int b = __ffs(m) - 1;
+      lut_set(L, 3, n0[b], b, n0, d0);
+      L.row[3] = lut[b];
+      c += lut_level<K>(p, 2, L, sl, valid);
+    }
+  };
+  if (a.lut_stream >= 0) {
+    // v2 over N(v1) \ N(v0), below the operation's bound, minus its exclusions
+    const ProgOp& o = p.ops[0][a.lut_stream];
+    int ub = INT_MAX;
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+      if ((o.bound >> j) & 1u) ub = min(ub, L.v[j]);
+    int i = 0;
+    for (int t = 0; t < d1; ++t) {
+      const int y = a.col[rb1 + t];
+      if (y >= ub) break;
+      while (i < d0 && n0[i] < y) ++i;
+      if (i < d0 && n0[i] == y) continue;
+      if ((((o.excl >> 0) & 1u) && y == v0) || (((o.excl >> 1) & 1u) && y == v1)) continue;
+      lut_set(L, 2, y, -1, n0, d0);
+      L.row[2] = row_over(n0, d0, y, a);
+      step2();
+    }
+  } else {
+    for (uint32_t m = lut_operand(L, p.cand[2], sl, valid); m; m &= m - 1) {
+      const int b = __ffs(m) - 1;
+      lut_set(L, 2, n0[b], b, n0, d0);
+      L.row[2] = lut[b];
+      step2();
+    }
+  }
+  return c;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
+  __shared__ Prog p;
+  __shared__ int32_t n0s[kWarps][32];
+  __shared__ uint32_t luts[kWarps][32];
+  __shared__ uint32_t sls[kWarps][kProgMaxSlots * 32];
+  if (threadIdx.x == 0) p = prog;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned long long c = 0;
+  for (;;) {
+    unsigned long long v0 = 0;
+    if (lane == 0) v0 = atomicAdd(a.heads + 3, 1ull);
+    v0 = __shfl_sync(0xffffffffu, v0, 0);
+    if ((long long)v0 >= a.nv) break;
+    {
+      const long long rb = a.rowptr[v0];
+      const int d0 = (int)(a.rowptr[v0 + 1] - rb);
+      if (d0 == 0 || d0 > kLutDeg) continue;
+      if (lane < d0) n0s[wib][lane] = a.col[rb + lane];
+      __syncwarp();
+      if (lane < d0) luts[wib][lane] = row_over(n0s[wib], d0, n0s[wib][lane], a);
+      __syncwarp();
+      if (lane < d0)
+        c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane]);
+      __syncwarp();
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0 && c) atomicAdd(a.total, c);
+}
+
 template <int K>
 cudaError_t launch_k(const Prog& p, const ProgArgs& a, int grid, cudaStream_t s) {
   ProgArgs b = a;
   b.split_mode = 0;
+  if (K >= 4 && a.lut_ok) {
+    k_setlut<K><<<grid, kThreads, 0, s>>>(p, b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   k_setprog<K><<<grid, kThreads, 0, s>>>(p, b);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || K == 3) return e;
@@ -519,13 +726,16 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   a.split_cap = kSplitCap;
   a.total = &ctx->d_sc->count;
   a.split_mode = 0;
+  ProgLut lut;
+  a.lut_ok = prog_lut(p, &lut) ? 1 : 0;
+  a.lut_stream = lut.stream;
   int launches = 0;
   if (g.ne > 0) {
     cudaError_t e = p.k == 3   ? launch_k<3>(p, a, grid, s)
                     : p.k == 4 ? launch_k<4>(p, a, grid, s)
                                : launch_k<5>(p, a, grid, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_setprog", __FILE__, __LINE__);
-    launches = p.k == 3 ? 1 : 2;
+    launches = p.k == 3 ? 1 : (a.lut_ok ? 3 : 2);
   }
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->prog_heads + 1, sizeof(int64_t),

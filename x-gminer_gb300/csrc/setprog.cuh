@@ -64,6 +64,16 @@ bool prog_from_words(const int32_t* w, int n, Prog* p, std::string* why);
 // vertices.
 bool prog_check(const Prog& p, std::string* why);
 
+// Bitmap (LUT) form: whether the program runs in the index space of N(v0) — every
+// operand read after level 0, the v3 candidates and the counted operand descend from
+// N(v0); the v2 candidates may instead be the stream N(v1) \ N(v0) (one level-0
+// difference, `stream`), whose vertices get their rows built on the fly.
+struct ProgLut {
+  int8_t ok = 0;
+  int8_t stream = -1;  // index of the level-0 operation giving cand[2] from N(v1), or -1
+};
+bool prog_lut(const Prog& p, ProgLut* out);
+
 // GLUMIN's P6..P22 (vertex-induced 5-vertex plans), exactly as generated.
 bool prog_glumin(int pid, Prog* p);
 // A program counting each occurrence of the pattern (k vertices, symmetric 0/1
