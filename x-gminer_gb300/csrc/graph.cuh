@@ -27,6 +27,12 @@ struct DevGraph {
   mutable int32_t* bcol = nullptr;
   mutable uint32_t* boff = nullptr;
   mutable uint16_t* bmask = nullptr;
+  // adjacency rows among N(v) for v of degree 33..1024 (setprog.cu), built on first use
+  // by a set-operation program: lut_off[v] words into lut_rows; lut_state 1 built,
+  // -1 not built (too large)
+  mutable uint32_t* lut_rows = nullptr;
+  mutable int64_t* lut_off = nullptr;
+  mutable int lut_state = 0;
 
   GView view() const { return GView{col, rowptr, dptr, nv, bcol, boff, bmask}; }
 };

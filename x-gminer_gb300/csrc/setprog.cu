@@ -27,6 +27,7 @@
 
 #include "api_internal.h"
 #include "graph.cuh"
+#include "prim.cuh"
 #include "setprog.cuh"
 
 namespace xgm {
@@ -61,12 +62,18 @@ struct ProgArgs {
   int split_mode;
   int lut_ok;      // the bitmap kernel takes the tasks with small v0 (ProgLut)
   int lut_stream;  // its stream operation, or -1
+  const uint32_t* lut_rows;  // stored rows of v0 with degree 33..1024 (or null)
+  const int64_t* lut_off;
 };
 
 // Bitmap form: a v0 of degree up to kLutDeg runs in k_setlut, one lane per (v0, v1)
 // task; for stream programs only while d(v1) <= kLutStream (the lane walks N(v1)).
 constexpr int kLutDeg = 32;
 constexpr int kLutStream = 32;
+// A v0 of degree kLutDeg < d0 <= kLutMed runs its tasks in the warp-wide bitmap form
+// (one word of N(v0) index space per lane) on the graph's stored rows.
+constexpr int kLutMed = 1024;
+constexpr int64_t kLutBudget = int64_t(4) << 30;  // bytes of stored rows at most
 
 __device__ __forceinline__ bool lut_task_taken(const ProgArgs& a, int d0, int d1) {
   return a.lut_ok && d0 <= kLutDeg && (a.lut_stream < 0 || d1 <= kLutStream);
@@ -77,6 +84,12 @@ struct WarpState {
   int vl[kProgMaxK];
   long long vb[kProgMaxK];
   int slen[kProgMaxSlots];
+  // warp-wide bitmap form: index in N(v0) (or -1), elements of N(v0) below v_j, the
+  // slots (one word per lane) and the row of a v2 outside N(v0)
+  int idx[kProgMaxK];
+  int pre[kProgMaxK];
+  uint32_t bits[kProgMaxSlots][32];
+  uint32_t rowbuf[32];
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -408,6 +421,308 @@ __device__ __forceinline__ int row_of(const int64_t* rowptr, int64_t nv, long lo
   return (int)(lo - 1);
 }
 
+// ------------------------------------------------------- warp-wide bitmap form
+// For a v0 of degree 33..1024 the tasks of a bitmap-eligible program run on the
+// graph's stored rows (row i = the N(v0) indices adjacent to N(v0)[i], W = d0/32
+// words): lane w owns word w of every N(v0)-space slot, an operation is one AND /
+// AND-NOT per lane, and the final count one AND + popc per lane per v3 instead of
+// binary searches.  A v2 from the stream N(v1) \ N(v0) gets its row built into
+// `rowbuf` (each lane searches its share of N(v2) in N(v0)).
+
+__device__ __forceinline__ bool bits_task(const ProgArgs& a, int d0) {
+  return a.lut_ok && a.lut_rows && d0 > kLutDeg && d0 <= kLutMed;
+}
+
+struct BitsCtx {
+  const int32_t* n0;    // N(v0)
+  const uint32_t* row;  // stored rows of v0
+  int d0, W;
+  uint32_t valid;       // this lane's word of [0, d0)
+  bool act;             // lane < W
+};
+
+__device__ __forceinline__ uint32_t bits_row(const WarpState& w, const BitsCtx& B, int code,
+                                             int lane) {
+  const int j = code - kOpList;
+  if (j == 0) return B.valid;
+  const int i = w.idx[j];
+  if (i >= 0) return B.act ? B.row[(int64_t)i * B.W + lane] : 0u;
+  return w.rowbuf[lane];
+}
+
+__device__ __forceinline__ uint32_t bits_keep(const WarpState& w, const BitsCtx& B, const ProgOp& o,
+                                              int lane) {
+  int pb = INT_MAX;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j)
+    if ((o.bound >> j) & 1u) pb = min(pb, w.pre[j]);
+  const int lo = 32 * lane;
+  uint32_t m = pb >= lo + 32 ? 0xffffffffu : (pb <= lo ? 0u : ((1u << (pb - lo)) - 1u));
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j)
+    if (((o.excl >> j) & 1u) && w.idx[j] >= lo && w.idx[j] < lo + 32) m &= ~(1u << (w.idx[j] - lo));
+  return m & B.valid;
+}
+
+__device__ __forceinline__ uint32_t bits_operand(const WarpState& w, const BitsCtx& B, int code,
+                                                 int lane) {
+  if (code == kOpList) return B.valid;                  // N(v0)
+  if (code == kOpList + 1) return bits_row(w, B, code, lane);  // N(v1) n N(v0)
+  return w.bits[code][lane];
+}
+
+__device__ __forceinline__ uint32_t bits_apply(const WarpState& w, const BitsCtx& B, const ProgOp& o,
+                                               uint32_t A, int lane) {
+  if (o.kind == OP_INTERSECT) A &= bits_row(w, B, o.b, lane);
+  else if (o.kind == OP_DIFFERENCE) A &= ~bits_row(w, B, o.b, lane);
+  return A & bits_keep(w, B, o, lane);
+}
+
+__device__ __forceinline__ void bits_level(const Prog& p, int l, WarpState& w, const BitsCtx& B,
+                                           int lane) {
+  for (int i = 0; i < p.nops[l]; ++i) {
+    const ProgOp& o = p.ops[l][i];
+    w.bits[o.out][lane] = bits_apply(w, B, o, bits_operand(w, B, o.a, lane), lane);
+  }
+}
+
+__device__ __forceinline__ void bits_set(WarpState& w, int j, int x, int i, int pre, int lane) {
+  if (lane == 0) {
+    w.v[j] = x;
+    w.idx[j] = i;
+    w.pre[j] = pre;
+  }
+  __syncwarp();
+}
+
+// Word wi of the N(v0)-space operands, read by any lane (for bits_flat_fin).
+__device__ __forceinline__ uint32_t valid_word(const BitsCtx& B, int wi) {
+  return (wi < B.W - 1 || (B.d0 & 31) == 0) ? 0xffffffffu : ((1u << (B.d0 & 31)) - 1u);
+}
+
+__device__ __forceinline__ uint32_t row_word(const WarpState& w, const BitsCtx& B, int j, int wi) {
+  if (j == 0) return valid_word(B, wi);
+  const int i = w.idx[j];
+  return i >= 0 ? B.row[(int64_t)i * B.W + wi] : w.rowbuf[wi];
+}
+
+__device__ __forceinline__ uint32_t operand_word(const WarpState& w, const BitsCtx& B, int code,
+                                                 int wi) {
+  if (code == kOpList) return valid_word(B, wi);
+  if (code == kOpList + 1) return row_word(w, B, 1, wi);
+  return w.bits[code][wi];
+}
+
+// The final count with the v3 loop spread over lanes: the v3 candidates (bits of c3w,
+// one word per lane) are compacted into `list`, then each lane counts one v3 over all
+// W words.  For the programs whose last level is the count alone.
+__device__ unsigned long long bits_flat_fin(const Prog& p, const WarpState& w, const BitsCtx& B,
+                                            uint32_t c3w, int32_t* list, int lane) {
+  const int cnt = __popc(c3w);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int n3 = __shfl_sync(0xffffffffu, incl, 31);
+  int pos = incl - cnt;
+  for (uint32_t m = c3w; m; m &= m - 1) list[pos++] = lane * 32 + __ffs(m) - 1;
+  __syncwarp();
+  const ProgOp& o = p.fin;
+  int pbs = INT_MAX, ex[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    if ((o.bound >> j) & 1u) pbs = min(pbs, w.pre[j]);
+    ex[j] = ((o.excl >> j) & 1u) ? w.idx[j] : -1;
+  }
+  const bool ub = (o.bound >> 3) & 1u, ux = (o.excl >> 3) & 1u;
+  const int jb = o.kind == OP_FILTER ? -1 : o.b - kOpList;
+  unsigned long long c = 0;
+  for (int t = lane; t < n3; t += 32) {
+    const int b3 = list[t];
+    const int pb = ub ? min(pbs, b3) : pbs;
+    for (int wi = 0; wi < B.W; ++wi) {
+      const int lo = 32 * wi;
+      if (pb <= lo) break;  // the bound's prefix ends here
+      uint32_t keep = valid_word(B, wi) & (pb >= lo + 32 ? 0xffffffffu : ((1u << (pb - lo)) - 1u));
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (ex[j] >= lo && ex[j] < lo + 32) keep &= ~(1u << (ex[j] - lo));
+      if (ux && b3 >= lo && b3 < lo + 32) keep &= ~(1u << (b3 - lo));
+      uint32_t A = operand_word(w, B, o.a, wi);
+      if (jb >= 0) {
+        const uint32_t r = jb == 3 ? B.row[(int64_t)b3 * B.W + wi] : row_word(w, B, jb, wi);
+        A = o.kind == OP_INTERSECT ? (A & r) : (A & ~r);
+      }
+      c += __popc(A & keep);
+    }
+  }
+  __syncwarp();
+  return c;
+}
+
+// v2 fixed: the level-1 operations, then the v3 loop (5 vertices) or the count.
+template <int K>
+__device__ unsigned long long bits_step2(const Prog& p, WarpState& w, const BitsCtx& B,
+                                         int32_t* list, int lane) {
+  bits_level(p, 1, w, B, lane);
+  if (K == 4) return (unsigned long long)__popc(bits_apply(w, B, p.fin, bits_operand(w, B, p.fin.a, lane), lane));
+  __syncwarp();  // the level-1 slots are read across lanes below
+  const uint32_t c3 = bits_operand(w, B, p.cand[3], lane);
+  if (p.nops[2] == 0) return bits_flat_fin(p, w, B, c3, list, lane);
+  unsigned long long c = 0;
+  for (int wi = 0; wi < B.W; ++wi) {
+    for (uint32_t m = __shfl_sync(0xffffffffu, c3, wi); m; m &= m - 1) {
+      const int b = wi * 32 + __ffs(m) - 1;
+      bits_set(w, 3, B.n0[b], b, b, lane);
+      bits_level(p, 2, w, B, lane);
+      c += __popc(bits_apply(w, B, p.fin, bits_operand(w, B, p.fin.a, lane), lane));
+    }
+  }
+  return c;
+}
+
+template <int K>
+__device__ unsigned long long run_task_bits(const Prog& p, WarpState& w, const ProgArgs& a,
+                                            int32_t* slots, int v0, int v1, long long e, int lo,
+                                            int hi, bool may_split, int lane) {
+  set_vertex(w, 0, v0, a, lane);
+  set_vertex(w, 1, v1, a, lane);
+  int32_t* list = slots + (int64_t)a.nslots * a.slot_cap;  // v3 candidates (bits_flat_fin)
+  BitsCtx B;
+  B.d0 = w.vl[0];
+  B.W = (B.d0 + 31) >> 5;
+  B.n0 = a.col + w.vb[0];
+  B.row = a.lut_rows + a.lut_off[v0];
+  B.act = lane < B.W;
+  B.valid = !B.act ? 0u
+                   : ((lane < B.W - 1 || (B.d0 & 31) == 0) ? 0xffffffffu
+                                                           : ((1u << (B.d0 & 31)) - 1u));
+  const int i1 = lower_index(B.n0, B.d0, v1);
+  if (lane == 0) {
+    w.idx[0] = -1;
+    w.pre[0] = lower_index(B.n0, B.d0, v0);
+    w.idx[1] = i1;
+    w.pre[1] = i1;
+  }
+  __syncwarp();
+  for (int i = 0; i < p.nops[0]; ++i) {
+    const ProgOp& o = p.ops[0][i];
+    if (i == a.lut_stream) run_op(o, w, a, slots, lane);  // the v2 list N(v1) \ N(v0)
+    else w.bits[o.out][lane] = bits_apply(w, B, o, bits_operand(w, B, o.a, lane), lane);
+  }
+  __syncwarp();
+  const bool stream = a.lut_stream >= 0;
+  const Operand C2 = stream ? operand(w, p.cand[2], a, slots) : Operand{nullptr, 0};
+  const uint32_t c2w = stream ? 0u : bits_operand(w, B, p.cand[2], lane);
+  int n2 = stream ? C2.n : __popc(c2w);
+  if (!stream) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+  }
+  if (hi < 0 || hi > n2) hi = n2;
+  if (may_split && n2 > 1) {
+    const long long step = 4 + (K == 5 ? B.d0 : 0);
+    if ((long long)n2 * step > kSplitWork) {
+      const int per = (int)max(1LL, min((long long)n2, kSplitWork / step));
+      const int nrec = (n2 + per - 1) / per;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(a.heads + 1, (unsigned long long)nrec);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const bool fits = base + nrec <= (unsigned long long)a.split_cap;
+      for (int r = lane; r < nrec; r += 32) {
+        if (base + r >= (unsigned long long)a.split_cap) break;
+        const int rlo = per * r;
+        a.split[base + r] = fits ? SplitRec{(int32_t)(e & 0xffffffffLL), (int32_t)(e >> 32), rlo,
+                                            min(rlo + per, n2)}
+                                 : SplitRec{0, 0, 0, 0};
+      }
+      if (fits) return 0;
+    }
+  }
+  unsigned long long c = 0;
+  if (stream) {
+    for (int i2 = lo; i2 < hi; ++i2) {
+      const int y = C2.p[i2];
+      set_vertex(w, 2, y, a, lane);
+      bits_set(w, 2, y, -1, lower_index(B.n0, B.d0, y), lane);
+      if (lane < 32) w.rowbuf[lane] = 0u;
+      __syncwarp();
+      for (int t = lane; t < w.vl[2]; t += 32) {
+        const int z = a.col[w.vb[2] + t];
+        const int k = lower_index(B.n0, B.d0, z);
+        if (k < B.d0 && B.n0[k] == z) atomicOr(&w.rowbuf[k >> 5], 1u << (k & 31));
+      }
+      __syncwarp();
+      c += bits_step2<K>(p, w, B, list, lane);
+    }
+  } else {
+    int rank = 0;
+    for (int wi = 0; wi < B.W && rank < hi; ++wi) {
+      uint32_t m = __shfl_sync(0xffffffffu, c2w, wi);
+      const int pc = __popc(m);
+      if (rank + pc <= lo) {
+        rank += pc;
+        continue;
+      }
+      for (; m && rank < hi; m &= m - 1, ++rank) {
+        if (rank < lo) continue;
+        const int b = wi * 32 + __ffs(m) - 1;
+        bits_set(w, 2, B.n0[b], b, b, lane);
+        c += bits_step2<K>(p, w, B, list, lane);
+      }
+    }
+  }
+  return c;
+}
+
+// Stored rows: per v of degree 33..1024, d(v) rows of ceil(d(v)/32) words.
+__global__ void k_lut_sizes(const int64_t* rowptr, int64_t nv, int64_t* sz) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int d = (int)(rowptr[v + 1] - rowptr[v]);
+    sz[v] = (d > kLutDeg && d <= kLutMed) ? (int64_t)d * ((d + 31) / 32) : 0;
+  }
+}
+
+// One warp per vertex v, one lane per row: the row of u = N(v)[i] scans N(u) into N(v)
+// when that is cheaper, else searches every N(v) element in N(u).
+__global__ void __launch_bounds__(kThreads) k_lut_rows(const int64_t* rowptr, const int32_t* col,
+                                                       int64_t nv, const int64_t* off,
+                                                       uint32_t* rows) {
+  __shared__ uint32_t buf[kWarps][32][33];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t nw = (int64_t)gridDim.x * kWarps;
+  for (int64_t v = (int64_t)blockIdx.x * kWarps + wib; v < nv; v += nw) {
+    const int64_t rb = rowptr[v];
+    const int d = (int)(rowptr[v + 1] - rb);
+    if (d <= kLutDeg || d > kLutMed) continue;
+    const int W = (d + 31) >> 5;
+    const int32_t* n0 = col + rb;
+    uint32_t* out = rows + off[v];
+    uint32_t* r = buf[wib][lane];
+    const int lgd = 32 - __clz(d);
+    for (int i = lane; i < d; i += 32) {
+      for (int k = 0; k < W; ++k) r[k] = 0u;
+      const int u = n0[i];
+      const int64_t ru = rowptr[u];
+      const int du = (int)(rowptr[u + 1] - ru);
+      if ((int64_t)du * lgd <= (int64_t)d * (32 - __clz(du | 1))) {
+        for (int t = 0; t < du; ++t) {
+          const int y = col[ru + t];
+          const int k = lower_index(n0, d, y);
+          if (k < d && n0[k] == y) r[k >> 5] |= 1u << (k & 31);
+        }
+      } else {
+        for (int k = 0; k < d; ++k)
+          if (member(col + ru, du, n0[k])) r[k >> 5] |= 1u << (k & 31);
+      }
+      for (int k = 0; k < W; ++k) out[(int64_t)i * W + k] = r[k];
+    }
+  }
+}
+
 template <int K>
 __global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) {
   __shared__ Prog p;
@@ -436,10 +751,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) 
         while (a.rowptr[v0 + 1] <= e) ++v0;
         const int v1 = a.col[e];
         if (p.v1lt && v1 >= v0) continue;
-        if (a.lut_ok && lut_task_taken(a, (int)(a.rowptr[v0 + 1] - a.rowptr[v0]),
-                                       (int)(a.rowptr[v1 + 1] - a.rowptr[v1])))
-          continue;
-        c += run_task<K>(p, roots, w, a, slots, v0, v1, e, 0, -1, true, lane);
+        const int d0 = (int)(a.rowptr[v0 + 1] - a.rowptr[v0]);
+        if (a.lut_ok && lut_task_taken(a, d0, (int)(a.rowptr[v1 + 1] - a.rowptr[v1]))) continue;
+        if (K >= 4 && bits_task(a, d0))
+          c += run_task_bits<K>(p, w, a, slots, v0, v1, e, 0, -1, true, lane);
+        else
+          c += run_task<K>(p, roots, w, a, slots, v0, v1, e, 0, -1, true, lane);
       }
     }
   } else {
@@ -456,7 +773,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) 
       int v0 = 0;
       if (lane == 0) v0 = row_of(a.rowptr, a.nv, e);
       v0 = __shfl_sync(0xffffffffu, v0, 0);
-      c += run_task<K>(p, roots, w, a, slots, v0, a.col[e], e, rec.lo, rec.hi, false, lane);
+      const int d0 = (int)(a.rowptr[v0 + 1] - a.rowptr[v0]);
+      if (K >= 4 && bits_task(a, d0))
+        c += run_task_bits<K>(p, w, a, slots, v0, a.col[e], e, rec.lo, rec.hi, false, lane);
+      else
+        c += run_task<K>(p, roots, w, a, slots, v0, a.col[e], e, rec.lo, rec.hi, false, lane);
     }
   }
 #pragma unroll
@@ -679,6 +1000,57 @@ int occupancy(int k) {
 
 }  // namespace
 
+// Stored rows for the warp-wide bitmap form, built once per graph (kept while they
+// fit kLutBudget; otherwise those tasks stay on the list form).
+cudaError_t ensure_lut_rows(const DevGraph& g, cudaStream_t s) {
+  if (g.lut_state != 0) return cudaSuccess;
+  if (g.nv == 0) {
+    g.lut_state = -1;
+    return cudaSuccess;
+  }
+  int64_t* off = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&off, sizeof(int64_t) * (g.nv + 1), s);
+  if (e == cudaErrorMemoryAllocation) {  // no room: those tasks stay on the list form
+    cudaGetLastError();
+    g.lut_state = -1;
+    return cudaSuccess;
+  }
+  if (e != cudaSuccess) return e;
+  const int blocks = (int)std::min<int64_t>((g.nv + kThreads - 1) / kThreads, 65536);
+  k_lut_sizes<<<blocks, kThreads, 0, s>>>(g.rowptr_o, g.nv, off);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = scan_excl(off, off, g.nv, off + g.nv, s);
+  int64_t total = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&total, off + g.nv, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess || total == 0 || total * (int64_t)sizeof(uint32_t) > kLutBudget) {
+    cudaFreeAsync(off, s);
+    if (e == cudaSuccess) g.lut_state = -1;
+    return e;
+  }
+  uint32_t* rows = nullptr;
+  e = cudaMallocAsync((void**)&rows, sizeof(uint32_t) * total, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(off, s);
+    if (e != cudaErrorMemoryAllocation) return e;
+    cudaGetLastError();
+    g.lut_state = -1;
+    return cudaSuccess;
+  }
+  const int wblocks = (int)std::min<int64_t>((g.nv + kWarps - 1) / kWarps, 65536);
+  k_lut_rows<<<wblocks, kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.nv, off, rows);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaFreeAsync(rows, s);
+    cudaFreeAsync(off, s);
+    return e;
+  }
+  g.lut_rows = rows;
+  g.lut_off = off;
+  g.lut_state = 1;
+  return cudaSuccess;
+}
+
 xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_t* out,
                          xgm_stats& st) {
   std::string why;
@@ -712,6 +1084,9 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
     XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_heads, sizeof(unsigned long long) * 4, s));
   }
   XGM_CUDA_TRY(cudaMemsetAsync(ctx->prog_heads, 0, sizeof(unsigned long long) * 4, s));
+  ProgLut lut;
+  const bool lut_ok = prog_lut(p, &lut);
+  if (lut_ok && p.k >= 4) XGM_CUDA_TRY(ensure_lut_rows(g, s));  // once per graph
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
   ProgArgs a;
   a.rowptr = g.rowptr_o;
@@ -726,9 +1101,10 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   a.split_cap = kSplitCap;
   a.total = &ctx->d_sc->count;
   a.split_mode = 0;
-  ProgLut lut;
-  a.lut_ok = prog_lut(p, &lut) ? 1 : 0;
+  a.lut_ok = lut_ok ? 1 : 0;
   a.lut_stream = lut.stream;
+  a.lut_rows = (lut_ok && g.lut_state == 1) ? g.lut_rows : nullptr;
+  a.lut_off = (lut_ok && g.lut_state == 1) ? g.lut_off : nullptr;
   int launches = 0;
   if (g.ne > 0) {
     cudaError_t e = p.k == 3   ? launch_k<3>(p, a, grid, s)
