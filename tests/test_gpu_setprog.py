@@ -57,6 +57,7 @@ def test_glumin5_vs_oracle_and_split(xgm, ctx, orc):
             # bitmap launch (small-degree v0) where the plan allows it, task launch, split
             # launch
             assert st["launches"] in (2, 3) and st["tasks"] == len(col)
+            assert ctx.count_kernels(g, f"P{pid}") == st["launches"]
             split += st["variant_tasks"][xgm.VAR_SPLIT]
         g.close()
     assert split > 0  # the hub graph's long candidate lists went through split records

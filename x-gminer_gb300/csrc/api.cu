@@ -503,8 +503,9 @@ xgm_status xgm_motif_count(xgm_ctx* ctx, const xgm_graph* g, int k, const xgm_sc
 xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan,
                              const xgm_sched* sched, int* n_kernels) {
   if (!ctx || !g || !plan || !n_kernels) return XGM_ERR_INVALID;
-  if (plan->pattern == XGM_PATTERN_PROGRAM) {
-    *n_kernels = plan->prog.k == 3 ? 1 : 2;
+  if (plan->pattern == XGM_PATTERN_PROGRAM) {  // bitmap launch (where eligible), tasks, splits
+    ProgLut lut;
+    *n_kernels = plan->prog.k == 3 ? 1 : (prog_lut(plan->prog, &lut) ? 3 : 2);
     return XGM_OK;
   }
   xgm_sched def;
