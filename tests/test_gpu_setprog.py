@@ -127,3 +127,21 @@ def test_program_edge_cases(xgm, ctx):
     assert ctx.count(g, "5-cycle") == 56 * 12
     assert ctx.count(g, "5-star") == 8 * 35  # centre, then any 4 of the other 7
     g.close()
+
+
+def test_glumin5_identities_rmat_s12(xgm, ctx):
+    # at a size the oracle would take minutes on: each GLUMIN plan whose count is a
+    # multiple of one vertex-induced pattern equals that multiple of the compiled
+    # program's count (a different program, symmetry breaking and code path), and
+    # P22 = 24 x 4-cliques (clique kernel) + 12 x induced (K5 minus an edge)
+    from test_setprog import GLUMIN5_PATTERNS
+
+    nv, s, d = xgm.gen_rmat(12, 8, seed=3)
+    g = ctx.graph_from_edges(nv, s, d)
+    for pid, (edges, factor) in GLUMIN5_PATTERNS.items():
+        compiled = ctx.count(g, ctx.plan(_adj(edges), induced=True))
+        assert ctx.count(g, f"P{pid}") == factor * compiled, pid
+    k5e = ctx.plan(_adj([e for e in itertools.combinations(range(5), 2) if e != (3, 4)]),
+                   induced=True)
+    assert ctx.count(g, "P22") == 24 * ctx.count(g, "4-clique") + 12 * ctx.count(g, k5e)
+    g.close()
