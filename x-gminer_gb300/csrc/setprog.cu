@@ -66,8 +66,9 @@ struct ProgArgs {
   const int64_t* lut_off;
 };
 
-// Bitmap form: a v0 of degree up to kLutDeg runs in k_setlut, one lane per (v0, v1)
-// task; for stream programs only while d(v1) <= kLutStream (the lane walks N(v1)).
+// Bitmap form: every task of a v0 of degree up to kLutDeg runs in k_setlut, one lane
+// per (v0, v1) task, except the stream tasks with d(v1) > kLutStream, which the warp
+// runs one at a time with its lanes striding over N(v1).
 constexpr int kLutDeg = 32;
 constexpr int kLutStream = 32;
 // A v0 of degree kLutDeg < d0 <= kLutMed runs its tasks in the warp-wide bitmap form
@@ -75,8 +76,8 @@ constexpr int kLutStream = 32;
 constexpr int kLutMed = 1024;
 constexpr int64_t kLutBudget = int64_t(4) << 30;  // bytes of stored rows at most
 
-__device__ __forceinline__ bool lut_task_taken(const ProgArgs& a, int d0, int d1) {
-  return a.lut_ok && d0 <= kLutDeg && (a.lut_stream < 0 || d1 <= kLutStream);
+__device__ __forceinline__ bool lut_task_taken(const ProgArgs& a, int d0) {
+  return a.lut_ok && d0 <= kLutDeg;
 }
 
 struct WarpState {
@@ -752,7 +753,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_setprog(Prog prog, ProgArgs a) 
         const int v1 = a.col[e];
         if (p.v1lt && v1 >= v0) continue;
         const int d0 = (int)(a.rowptr[v0 + 1] - a.rowptr[v0]);
-        if (a.lut_ok && lut_task_taken(a, d0, (int)(a.rowptr[v1 + 1] - a.rowptr[v1]))) continue;
+        if (lut_task_taken(a, d0)) continue;
         if (K >= 4 && bits_task(a, d0))
           c += run_task_bits<K>(p, w, a, slots, v0, v1, e, 0, -1, true, lane);
         else
@@ -875,15 +876,17 @@ __device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, uint32
   return 0;
 }
 
-// One (v0, v1) task on masks; sl = this lane's slots (stride 32).
+// One (v0, v1) task on masks; sl = this lane's slots (stride 32).  A stream program's
+// v2 candidates are the entries t0, t0 + ts, ... of N(v1) (ts = 1: this lane runs the
+// whole task; ts = 32: the warp's lanes share it).
 template <int K>
 __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0, int i1, int d0,
-                                       const int32_t* n0, const uint32_t* lut, uint32_t* sl) {
+                                       const int32_t* n0, const uint32_t* lut, uint32_t* sl,
+                                       int t0, int ts) {
   const int v1 = n0[i1];
   if (p.v1lt && v1 >= v0) return 0;
   const long long rb1 = a.rowptr[v1];
   const int d1 = (int)(a.rowptr[v1 + 1] - rb1);
-  if (!lut_task_taken(a, d0, d1)) return 0;  // the list kernel runs it
   const uint32_t valid = d0 >= 32 ? 0xffffffffu : ((1u << d0) - 1u);
   LutLane L;
 #pragma unroll
@@ -918,11 +921,10 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
 #pragma unroll
     for (int j = 0; j < 2; ++j)
       if ((o.bound >> j) & 1u) ub = min(ub, L.v[j]);
-    int i = 0;
-    for (int t = 0; t < d1; ++t) {
+    for (int t = t0; t < d1; t += ts) {
       const int y = a.col[rb1 + t];
       if (y >= ub) break;
-      while (i < d0 && n0[i] < y) ++i;
+      const int i = lower_index(n0, d0, y);
       if (i < d0 && n0[i] == y) continue;
       if ((((o.excl >> 0) & 1u) && y == v0) || (((o.excl >> 1) & 1u) && y == v1)) continue;
       lut_set(L, 2, y, -1, n0, d0);
@@ -963,9 +965,22 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
       __syncwarp();
       if (lane < d0) luts[wib][lane] = row_over(n0s[wib], d0, n0s[wib][lane], a);
       __syncwarp();
-      if (lane < d0)
-        c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane]);
+      // one lane per task; stream tasks with a long N(v1) are left to the pass below
+      if (lane < d0) {
+        const int v1 = n0s[wib][lane];
+        const int d1 = (int)(a.rowptr[v1 + 1] - a.rowptr[v1]);
+        if (a.lut_stream < 0 || d1 <= kLutStream)
+          c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane], 0, 1);
+      }
       __syncwarp();
+      if (a.lut_stream >= 0) {
+        for (int i1 = 0; i1 < d0; ++i1) {
+          const int v1 = n0s[wib][i1];
+          if ((int)(a.rowptr[v1 + 1] - a.rowptr[v1]) <= kLutStream) continue;
+          c += lut_task<K>(p, a, (int)v0, i1, d0, n0s[wib], luts[wib], &sls[wib][lane], lane, 32);
+        }
+        __syncwarp();
+      }
     }
   }
 #pragma unroll
