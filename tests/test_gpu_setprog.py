@@ -54,9 +54,9 @@ def test_glumin5_vs_oracle_and_split(xgm, ctx, orc):
         for pid in range(6, 23):
             got, st = ctx.count(g, f"P{pid}", with_stats=True)
             assert got == orc.glumin5(pid, rowptr, col), pid
-            # bitmap launch (small-degree v0) where the plan allows it, task launch, split
-            # launch
-            assert st["launches"] in (2, 3) and st["tasks"] == len(col)
+            # bitmap launches (small-degree v0; a second for long N(v1) streams) where the
+            # plan allows them, task launch, split launch
+            assert st["launches"] in (2, 3, 4) and st["tasks"] == len(col)
             assert ctx.count_kernels(g, f"P{pid}") == st["launches"]
             split += st["variant_tasks"][xgm.VAR_SPLIT]
         g.close()

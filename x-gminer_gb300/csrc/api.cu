@@ -505,7 +505,8 @@ xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   if (!ctx || !g || !plan || !n_kernels) return XGM_ERR_INVALID;
   if (plan->pattern == XGM_PATTERN_PROGRAM) {  // bitmap launch (where eligible), tasks, splits
     ProgLut lut;
-    *n_kernels = plan->prog.k == 3 ? 1 : (prog_lut(plan->prog, &lut) ? 3 : 2);
+    *n_kernels = plan->prog.k == 3 ? 1
+                                   : (prog_lut(plan->prog, &lut) ? (lut.stream >= 0 ? 4 : 3) : 2);
     return XGM_OK;
   }
   xgm_sched def;

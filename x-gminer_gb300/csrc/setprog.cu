@@ -42,6 +42,10 @@ constexpr int kChunk = 8;       // CSR entries claimed per queue step
 // of one warp).
 constexpr long long kSplitWork = 4096;
 constexpr int64_t kSplitCap = int64_t(1) << 22;  // records (64 MB)
+// Long streams of the bitmap form: records of (v0, v1 index, N(v1) entry range) after
+// the split records in the same buffer.
+constexpr int64_t kStreamCap = int64_t(1) << 20;
+constexpr int kStreamChunk = 256;  // N(v1) entries per record
 
 struct SplitRec {
   int32_t e_lo, e_hi;  // CSR entry
@@ -55,13 +59,16 @@ struct ProgArgs {
   int32_t* scratch;
   int64_t slot_cap;   // ints per slot
   int nslots;
-  unsigned long long* heads;  // [0] entry head, [1] split tail, [2] split head, [3] v0 head (bitmap form)
+  // [0] entry head, [1] split tail, [2] split head, [3] v0 head (bitmap form), [4] stream
+  // record tail, [5] stream record head
+  unsigned long long* heads;
   SplitRec* split;
   int64_t split_cap;
   unsigned long long* total;
   int split_mode;
   int lut_ok;      // the bitmap kernel takes the tasks with small v0 (ProgLut)
   int lut_stream;  // its stream operation, or -1
+  int lut_phase;   // k_setlut: 0 vertices, 1 stream records
   const uint32_t* lut_rows;  // stored rows of v0 with degree 33..1024 (or null)
   const int64_t* lut_off;
 };
@@ -877,12 +884,12 @@ __device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, uint32
 }
 
 // One (v0, v1) task on masks; sl = this lane's slots (stride 32).  A stream program's
-// v2 candidates are the entries t0, t0 + ts, ... of N(v1) (ts = 1: this lane runs the
-// whole task; ts = 32: the warp's lanes share it).
+// v2 candidates are the entries t0, t0 + ts, ... of N(v1) within [s_lo, s_hi) (ts = 1:
+// this lane runs the whole task; ts = 32: the warp's lanes share it).
 template <int K>
 __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0, int i1, int d0,
                                        const int32_t* n0, const uint32_t* lut, uint32_t* sl,
-                                       int t0, int ts) {
+                                       int t0, int ts, int s_lo = 0, int s_hi = 1 << 30) {
   const int v1 = n0[i1];
   if (p.v1lt && v1 >= v0) return 0;
   const long long rb1 = a.rowptr[v1];
@@ -921,7 +928,8 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
 #pragma unroll
     for (int j = 0; j < 2; ++j)
       if ((o.bound >> j) & 1u) ub = min(ub, L.v[j]);
-    for (int t = t0; t < d1; t += ts) {
+    const int tend = min(d1, s_hi);
+    for (int t = max(t0, s_lo); t < tend; t += ts) {
       const int y = a.col[rb1 + t];
       if (y >= ub) break;
       const int i = lower_index(n0, d0, y);
@@ -942,6 +950,15 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
   return c;
 }
 
+// N(v0) and its rows into the warp's shared memory (lanes < d0).
+__device__ __forceinline__ void lut_load(int32_t* n0, uint32_t* lut, long long rb, int d0,
+                                         const ProgArgs& a, int lane) {
+  if (lane < d0) n0[lane] = a.col[rb + lane];
+  __syncwarp();
+  if (lane < d0) lut[lane] = row_over(n0, d0, n0[lane], a);
+  __syncwarp();
+}
+
 template <int K>
 __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
   __shared__ Prog p;
@@ -951,36 +968,64 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
   if (threadIdx.x == 0) p = prog;
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  SplitRec* srec = a.split + a.split_cap;  // stream records
   unsigned long long c = 0;
-  for (;;) {
-    unsigned long long v0 = 0;
-    if (lane == 0) v0 = atomicAdd(a.heads + 3, 1ull);
-    v0 = __shfl_sync(0xffffffffu, v0, 0);
-    if ((long long)v0 >= a.nv) break;
-    {
+  if (a.lut_phase == 0) {
+    for (;;) {
+      unsigned long long v0 = 0;
+      if (lane == 0) v0 = atomicAdd(a.heads + 3, 1ull);
+      v0 = __shfl_sync(0xffffffffu, v0, 0);
+      if ((long long)v0 >= a.nv) break;
       const long long rb = a.rowptr[v0];
       const int d0 = (int)(a.rowptr[v0 + 1] - rb);
       if (d0 == 0 || d0 > kLutDeg) continue;
-      if (lane < d0) n0s[wib][lane] = a.col[rb + lane];
-      __syncwarp();
-      if (lane < d0) luts[wib][lane] = row_over(n0s[wib], d0, n0s[wib][lane], a);
-      __syncwarp();
-      // one lane per task; stream tasks with a long N(v1) are left to the pass below
+      lut_load(n0s[wib], luts[wib], rb, d0, a, lane);
+      // one lane per task; stream tasks with a long N(v1) become stream records
+      int d1 = 0;
       if (lane < d0) {
         const int v1 = n0s[wib][lane];
-        const int d1 = (int)(a.rowptr[v1 + 1] - a.rowptr[v1]);
+        d1 = (int)(a.rowptr[v1 + 1] - a.rowptr[v1]);
         if (a.lut_stream < 0 || d1 <= kLutStream)
           c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane], 0, 1);
       }
       __syncwarp();
       if (a.lut_stream >= 0) {
-        for (int i1 = 0; i1 < d0; ++i1) {
-          const int v1 = n0s[wib][i1];
-          if ((int)(a.rowptr[v1 + 1] - a.rowptr[v1]) <= kLutStream) continue;
-          c += lut_task<K>(p, a, (int)v0, i1, d0, n0s[wib], luts[wib], &sls[wib][lane], lane, 32);
+        const bool lng = lane < d0 && d1 > kLutStream;
+        const int nrec = lng ? (d1 + kStreamChunk - 1) / kStreamChunk : 0;
+        const unsigned long long base = nrec ? atomicAdd(a.heads + 4, (unsigned long long)nrec) : 0;
+        const bool fits = base + nrec <= (unsigned long long)kStreamCap;
+        for (int r = 0; r < nrec; ++r)
+          if (base + r < (unsigned long long)kStreamCap)
+            srec[base + r] = fits ? SplitRec{(int32_t)v0, lane, r * kStreamChunk,
+                                            min((r + 1) * kStreamChunk, d1)}
+                                  : SplitRec{0, 0, 0, 0};
+        // no room: the warp runs the task itself, lanes striding over N(v1)
+        unsigned todo = __ballot_sync(0xffffffffu, lng && !fits);
+        for (; todo; todo &= todo - 1) {
+          const int i1 = __ffs(todo) - 1;
+          c += lut_task<K>(p, a, (int)v0, i1, d0, n0s[wib], luts[wib], &sls[wib][lane], lane, 32,
+                           0, 1 << 30);
         }
         __syncwarp();
       }
+    }
+  } else {
+    const unsigned long long nrec = min(*(volatile unsigned long long*)(a.heads + 4),
+                                        (unsigned long long)kStreamCap);
+    for (;;) {
+      unsigned long long r = 0;
+      if (lane == 0) r = atomicAdd(a.heads + 5, 1ull);
+      r = __shfl_sync(0xffffffffu, r, 0);
+      if (r >= nrec) break;
+      const SplitRec rec = srec[r];
+      if (rec.lo >= rec.hi) continue;
+      const int v0 = rec.e_lo;
+      const long long rb = a.rowptr[v0];
+      const int d0 = (int)(a.rowptr[v0 + 1] - rb);
+      lut_load(n0s[wib], luts[wib], rb, d0, a, lane);
+      c += lut_task<K>(p, a, v0, rec.e_hi, d0, n0s[wib], luts[wib], &sls[wib][lane], rec.lo + lane,
+                       32, rec.lo, rec.hi);
+      __syncwarp();
     }
   }
 #pragma unroll
@@ -993,9 +1038,16 @@ cudaError_t launch_k(const Prog& p, const ProgArgs& a, int grid, cudaStream_t s)
   ProgArgs b = a;
   b.split_mode = 0;
   if (K >= 4 && a.lut_ok) {
+    b.lut_phase = 0;
     k_setlut<K><<<grid, kThreads, 0, s>>>(p, b);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (a.lut_stream >= 0) {
+      b.lut_phase = 1;
+      k_setlut<K><<<grid, kThreads, 0, s>>>(p, b);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
   }
   k_setprog<K><<<grid, kThreads, 0, s>>>(p, b);
   cudaError_t e = cudaGetLastError();
@@ -1095,10 +1147,11 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
     ctx->prog_scratch_cap = need;
   }
   if (!ctx->prog_split) {
-    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_split, sizeof(SplitRec) * kSplitCap, s));
-    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_heads, sizeof(unsigned long long) * 4, s));
+    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_split,
+                                 sizeof(SplitRec) * (kSplitCap + kStreamCap), s));
+    XGM_CUDA_TRY(cudaMallocAsync((void**)&ctx->prog_heads, sizeof(unsigned long long) * 8, s));
   }
-  XGM_CUDA_TRY(cudaMemsetAsync(ctx->prog_heads, 0, sizeof(unsigned long long) * 4, s));
+  XGM_CUDA_TRY(cudaMemsetAsync(ctx->prog_heads, 0, sizeof(unsigned long long) * 8, s));
   ProgLut lut;
   const bool lut_ok = prog_lut(p, &lut);
   if (lut_ok && p.k >= 4) XGM_CUDA_TRY(ensure_lut_rows(g, s));  // once per graph
@@ -1118,6 +1171,7 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   a.split_mode = 0;
   a.lut_ok = lut_ok ? 1 : 0;
   a.lut_stream = lut.stream;
+  a.lut_phase = 0;
   a.lut_rows = (lut_ok && g.lut_state == 1) ? g.lut_rows : nullptr;
   a.lut_off = (lut_ok && g.lut_state == 1) ? g.lut_off : nullptr;
   int launches = 0;
@@ -1126,7 +1180,7 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
                     : p.k == 4 ? launch_k<4>(p, a, grid, s)
                                : launch_k<5>(p, a, grid, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_setprog", __FILE__, __LINE__);
-    launches = p.k == 3 ? 1 : (a.lut_ok ? 3 : 2);
+    launches = p.k == 3 ? 1 : (a.lut_ok ? (a.lut_stream >= 0 ? 4 : 3) : 2);
   }
   XGM_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   XGM_CUDA_TRY(cudaMemcpyAsync(ctx->d_sc->n, ctx->prog_heads + 1, sizeof(int64_t),
