@@ -98,6 +98,7 @@ struct WarpState {
   int pre[kProgMaxK];
   uint32_t bits[kProgMaxSlots][32];
   uint32_t rowbuf[32];
+  uint32_t fk[32];  // bits_flat_fin: the counted operand with the v3-independent masks
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -503,67 +504,53 @@ __device__ __forceinline__ void bits_set(WarpState& w, int j, int x, int i, int 
   __syncwarp();
 }
 
-// Word wi of the N(v0)-space operands, read by any lane (for bits_flat_fin).
-__device__ __forceinline__ uint32_t valid_word(const BitsCtx& B, int wi) {
-  return (wi < B.W - 1 || (B.d0 & 31) == 0) ? 0xffffffffu : ((1u << (B.d0 & 31)) - 1u);
-}
-
-__device__ __forceinline__ uint32_t row_word(const WarpState& w, const BitsCtx& B, int j, int wi) {
-  if (j == 0) return valid_word(B, wi);
-  const int i = w.idx[j];
-  return i >= 0 ? B.row[(int64_t)i * B.W + wi] : w.rowbuf[wi];
-}
-
-__device__ __forceinline__ uint32_t operand_word(const WarpState& w, const BitsCtx& B, int code,
-                                                 int wi) {
-  if (code == kOpList) return valid_word(B, wi);
-  if (code == kOpList + 1) return row_word(w, B, 1, wi);
-  return w.bits[code][wi];
-}
-
 // The final count with the v3 loop spread over lanes: the v3 candidates (bits of c3w,
-// one word per lane) are compacted into `list`, then each lane counts one v3 over all
-// W words.  For the programs whose last level is the count alone.
-__device__ unsigned long long bits_flat_fin(const Prog& p, const WarpState& w, const BitsCtx& B,
+// one word per lane) are compacted into `list`, then each lane counts one v3 over the
+// W words.  Everything that does not depend on v3 (the counted operand, the valid
+// range, the bound and exclusions of v0..v2, and the row of the second operand when it
+// is not v3's) is folded into fk[] once; per v3 and word that leaves one AND (with v3's
+// row) and a popc, plus v3's own bound / exclusion in its word.  For the programs whose
+// last level is the count alone.
+__device__ unsigned long long bits_flat_fin(const Prog& p, WarpState& w, const BitsCtx& B,
                                             uint32_t c3w, int32_t* list, int lane) {
+  const ProgOp& o = p.fin;
+  const bool ub = (o.bound >> 3) & 1u, ux = (o.excl >> 3) & 1u;
+  const int jb = o.kind == OP_FILTER ? -1 : o.b - kOpList;
+  const bool per_v3 = jb == 3;  // the second operand is N(v3)
+  {
+    ProgOp o2 = o;  // fold v0..v2's masks (and a row that is not v3's) into fk
+    o2.bound &= 0x7u;
+    o2.excl &= 0x7u;
+    if (per_v3) o2.kind = OP_FILTER;
+    w.fk[lane] = bits_apply(w, B, o2, bits_operand(w, B, o.a, lane), lane);
+  }
   const int cnt = __popc(c3w);
   int incl = cnt;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
+  for (int k = 1; k < 32; k <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, k);
+    if (lane >= k) incl += y;
   }
   const int n3 = __shfl_sync(0xffffffffu, incl, 31);
   int pos = incl - cnt;
   for (uint32_t m = c3w; m; m &= m - 1) list[pos++] = lane * 32 + __ffs(m) - 1;
   __syncwarp();
-  const ProgOp& o = p.fin;
-  int pbs = INT_MAX, ex[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    if ((o.bound >> j) & 1u) pbs = min(pbs, w.pre[j]);
-    ex[j] = ((o.excl >> j) & 1u) ? w.idx[j] : -1;
-  }
-  const bool ub = (o.bound >> 3) & 1u, ux = (o.excl >> 3) & 1u;
-  const int jb = o.kind == OP_FILTER ? -1 : o.b - kOpList;
+  const bool isect = o.kind == OP_INTERSECT;
   unsigned long long c = 0;
   for (int t = lane; t < n3; t += 32) {
     const int b3 = list[t];
-    const int pb = ub ? min(pbs, b3) : pbs;
-    for (int wi = 0; wi < B.W; ++wi) {
-      const int lo = 32 * wi;
-      if (pb <= lo) break;  // the bound's prefix ends here
-      uint32_t keep = valid_word(B, wi) & (pb >= lo + 32 ? 0xffffffffu : ((1u << (pb - lo)) - 1u));
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-        if (ex[j] >= lo && ex[j] < lo + 32) keep &= ~(1u << (ex[j] - lo));
-      if (ux && b3 >= lo && b3 < lo + 32) keep &= ~(1u << (b3 - lo));
-      uint32_t A = operand_word(w, B, o.a, wi);
-      if (jb >= 0) {
-        const uint32_t r = jb == 3 ? B.row[(int64_t)b3 * B.W + wi] : row_word(w, B, jb, wi);
-        A = o.kind == OP_INTERSECT ? (A & r) : (A & ~r);
+    const int bw = b3 >> 5;
+    const uint32_t below = (1u << (b3 & 31)) - 1u;
+    const int lim = ub ? bw + 1 : B.W;
+    const uint32_t* r3 = B.row + (int64_t)b3 * B.W;
+    for (int wi = 0; wi < lim; ++wi) {
+      uint32_t x = w.fk[wi];
+      if (wi == bw) {
+        if (ub) x &= below;
+        if (ux) x &= ~(1u << (b3 & 31));
       }
-      c += __popc(A & keep);
+      if (per_v3) x = isect ? (x & r3[wi]) : (x & ~r3[wi]);
+      c += __popc(x);
     }
   }
   __syncwarp();
