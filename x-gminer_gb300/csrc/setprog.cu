@@ -1,26 +1,32 @@
 // Interpreter for set-operation programs (setprog.cuh) on the undirected CSR in
-// original ids.
-//
-// One warp per task; a task is one directed CSR entry (v0, v1), as GLUMIN's
+// original ids.  Tasks are the directed CSR entries (v0, v1), as GLUMIN's
 // edge-parallel kernels walk the full edge list (G2Miner/gpu_GM_LUT.cu:78-95,
-// GM_kernels/P*-GM.yml.cuh: `for eid ... g.get_src(eid), g.get_dst(eid)`).  Warps
-// claim chunks of entries from an atomic head; the row of a chunk's first entry is
-// found by binary search over rowptr and then advanced entry by entry.
+// GM_kernels/P*-GM.yml.cuh: `for eid ... g.get_src(eid), g.get_dst(eid)`).  Three
+// forms, chosen per task by the degree of v0:
 //
-// A set operation streams its first list through the warp (coalesced, 32 elements a
-// step), tests each element against the second list by binary search, and compacts
-// the survivors with a ballot into the warp's slot; a bound stops the stream at the
-// first element at or above it (the lists are sorted).  The last vertex is never
-// enumerated: the final count runs flat over every (v_{k-2}, x) pair of the last
-// candidate list and the counted operand, so a warp keeps all 32 lanes busy when the
-// lists are short, which they mostly are on sparse graphs.  A task whose estimated
-// work (v2 candidates x the cost of one v2 step, from the lengths of the level-0
-// slots the later steps read) passes kSplitWork queues its v2 candidates as split
-// records of about kSplitWork each; a second launch runs those (each record recomputes the level-0 slots, O(d(v0) + d(v1)) lane-steps / 32,
-// a few percent of a record).
+// - List form (k_setprog, any degree): one warp per task.  A set operation streams
+//   its first list through the warp (coalesced, 32 elements a step), tests each
+//   element against the second list by binary search, and compacts the survivors with
+//   a ballot into the warp's slot; a bound stops the stream at the first element at
+//   or above it (the lists are sorted).  The last vertex is never enumerated: the
+//   final count runs flat over every (v_{k-2}, x) pair, or, when the counted operand
+//   is long, searches the short neighbour lists of the candidates in it.
+// - Bitmap form for d(v0) <= 32 (k_setlut): GLUMIN's LUT idea, one warp per v0 with
+//   its adjacency rows in shared memory and one lane per task on 32-bit masks.
+// - Warp-wide bitmap form for 32 < d(v0) <= 1024 (run_task_bits inside k_setprog):
+//   the graph's stored rows, one word of N(v0) index space per lane.
 //
-// Slots live in a per-warp global scratch area ((slot count + 1) x max degree ints),
-// which stays in L1/L2: a slot is written once per level and read by every later step.
+// The bitmap forms need a program whose operands live in N(v0) (prog_lut); others
+// run in the list form throughout.  Warps claim chunks of entries from an atomic head
+// (the row of a chunk's first entry by binary search over rowptr, then entry by
+// entry).  A task whose estimated work passes kSplitWork queues its v2 candidates as
+// split records of about kSplitWork each, run by a second k_setprog launch (each
+// record recomputes the level-0 slots, a few percent of its work).  Launches per
+// count: k_setlut (and its stream-record pass), k_setprog tasks, k_setprog splits.
+//
+// List slots live in a per-warp global scratch area ((slot count + 1) x max degree
+// ints), which stays in L1/L2: a slot is written once per level and read by every
+// later step.
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -74,8 +80,8 @@ struct ProgArgs {
 };
 
 // Bitmap form: every task of a v0 of degree up to kLutDeg runs in k_setlut, one lane
-// per (v0, v1) task, except the stream tasks with d(v1) > kLutStream, which the warp
-// runs one at a time with its lanes striding over N(v1).
+// per (v0, v1) task, except the stream tasks with d(v1) > kLutStream, which become
+// stream records (kStreamChunk entries of N(v1) each) for a second k_setlut pass.
 constexpr int kLutDeg = 32;
 constexpr int kLutStream = 32;
 // A v0 of degree kLutDeg < d0 <= kLutMed runs its tasks in the warp-wide bitmap form
