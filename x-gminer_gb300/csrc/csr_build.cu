@@ -146,15 +146,76 @@ __global__ void k_rank_from_sorted(const uint64_t* keys, const int32_t* deg, int
 // rank-space entries with row and column swapped; a stable sort on the row bits alone
 // (bits [vb, 2 vb)) then leaves every row's columns sorted — half the radix passes of
 // sorting (row, column) keys from scratch.
+// A warp takes 32 consecutive new rows at once: lane i fetches row i's source and
+// destination, then the lanes walk the 32 rows' entries as one flat range (each entry
+// finds its row by a 5-step search over the lanes' prefix of lengths), so short rows
+// keep every lane busy and the rows' loads overlap.  Rows longer than kLongRow (the
+// hubs, which rank order puts together at the end) are listed in `longs` (count in
+// nlong) for k_rank_entry_keys_long.
+constexpr int64_t kLongRow = 1024;
+constexpr int kLongSplit = 16;  // blocks per long row
+
 __global__ void k_rank_entry_keys(const int64_t* rowptr_o, const int32_t* col_o,
                                   const int32_t* rank, const int32_t* perm,
-                                  const int64_t* rowptr_r, int64_t nv, int vb, uint64_t* keys) {
+                                  const int64_t* rowptr_r, int64_t nv, int vb, uint64_t* keys,
+                                  int32_t* longs, unsigned long long* nlong) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < nv; r += warps) {
-    const int32_t x = perm[r];
-    const int64_t src = rowptr_o[x], dst = rowptr_r[r], len = rowptr_r[r + 1] - dst;
-    for (int64_t j = lane; j < len; j += 32)
+  for (int64_t r0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32; r0 < nv;
+       r0 += warps * 32) {
+    const int64_t r = r0 + lane;
+    int64_t src = 0, dst = 0, len = 0;
+    if (r < nv) {
+      dst = rowptr_r[r];
+      len = rowptr_r[r + 1] - dst;
+      if (len > kLongRow) {
+        longs[atomicAdd(nlong, 1ull)] = (int32_t)r;
+        len = 0;
+      } else {
+        src = rowptr_o[perm[r]];
+      }
+    }
+    int64_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int64_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const int64_t excl = incl - len;
+    for (int64_t b = 0; b < total; b += 32) {
+      const int64_t t = b + lane;
+      int k = 0;  // last row whose first flat index is <= t
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int64_t ex = __shfl_sync(0xffffffffu, excl, k + step);
+        if (ex <= t) k += step;
+      }
+      const int64_t ks = __shfl_sync(0xffffffffu, src, k);
+      const int64_t kd = __shfl_sync(0xffffffffu, dst, k);
+      const int64_t kx = __shfl_sync(0xffffffffu, excl, k);
+      if (t < total) {
+        const int64_t j = t - kx;
+        keys[kd + j] = ((uint64_t)rank[col_o[ks + j]] << vb) | (uint64_t)(r0 + k);
+      }
+    }
+  }
+}
+
+// The listed long rows: kLongSplit blocks per row (blockIdx.y), each one slice of the
+// row's entries, its threads striding the slice.
+__global__ void k_rank_entry_keys_long(const int64_t* rowptr_o, const int32_t* col_o,
+                                       const int32_t* rank, const int32_t* perm,
+                                       const int64_t* rowptr_r, const int32_t* longs,
+                                       const unsigned long long* nlong, int vb,
+                                       uint64_t* keys) {
+  const int64_t n = (int64_t)*nlong;
+  for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const int64_t r = longs[i];
+    const int64_t dst = rowptr_r[r], len = rowptr_r[r + 1] - dst;
+    const int64_t src = rowptr_o[perm[r]];
+    const int64_t lo = len * blockIdx.y / gridDim.y, hi = len * (blockIdx.y + 1) / gridDim.y;
+    for (int64_t j = lo + threadIdx.x; j < hi; j += blockDim.x)
       keys[dst + j] = ((uint64_t)rank[col_o[src + j]] << vb) | (uint64_t)r;
   }
 }
@@ -338,11 +399,11 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
   const int64_t nv = g.nv, ne = g.ne;
   const int vb = bits_for(nv);
   int32_t *deg = nullptr, *degp = nullptr;
-  unsigned long long* stats = nullptr;  // [0] max deg, [1] max out, [2] ne_dag
+  unsigned long long* stats = nullptr;  // [0] max deg, [1] max out, [2] ne_dag, [3] long rows
   TRY(dalloc(&deg, nv, s));
   TRY(dalloc(&degp, nv, s));
-  TRY(dalloc(&stats, 3, s));
-  TRY(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
+  TRY(dalloc(&stats, 4, s));
+  TRY(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s));
   if (nv > 0) {
     k_degrees<<<grid_for(nv), kThreads, 0, s>>>(g.rowptr_o, nv, deg, stats);
     TRY(cudaGetLastError());
@@ -379,9 +440,19 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
   }
   TRY(scan_excl(degp, g.rowptr, nv, g.rowptr + nv, s));
   if (nv > 0) {
-    k_rank_entry_keys<<<grid_for(nv * 32), kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.rank,
-                                                             g.perm, g.rowptr, nv, vb, keys);
+    // at most ne / kLongRow rows are long
+    const int64_t cap = ne / kLongRow + 1;
+    int32_t* longs = nullptr;
+    TRY(dalloc(&longs, cap, s));
+    TRY(cudaMemsetAsync(stats + 3, 0, sizeof(unsigned long long), s));
+    k_rank_entry_keys<<<grid_for(nv), kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.rank, g.perm,
+                                                        g.rowptr, nv, vb, keys, longs, stats + 3);
     TRY(cudaGetLastError());
+    const dim3 lg((unsigned)std::min<int64_t>(cap, 2048), kLongSplit);
+    k_rank_entry_keys_long<<<lg, kThreads, 0, s>>>(g.rowptr_o, g.col_o, g.rank, g.perm, g.rowptr,
+                                                   longs, stats + 3, vb, keys);
+    TRY(cudaGetLastError());
+    cudaFreeAsync(longs, s);
   }
   TRY(radix_sort_u64(keys, tmp, ne, vb, s, vb));
   if (ne > 0) {

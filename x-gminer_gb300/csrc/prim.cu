@@ -128,8 +128,8 @@ cudaError_t scan_impl(const T* in, int64_t* out, int64_t n, int64_t* total, cuda
 
 // ------------------------------------------------------------------ radix sort
 constexpr int kSortWarps = 8;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortWarps * 32 * kSortItems;  // 4096 keys
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortWarps * 32 * kSortItems;  // 2048 keys
 constexpr int kRadix = 256;
 
 __global__ void __launch_bounds__(kSortWarps * 32) k_radix_hist(const uint64_t* keys, int64_t n,
@@ -147,51 +147,81 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_radix_hist(const uint64_t* 
   for (int d = threadIdx.x; d < kRadix; d += blockDim.x) counts[(int64_t)d * tiles + blockIdx.x] = h[d];
 }
 
-// Stable scatter: warp w of the tile owns keys [w*512, (w+1)*512) of the tile and
-// walks them in 16 rounds of 32; __match_any_sync groups equal digits inside a round
-// so each key gets its rank among equal digits in tile order.
+// Stable scatter: warp w of the tile owns keys [w*256, (w+1)*256) of the tile and
+// walks them in 8 rounds of 32; __match_any_sync groups equal digits inside a round
+// so each key gets its rank among equal digits in tile order.  The keys are then
+// placed in digit order in shared memory and written out in that order, so every
+// digit's run reaches global memory as contiguous, coalesced stores.
 __global__ void __launch_bounds__(kSortWarps * 32) k_radix_scatter(const uint64_t* in,
                                                                   uint64_t* out, int64_t n,
                                                                   int shift,
                                                                   const int64_t* offs,
                                                                   int64_t tiles) {
+  __shared__ uint64_t sk[kSortTile];
   __shared__ uint32_t wcnt[kSortWarps][kRadix];
+  __shared__ uint32_t dstart[kRadix];
+  __shared__ uint32_t wsum[kSortWarps];
   __shared__ int64_t gbase[kRadix];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int d = tid; d < kRadix; d += blockDim.x) gbase[d] = offs[(int64_t)d * tiles + blockIdx.x];
   for (int i = tid; i < kSortWarps * kRadix; i += blockDim.x) (&wcnt[0][0])[i] = 0;
   __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * kSortTile + warp * (32 * kSortItems);
+  const int64_t tile0 = (int64_t)blockIdx.x * kSortTile;
+  const int tn = (int)min((int64_t)kSortTile, n - tile0);
+  const int64_t base = tile0 + warp * (32 * kSortItems);
   uint64_t k[kSortItems];
   uint32_t rk[kSortItems];
-  int dg[kSortItems];
 #pragma unroll
   for (int t = 0; t < kSortItems; ++t) {
-    int64_t i = base + t * 32 + lane;
-    bool valid = i < n;
+    const int64_t i = base + t * 32 + lane;
+    const bool valid = i < n;
     k[t] = valid ? in[i] : 0ull;
-    int d = valid ? (int)((k[t] >> shift) & (kRadix - 1)) : kRadix;
-    dg[t] = d;
-    unsigned peers = __match_any_sync(kFull, d);
-    uint32_t before = valid ? wcnt[warp][d] : 0u;
+    const int d = valid ? (int)((k[t] >> shift) & (kRadix - 1)) : kRadix;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t before = valid ? wcnt[warp][d] : 0u;
     rk[t] = before + __popc(peers & lanemask_lt());
     __syncwarp();
     if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = before + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
-  for (int d = tid; d < kRadix; d += blockDim.x) {
-    uint32_t run = 0;
+  // per digit: exclusive prefix over the warps, then the tile-local start of each digit
+  uint32_t tot = 0;
+  if (tid < kRadix) {
     for (int w = 0; w < kSortWarps; ++w) {
-      uint32_t c = wcnt[w][d];
-      wcnt[w][d] = run;
-      run += c;
+      const uint32_t c = wcnt[w][tid];
+      wcnt[w][tid] = tot;
+      tot += c;
     }
+  }
+  uint32_t incl = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (tid < kRadix) {
+    uint32_t off = 0;
+    for (int w = 0; w < warp; ++w) off += wsum[w];
+    dstart[tid] = off + incl - tot;
   }
   __syncthreads();
 #pragma unroll
-  for (int t = 0; t < kSortItems; ++t)
-    if (dg[t] < kRadix) out[gbase[dg[t]] + wcnt[warp][dg[t]] + rk[t]] = k[t];
+  for (int t = 0; t < kSortItems; ++t) {
+    const int64_t i = base + t * 32 + lane;
+    if (i < n) {
+      const int d = (int)((k[t] >> shift) & (kRadix - 1));
+      sk[dstart[d] + wcnt[warp][d] + rk[t]] = k[t];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < tn; i += blockDim.x) {
+    const uint64_t key = sk[i];
+    const int d = (int)((key >> shift) & (kRadix - 1));
+    out[gbase[d] + (i - (int)dstart[d])] = key;
+  }
 }
 
 }  // namespace
