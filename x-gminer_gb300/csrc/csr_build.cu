@@ -454,9 +454,10 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
     TRY(cudaGetLastError());
     cudaFreeAsync(longs, s);
   }
-  TRY(radix_sort_u64(keys, tmp, ne, vb, s, vb));
+  uint64_t* sorted = keys;
+  TRY(radix_sort_u64(keys, tmp, ne, vb, s, vb, &sorted));
   if (ne > 0) {
-    k_extract_col<<<grid_for(ne), kThreads, 0, s>>>(keys, ne, vb, g.col);
+    k_extract_col<<<grid_for(ne), kThreads, 0, s>>>(sorted, ne, vb, g.col);
     TRY(cudaGetLastError());
   }
   if (nv > 0) {

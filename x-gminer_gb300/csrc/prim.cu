@@ -237,7 +237,8 @@ cudaError_t scan_excl(const uint8_t* in, int64_t* out, int64_t n, int64_t* total
 }
 
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, int64_t n, int bits, cudaStream_t st,
-                           int shift0) {
+                           int shift0, uint64_t** where) {
+  if (where) *where = keys;
   if (n <= 1 || bits <= 0) return cudaSuccess;
   int64_t tiles = (n + kSortTile - 1) / kSortTile;
   int64_t* counts = nullptr;
@@ -254,7 +255,8 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, int64_t n, int bits, c
     a = b;
     b = t;
   }
-  if (e == cudaSuccess && a != keys)
+  if (e == cudaSuccess && where) *where = a;
+  else if (e == cudaSuccess && a != keys)
     e = cudaMemcpyAsync(keys, a, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, st);
   cudaFreeAsync(counts, st);
   return e;
