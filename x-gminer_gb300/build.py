@@ -1,4 +1,5 @@
-"""In-tree build of the engine's shared library (libxgm.so) for sm_103a.
+"""In-tree build of the engine's shared library (libxgm.so) for sm_103a, and of the
+command-line front end xgm_count_cli (cli/xgm_count_cli.cpp, C ABI only).
 
 Every translation unit under csrc/ is compiled by nvcc in parallel and linked into
 x-gminer_gb300/libxgm.so with the CUDA runtime linked statically, so the library loads
@@ -16,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libxgm.so")
+CLI_SRC = os.path.join(HERE, "cli", "xgm_count_cli.cpp")
+CLI = os.path.join(HERE, "xgm_count_cli")
+INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr"]
@@ -74,9 +78,27 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    _build_cli(relink=bool(jobs), hdr=hdr)
     if verbose:
         print(f"built {LIB} ({len(jobs)} units recompiled)", file=sys.stderr)
     return LIB
+
+
+def _build_cli(relink: bool, hdr: float) -> None:
+    """xgm_count_cli next to libxgm.so (found through an $ORIGIN rpath)."""
+    if (not relink and os.path.exists(CLI)
+            and os.path.getmtime(CLI) >= max(os.path.getmtime(CLI_SRC), hdr)):
+        return
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for xgm_count_cli")
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, CLI_SRC, "-L", HERE, "-lxgm",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"xgm_count_cli build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
 
 
 if __name__ == "__main__":
