@@ -315,6 +315,11 @@ def engine_arm(args, dist: Dist) -> None:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                      "traffic": traffic, "algo_bytes_per_launch": algo,
+                     # the measured DRAM traffic of the launch over its time: what the
+                     # kernel actually moves (it reads each list once per task)
+                     "dram_gbs": (traffic / (kern_ms / 1e3) / 1e9) if traffic else None,
+                     "dram_frac": (traffic / (kern_ms / 1e3) / 1e9 / peaks["hbm_gbs"])
+                     if traffic else None,
                      "peak_source": peaks["source"]},
         "clocks": clk,
     }
