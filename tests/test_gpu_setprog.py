@@ -145,3 +145,29 @@ def test_glumin5_identities_rmat_s12(xgm, ctx):
                    induced=True)
     assert ctx.count(g, "P22") == 24 * ctx.count(g, "4-clique") + 12 * ctx.count(g, k5e)
     g.close()
+
+
+def test_glumin5_hub_above_bitmap_range(xgm, ctx, orc):
+    # a hub of degree 1,499 (above the bitmap forms' 1,024): its tasks run in the list
+    # form while the other vertices' tasks take the bitmap forms, within one count; the
+    # plans here are the ones the oracle finishes quickly on such a hub (P12 a stream plan)
+    rowptr, col = _hub_graph(1500, 0.01, 9)
+    assert int(np.diff(rowptr).max()) > 1024
+    g = ctx.graph_from_csr(rowptr, col)
+    for pid in (9, 12, 13, 14, 17, 19, 20, 22):
+        assert ctx.count(g, f"P{pid}") == orc.glumin5(pid, rowptr, col), pid
+    g.close()
+
+
+def test_record_overflow_paths(xgm, ctx, orc, monkeypatch):
+    # with the record capacities lowered (test hook), the tasks that cannot queue their
+    # split / stream records run them themselves; counts are unchanged
+    rowptr, col = _hub_graph(400, 0.02, 5)
+    g = ctx.graph_from_csr(rowptr, col)
+    want = {pid: orc.glumin5(pid, rowptr, col) for pid in (6, 7, 10, 15)}
+    for cap in ("0", "7"):
+        monkeypatch.setenv("XGM_PROG_RECORD_CAP", cap)
+        for pid, w in want.items():
+            assert ctx.count(g, f"P{pid}") == w, (cap, pid)
+    monkeypatch.delenv("XGM_PROG_RECORD_CAP")
+    g.close()

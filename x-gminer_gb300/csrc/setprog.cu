@@ -29,6 +29,7 @@
 // later step.
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 
 #include "api_internal.h"
@@ -69,7 +70,8 @@ struct ProgArgs {
   // record tail, [5] stream record head
   unsigned long long* heads;
   SplitRec* split;
-  int64_t split_cap;
+  int64_t split_cap;   // split records (then the stream records at split + split_cap)
+  int64_t stream_cap;  // stream records of the bitmap form
   unsigned long long* total;
   int split_mode;
   int lut_ok;      // the bitmap kernel takes the tasks with small v0 (ProgLut)
@@ -986,9 +988,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
         const bool lng = lane < d0 && d1 > kLutStream;
         const int nrec = lng ? (d1 + kStreamChunk - 1) / kStreamChunk : 0;
         const unsigned long long base = nrec ? atomicAdd(a.heads + 4, (unsigned long long)nrec) : 0;
-        const bool fits = base + nrec <= (unsigned long long)kStreamCap;
+        const bool fits = base + nrec <= (unsigned long long)a.stream_cap;
         for (int r = 0; r < nrec; ++r)
-          if (base + r < (unsigned long long)kStreamCap)
+          if (base + r < (unsigned long long)a.stream_cap)
             srec[base + r] = fits ? SplitRec{(int32_t)v0, lane, r * kStreamChunk,
                                             min((r + 1) * kStreamChunk, d1)}
                                   : SplitRec{0, 0, 0, 0};
@@ -1004,7 +1006,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
     }
   } else {
     const unsigned long long nrec = min(*(volatile unsigned long long*)(a.heads + 4),
-                                        (unsigned long long)kStreamCap);
+                                        (unsigned long long)a.stream_cap);
     for (;;) {
       unsigned long long r = 0;
       if (lane == 0) r = atomicAdd(a.heads + 5, 1ull);
@@ -1160,6 +1162,16 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   a.heads = (unsigned long long*)ctx->prog_heads;
   a.split = (SplitRec*)ctx->prog_split;
   a.split_cap = kSplitCap;
+  a.stream_cap = kStreamCap;
+  // test hook: XGM_PROG_RECORD_CAP lowers both record capacities, so the overflow
+  // paths (a task that cannot queue its records runs them itself) can be exercised
+  if (const char* cap = std::getenv("XGM_PROG_RECORD_CAP")) {
+    const long long c = std::atoll(cap);
+    if (c >= 0) {
+      a.split_cap = std::min<int64_t>(a.split_cap, c);
+      a.stream_cap = std::min<int64_t>(a.stream_cap, c);
+    }
+  }
   a.total = &ctx->d_sc->count;
   a.split_mode = 0;
   a.lut_ok = lut_ok ? 1 : 0;
@@ -1188,7 +1200,7 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   st.kernel_ms = kern;
   st.launches = launches;
   st.tasks = g.ne;
-  st.variant_tasks[XGM_VAR_SPLIT] = std::min<int64_t>(ctx->h_sc->n[0], kSplitCap);
+  st.variant_tasks[XGM_VAR_SPLIT] = std::min<int64_t>(ctx->h_sc->n[0], a.split_cap);
   *out = ctx->h_sc->count;
   return XGM_OK;
 }
