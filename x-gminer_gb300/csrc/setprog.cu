@@ -818,6 +818,55 @@ __device__ uint32_t row_over(const int32_t* n0, int d0, int y, const ProgArgs& a
   return r;
 }
 
+// Two-hop rows of a small v0 (stream programs): for every y adjacent to some N(v0)[i],
+// the bits i with y in N(N(v0)[i]) — which is y's row over N(v0) (the graph is
+// symmetric).  Built once per v0 by streaming the N(v0) members' lists into an
+// open-addressing map in shared memory, so a streamed v2's row is one probe instead of
+// a walk over N(v2).  Skipped (rows built on the fly) when the lists would fill more
+// than half the map.
+constexpr int kMapSlots = 512;
+
+__device__ __forceinline__ uint32_t map_hash(int y) { return ((uint32_t)y * 2654435761u) >> 23; }
+
+// Returns whether the map was built (all lanes agree).
+__device__ bool map_build(int32_t* hkey, uint32_t* hval, const int32_t* n0, int d0,
+                          const ProgArgs& a, int lane) {
+  long long tot = 0;
+  if (lane < d0) tot = a.rowptr[n0[lane] + 1] - a.rowptr[n0[lane]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (tot > kMapSlots / 2) return false;
+  for (int k = lane; k < kMapSlots; k += 32) hkey[k] = -1, hval[k] = 0u;
+  __syncwarp();
+  for (int i = 0; i < d0; ++i) {
+    const long long rb = a.rowptr[n0[i]];
+    const int du = (int)(a.rowptr[n0[i] + 1] - rb);
+    for (int t = lane; t < du; t += 32) {
+      const int y = a.col[rb + t];
+      uint32_t h = map_hash(y);
+      for (int probe = 0; probe < kMapSlots; ++probe, h = (h + 1) & (kMapSlots - 1)) {
+        const int prev = atomicCAS(&hkey[h], -1, y);
+        if (prev == -1 || prev == y) {
+          atomicOr(&hval[h], 1u << i);
+          break;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  return true;
+}
+
+__device__ __forceinline__ uint32_t map_row(const int32_t* hkey, const uint32_t* hval, int y) {
+  uint32_t h = map_hash(y);
+  for (int probe = 0; probe < kMapSlots; ++probe, h = (h + 1) & (kMapSlots - 1)) {
+    const int k = hkey[h];
+    if (k == y) return hval[h];
+    if (k == -1) break;
+  }
+  return 0u;
+}
+
 struct LutLane {
   int v[kProgMaxK];    // matched ids
   int idx[kProgMaxK];  // index in N(v0), or -1
@@ -884,7 +933,9 @@ __device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, uint32
 template <int K>
 __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0, int i1, int d0,
                                        const int32_t* n0, const uint32_t* lut, uint32_t* sl,
-                                       int t0, int ts, int s_lo = 0, int s_hi = 1 << 30) {
+                                       int t0, int ts, int s_lo = 0, int s_hi = 1 << 30,
+                                       const int32_t* hkey = nullptr,
+                                       const uint32_t* hval = nullptr) {
   const int v1 = n0[i1];
   if (p.v1lt && v1 >= v0) return 0;
   const long long rb1 = a.rowptr[v1];
@@ -903,13 +954,38 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
     sl[o.out * 32] = lut_apply(L, o, lut_operand(L, o.a, sl, valid), valid);
   }
   unsigned long long c = 0;
+  // the count when the last level is the count alone: everything that does not depend
+  // on v3 (operand, valid range, bounds / exclusions of v0..v2, a row that is not v3's)
+  // folded once per v2, then per v3 its own bound, exclusion and row, and a popc
+  const ProgOp& fo = p.fin;
+  const bool flat5 = K == 5 && p.nops[2] == 0;
+  const bool f_ub = (fo.bound >> 3) & 1u, f_ux = (fo.excl >> 3) & 1u;
+  const bool f_v3 = fo.kind != OP_FILTER && fo.b == kOpList + 3;
+  const bool f_is = fo.kind == OP_INTERSECT;
   auto step2 = [&]() {
     if (K == 4) {
       c += lut_level<K>(p, 1, L, sl, valid);
       return;
     }
     lut_level<K>(p, 1, L, sl, valid);
-    for (uint32_t m = lut_operand(L, p.cand[3], sl, valid); m; m &= m - 1) {
+    const uint32_t c3 = lut_operand(L, p.cand[3], sl, valid);
+    if (flat5) {
+      ProgOp o2 = fo;
+      o2.bound &= 0x7u;
+      o2.excl &= 0x7u;
+      if (f_v3) o2.kind = OP_FILTER;
+      const uint32_t fk = lut_apply(L, o2, lut_operand(L, fo.a, sl, valid), valid);
+      for (uint32_t m = c3; m; m &= m - 1) {
+        const int b = __ffs(m) - 1;
+        uint32_t x = fk;
+        if (f_ub) x &= (1u << b) - 1u;
+        if (f_ux) x &= ~(1u << b);
+        if (f_v3) x = f_is ? (x & lut[b]) : (x & ~lut[b]);
+        c += (unsigned long long)__popc(x);
+      }
+      return;
+    }
+    for (uint32_t m = c3; m; m &= m - 1) {
       const int b = __ffs(m) - 1;
       lut_set(L, 3, n0[b], b, n0, d0);
       L.row[3] = lut[b];
@@ -931,7 +1007,7 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
       if (i < d0 && n0[i] == y) continue;
       if ((((o.excl >> 0) & 1u) && y == v0) || (((o.excl >> 1) & 1u) && y == v1)) continue;
       lut_set(L, 2, y, -1, n0, d0);
-      L.row[2] = row_over(n0, d0, y, a);
+      L.row[2] = hkey ? map_row(hkey, hval, y) : row_over(n0, d0, y, a);
       step2();
     }
   } else {
@@ -960,10 +1036,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
   __shared__ int32_t n0s[kWarps][32];
   __shared__ uint32_t luts[kWarps][32];
   __shared__ uint32_t sls[kWarps][kProgMaxSlots * 32];
+  __shared__ int32_t hkeys[kWarps][kMapSlots];
+  __shared__ uint32_t hvals[kWarps][kMapSlots];
   if (threadIdx.x == 0) p = prog;
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   SplitRec* srec = a.split + a.split_cap;  // stream records
+  int32_t* hk = hkeys[wib];
+  uint32_t* hv = hvals[wib];
   unsigned long long c = 0;
   if (a.lut_phase == 0) {
     for (;;) {
@@ -975,13 +1055,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
       const int d0 = (int)(a.rowptr[v0 + 1] - rb);
       if (d0 == 0 || d0 > kLutDeg) continue;
       lut_load(n0s[wib], luts[wib], rb, d0, a, lane);
+      const bool mapped = a.lut_stream >= 0 && map_build(hk, hv, n0s[wib], d0, a, lane);
       // one lane per task; stream tasks with a long N(v1) become stream records
       int d1 = 0;
       if (lane < d0) {
         const int v1 = n0s[wib][lane];
         d1 = (int)(a.rowptr[v1 + 1] - a.rowptr[v1]);
         if (a.lut_stream < 0 || d1 <= kLutStream)
-          c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane], 0, 1);
+          c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane], 0, 1,
+                           0, 1 << 30, mapped ? hk : nullptr, hv);
       }
       __syncwarp();
       if (a.lut_stream >= 0) {
@@ -999,7 +1081,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
         for (; todo; todo &= todo - 1) {
           const int i1 = __ffs(todo) - 1;
           c += lut_task<K>(p, a, (int)v0, i1, d0, n0s[wib], luts[wib], &sls[wib][lane], lane, 32,
-                           0, 1 << 30);
+                           0, 1 << 30, mapped ? hk : nullptr, hv);
         }
         __syncwarp();
       }
@@ -1018,8 +1100,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
       const long long rb = a.rowptr[v0];
       const int d0 = (int)(a.rowptr[v0 + 1] - rb);
       lut_load(n0s[wib], luts[wib], rb, d0, a, lane);
+      const bool mapped = map_build(hk, hv, n0s[wib], d0, a, lane);
       c += lut_task<K>(p, a, v0, rec.e_hi, d0, n0s[wib], luts[wib], &sls[wib][lane], rec.lo + lane,
-                       32, rec.lo, rec.hi);
+                       32, rec.lo, rec.hi, mapped ? hk : nullptr, hv);
       __syncwarp();
     }
   }
