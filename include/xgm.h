@@ -175,7 +175,7 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* desc, xgm_plan** 
  * "5-solid-house", "5-star", "5-tailed-square") give compiled edge-induced programs. */
 xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out);
 /* Plan from a GLUMIN pattern description, the text of one of
- * codes/GLUMIN/codegen/codegen/patterns/*.yml: its `edges: [AB, AC, ...]` list (vertices
+ * the .yml files in codes/GLUMIN/codegen/codegen/patterns: its `edges: [AB, AC, ...]` list (vertices
  * named by letters) is matched against the builtins, else compiled to a set-operation
  * program (up to 5 vertices).  GLUMIN's plans count vertex-induced embeddings (pass
  * induced = 1 for the same meaning). */

@@ -515,7 +515,8 @@ xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
 }
 
 xgm_status xgm_tc_solver(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total) {
-  xgm_plan p{XGM_PATTERN_TRIANGLE};
+  xgm_plan p;
+  p.pattern = XGM_PATTERN_TRIANGLE;
   return xgm_count(ctx, g, &p, nullptr, total, nullptr);
 }
 
@@ -526,7 +527,8 @@ xgm_status xgm_clique_solver(xgm_ctx* ctx, const xgm_graph* g, int k, uint64_t* 
   }
   static const int kPat[8] = {0, 0, 0, XGM_PATTERN_TRIANGLE, XGM_PATTERN_CLIQUE4,
                               XGM_PATTERN_CLIQUE5, XGM_PATTERN_CLIQUE6, XGM_PATTERN_CLIQUE7};
-  xgm_plan p{kPat[k]};
+  xgm_plan p;
+  p.pattern = kPat[k];
   return xgm_count(ctx, g, &p, nullptr, total, nullptr);
 }
 

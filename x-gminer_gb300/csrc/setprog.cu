@@ -364,7 +364,7 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
   set_vertex(w, 0, v0, a, lane);
   set_vertex(w, 1, v1, a, lane);
   for (int i = 0; i < p.nops[0]; ++i) run_op(p.ops[0][i], w, a, slots, lane);
-  if (K == 3) return count_op(p.fin, w, a, slots, lane);
+  if constexpr (K == 3) return count_op(p.fin, w, a, slots, lane);
   const Operand C2 = operand(w, p.cand[2], a, slots);
   if (hi < 0 || hi > C2.n) hi = C2.n;
   if (may_split && C2.n > 1) {
@@ -398,7 +398,7 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
     }
   }
   unsigned long long c = 0;
-  if (K == 4) {
+  if constexpr (K == 4) {
     if (p.flat) return count_flat(p.fin, w, 2, C2, lo, hi, a, slots, big, lane);
     for (int i2 = lo; i2 < hi; ++i2) {
       set_vertex(w, 2, C2.p[i2], a, lane);
@@ -406,22 +406,23 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
       c += count_op(p.fin, w, a, slots, lane);
     }
     return c;
-  }
-  for (int i2 = lo; i2 < hi; ++i2) {
-    set_vertex(w, 2, C2.p[i2], a, lane);
-    for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
-    const Operand C3 = operand(w, p.cand[3], a, slots);
-    if (p.flat) {
-      c += count_flat(p.fin, w, 3, C3, 0, C3.n, a, slots, big, lane);
-    } else {
-      for (int i3 = 0; i3 < C3.n; ++i3) {
-        set_vertex(w, 3, C3.p[i3], a, lane);
-        for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
-        c += count_op(p.fin, w, a, slots, lane);
+  } else {
+    for (int i2 = lo; i2 < hi; ++i2) {
+      set_vertex(w, 2, C2.p[i2], a, lane);
+      for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
+      const Operand C3 = operand(w, p.cand[3], a, slots);
+      if (p.flat) {
+        c += count_flat(p.fin, w, 3, C3, 0, C3.n, a, slots, big, lane);
+      } else {
+        for (int i3 = 0; i3 < C3.n; ++i3) {
+          set_vertex(w, 3, C3.p[i3], a, lane);
+          for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
+          c += count_op(p.fin, w, a, slots, lane);
+        }
       }
     }
+    return c;
   }
-  return c;
 }
 
 __device__ __forceinline__ int row_of(const int64_t* rowptr, int64_t nv, long long e) {
