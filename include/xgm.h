@@ -140,18 +140,18 @@ typedef enum {
   XGM_PATTERN_CLIQUE6 = 10,         /* GLUMIN P23 (clique6_warp_edge*.cuh) */
   XGM_PATTERN_CLIQUE7 = 11,         /* GLUMIN P24 (clique7_warp_edge*.cuh) */
   XGM_PATTERN_PROGRAM = 12          /* set-operation program: GLUMIN's P6..P22, or a
-                                       compiled connected pattern of up to 5 vertices */
+                                       compiled connected pattern of up to 6 vertices */
 } xgm_pattern;
 
 /* Words of a set-operation program in flat form (xgm_plan_program). */
-#define XGM_PROGRAM_WORDS 124
+#define XGM_PROGRAM_WORDS 162
 
 typedef struct {
   int builtin;            /* xgm_pattern, or 0 to match `adj`: a builtin when one has this
                              shape, else a compiled set-operation program (connected
-                             patterns of up to 5 vertices, each occurrence counted once);
+                             patterns of up to 6 vertices, each occurrence counted once);
                              XGM_PATTERN_PROGRAM compiles `adj` even where a builtin exists */
-  int num_vertices;       /* pattern size when builtin == 0 (3..5; 6 and 7 for cliques) */
+  int num_vertices;       /* pattern size when builtin == 0 (3..6; 7 for the 7-clique) */
   uint8_t adj[8][8];      /* pattern adjacency when builtin == 0 */
   int induced;            /* 0: edge-induced; 1: vertex-induced (the non-clique motifs are
                              derived from edge-induced counts, the 4-clique count and the
@@ -177,12 +177,13 @@ xgm_status xgm_plan_from_name(xgm_ctx* ctx, const char* name, xgm_plan** out);
 /* Plan from a GLUMIN pattern description, the text of one of
  * the .yml files in codes/GLUMIN/codegen/codegen/patterns: its `edges: [AB, AC, ...]` list (vertices
  * named by letters) is matched against the builtins, else compiled to a set-operation
- * program (up to 5 vertices).  GLUMIN's plans count vertex-induced embeddings (pass
+ * program (up to 6 vertices).  GLUMIN's plans count vertex-induced embeddings (pass
  * induced = 1 for the same meaning). */
 xgm_status xgm_plan_from_spec(xgm_ctx* ctx, const char* spec, int induced, xgm_plan** out);
 int xgm_plan_pattern(const xgm_plan* p);
-/* A program plan's flat form: [1, k, slots, flat, v1 < v0 task filter, ops per level
- * (3), v2 / v3 candidate operands, then 19 operations of six words (out slot, kind 0 intersect /
+/* A program plan's flat form: [2 (format version), k, slots, flat, v1 < v0 task filter,
+ * ops per level (4), v2 / v3 / v4 candidate operands, then 25 operations of six words
+ * (out slot, kind 0 intersect /
  * 1 difference / 2 filter, operand a, operand b, bound mask, exclusion mask); an
  * operand >= 16 is N(v_(operand-16)), below it a slot].  Returns XGM_PROGRAM_WORDS
  * (writing words[] when n_words is at least that), 0 for a builtin plan. */

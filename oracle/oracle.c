@@ -741,8 +741,8 @@ int orc_glumin5(int pid, int64_t nv, const int64_t* rowptr, const int32_t* col, 
  * over its candidate operand; the last level ends with the counted operation.
  * Operand >= 16 is N(v_(operand-16)), below it a slot. */
 typedef struct {
-  int k, nslots, flat, v1lt, nops[3], cand[5];
-  int op[3][6][6];
+  int k, nslots, flat, v1lt, nops[4], cand[6];
+  int op[4][6][6];
   int fin[6];
 } prog_t;
 
@@ -750,9 +750,9 @@ typedef struct {
   const prog_t* p;
   const int64_t* rowptr;
   const int32_t* col;
-  vid_t v[5];
-  vid_t* slot[12];
-  eid_t slen[12];
+  vid_t v[6];
+  vid_t* slot[16];
+  eid_t slen[16];
 } pstate_t;
 
 static void p_operand(pstate_t* st, int code, const vid_t** a, eid_t* n) {
@@ -783,7 +783,7 @@ static uint64_t p_apply(pstate_t* st, const int* o, vid_t* out, eid_t* nout) {
   p_operand(st, o[2], &a, &na);
   if (o[1] != 2) p_operand(st, o[3], &b, &nb);
   vid_t up = INT32_MAX;
-  for (int j = 0; j < 5; j++)
+  for (int j = 0; j < 6; j++)
     if ((o[4] >> j) & 1)
       if (st->v[j] < up) up = st->v[j];
   uint64_t c = 0;
@@ -791,7 +791,7 @@ static uint64_t p_apply(pstate_t* st, const int* o, vid_t* out, eid_t* nout) {
   for (eid_t i = 0; i < na && a[i] < up; i++) {
     vid_t x = a[i];
     int skip = 0;
-    for (int j = 0; j < 5; j++)
+    for (int j = 0; j < 6; j++)
       if (((o[5] >> j) & 1) && x == st->v[j]) skip = 1;
     if (skip) continue;
     if (o[1] != 2 && p_member(b, nb, x) != (o[1] == 0)) continue;
@@ -823,19 +823,18 @@ static uint64_t p_level(pstate_t* st, int l) {
 /* Runs a program over every directed CSR entry; returns 0, or -1 for malformed words. */
 int orc_setprog(const int32_t* w, int nw, int64_t nv, const int64_t* rowptr, const int32_t* col,
                 int64_t max_deg, uint64_t* out) {
-  if (nw < 124 || w[0] != 1) return -1;
+  if (nw < 162 || w[0] != 2) return -1;  /* format version 2 */
   prog_t p;
   memset(&p, 0, sizeof(p));
   p.k = w[1];
   p.nslots = w[2];
   p.flat = w[3];
   p.v1lt = w[4];
-  for (int l = 0; l < 3; l++) p.nops[l] = w[5 + l];
-  p.cand[2] = w[8];
-  p.cand[3] = w[9];
-  if (p.k < 3 || p.k > 5 || p.nslots < 0 || p.nslots > 12) return -1;
-  const int32_t* o = w + 10;
-  for (int l = 0; l < 3; l++)
+  for (int l = 0; l < 4; l++) p.nops[l] = w[5 + l];
+  for (int i = 2; i < 5; i++) p.cand[i] = w[9 + i - 2];
+  if (p.k < 3 || p.k > 6 || p.nslots < 0 || p.nslots > 16) return -1;
+  const int32_t* o = w + 12;
+  for (int l = 0; l < 4; l++)
     for (int i = 0; i < 6; i++, o += 6) memcpy(p.op[l][i], o, sizeof(int) * 6);
   memcpy(p.fin, o, sizeof(int) * 6);
   uint64_t total = 0;
@@ -847,8 +846,8 @@ int orc_setprog(const int32_t* w, int nw, int64_t nv, const int64_t* rowptr, con
     st.p = &p;
     st.rowptr = rowptr;
     st.col = col;
-    vid_t* buf = (vid_t*)malloc(sizeof(vid_t) * 12 * (size_t)md);
-    for (int i = 0; i < 12; i++) st.slot[i] = buf + (size_t)i * md;
+    vid_t* buf = (vid_t*)malloc(sizeof(vid_t) * 16 * (size_t)md);
+    for (int i = 0; i < 16; i++) st.slot[i] = buf + (size_t)i * md;
 #pragma omp for schedule(dynamic, 16)
     for (int64_t v0 = 0; v0 < nv; v0++)
       for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {

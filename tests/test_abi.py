@@ -113,7 +113,7 @@ def test_plan_names_and_ids(xgm):
         p = xgm.plan(f"P{pid}")
         assert (p.pattern, p.induced) == (xgm.PROGRAM, True), pid
         w = p.program
-        assert w is not None and len(w) == xgm.PROGRAM_WORDS and w[0] == 1 and w[1] == 5
+        assert w is not None and len(w) == xgm.PROGRAM_WORDS and w[0] == 2 and w[1] == 5
     for name in xgm.YML5_EDGES:  # GLUMIN's 5-vertex .yml names: compiled, edge-induced
         p = xgm.plan(name)
         assert (p.pattern, p.induced) == (xgm.PROGRAM, False), name
@@ -141,7 +141,7 @@ def test_plan_from_spec(xgm):
     for bad, st in [(_spec(["AB", "A"]), xgm.ERR_INVALID), (_spec(["AA", "AB"]), xgm.ERR_INVALID),
                     ("pattern:\n  name: x\n", xgm.ERR_INVALID), (_spec([]), xgm.ERR_INVALID),
                     (_spec(["AB", "CD"]), xgm.ERR_UNSUPPORTED),  # disconnected
-                    (_spec(["AB", "BC", "CD", "DE", "EF"]), xgm.ERR_UNSUPPORTED)]:  # 6-path
+                    (_spec(["AB", "BC", "CD", "DE", "EF", "FG"]), xgm.ERR_UNSUPPORTED)]:  # 7-path
         with pytest.raises(xgm.XgmError) as e:
             xgm.plan_from_spec(bad)
         assert e.value.status == st, bad

@@ -171,3 +171,26 @@ def test_record_overflow_paths(xgm, ctx, orc, monkeypatch):
             assert ctx.count(g, f"P{pid}") == w, (cap, pid)
     monkeypatch.delenv("XGM_PROG_RECORD_CAP")
     g.close()
+
+
+def test_compiled_six_vertex_programs_gpu(xgm, ctx, orc):
+    # every connected 6-vertex pattern, vertex- and edge-induced, against brute force on a
+    # small random graph; then a hub graph (split records) against the oracle's
+    # interpreter of the same program words
+    pats = _connected_patterns(6)
+    rowptr, col = _random_graph(22, 0.35, 4)
+    g = ctx.graph_from_csr(rowptr, col)
+    for a in pats:
+        for induced in (True, False):
+            plan = ctx.plan(a, induced=induced, program=True)
+            assert ctx.count(g, plan) == orc.occurrences(a, induced, rowptr, col), \
+                (a.tolist(), induced)
+    g.close()
+    rowptr, col = _hub_graph(120, 0.04, 11)
+    g = ctx.graph_from_csr(rowptr, col)
+    for edges, induced in (([(0, i) for i in range(1, 6)], True),
+                           ([(i, i + 1) for i in range(5)], False),
+                           ([(i, (i + 1) % 6) for i in range(6)], True)):
+        plan = ctx.plan(_adj(edges, 6), induced=induced, program=True)
+        assert ctx.count(g, plan) == orc.program(plan.program, rowptr, col), edges
+    g.close()

@@ -109,10 +109,23 @@ def test_engine_glumin_tables(xgm, orc):
 
 
 def _connected_patterns(k):
+    """One adjacency matrix per isomorphism class of connected k-vertex graphs.  The
+    canonical form of every edge set (a bitmask over the vertex pairs) is the smallest
+    mask over all vertex permutations, computed for all edge sets at once."""
     pairs = list(itertools.combinations(range(k), 2))
-    seen, out = set(), []
-    for m in range(1, 1 << len(pairs)):
-        es = [pairs[i] for i in range(len(pairs)) if m >> i & 1]
+    index = {pq: i for i, pq in enumerate(pairs)}
+    masks = np.arange(1 << len(pairs), dtype=np.int64)
+    canon = masks.copy()
+    for perm in itertools.permutations(range(k)):
+        mapped = np.zeros_like(masks)
+        for i, (u, v) in enumerate(pairs):
+            pu, pv = perm[u], perm[v]
+            j = index[(pu, pv) if pu < pv else (pv, pu)]
+            mapped |= ((masks >> i) & 1) << j
+        np.minimum(canon, mapped, out=canon)
+    out = []
+    for m in np.unique(canon):
+        es = [pairs[i] for i in range(len(pairs)) if (int(m) >> i) & 1]
         a = _adj(es, k)
         reach, stack = {0}, [0]
         while stack:
@@ -121,11 +134,7 @@ def _connected_patterns(k):
                 if int(y) not in reach:
                     reach.add(int(y))
                     stack.append(int(y))
-        if len(reach) < k:
-            continue
-        key = min(tuple(a[np.ix_(q, q)].ravel()) for q in itertools.permutations(range(k)))
-        if key not in seen:
-            seen.add(key)
+        if len(reach) == k:
             out.append(a)
     return out
 
@@ -146,6 +155,20 @@ def test_compiled_programs_count_occurrences(xgm, orc):
                 assert orc.program(w, rowptr, col) == want, (a.tolist(), induced, n)
 
 
+def test_compiled_six_vertex_programs(xgm, orc):
+    # every connected 6-vertex pattern (112), vertex- and edge-induced, on a small random
+    # graph: the compiled program run by the oracle's interpreter equals brute force
+    pats = _connected_patterns(6)
+    assert len(pats) == 112
+    rowptr, col = _random_graph(22, 0.35, 4)
+    for a in pats:
+        for induced in (True, False):
+            w = xgm.plan(a, induced=induced, program=True).program
+            assert w is not None and w[1] == 6
+            assert orc.program(w, rowptr, col) == orc.occurrences(a, induced, rowptr, col), \
+                (a.tolist(), induced)
+
+
 def test_program_plan_api(xgm):
     # 5-vertex non-clique patterns compile without asking; the 5-clique stays a builtin
     bull = _adj([(0, 1), (0, 2), (0, 4), (1, 2), (1, 3)])
@@ -154,10 +177,11 @@ def test_program_plan_api(xgm):
     assert xgm.plan(np.ones((5, 5), np.uint8) - np.eye(5, dtype=np.uint8)).pattern == xgm.CLIQUE5
     # a program's words: version, k, slots within bounds, operand codes well formed
     w = p.program
-    assert w[0] == 1 and w[1] == 5 and 0 < w[2] <= 12 and w[4] in (0, 1)
+    assert w[0] == 2 and w[1] == 5 and 0 < w[2] <= 16 and w[4] in (0, 1)
     with pytest.raises(xgm.XgmError) as e:  # disconnected
         xgm.plan(_adj([(0, 1), (2, 3), (3, 4)]), induced=True)
     assert e.value.status == xgm.ERR_UNSUPPORTED
-    with pytest.raises(xgm.XgmError) as e:  # six vertices, no clique
-        xgm.plan(_adj([(i, i + 1) for i in range(5)], 6), induced=True)
+    with pytest.raises(xgm.XgmError) as e:  # seven vertices, no clique
+        xgm.plan(_adj([(i, i + 1) for i in range(6)], 7), induced=True)
     assert e.value.status == xgm.ERR_UNSUPPORTED
+    assert xgm.plan(_adj([(i, i + 1) for i in range(5)], 6), induced=True).program[1] == 6

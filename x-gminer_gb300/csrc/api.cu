@@ -346,12 +346,12 @@ xgm_status xgm_plan_compile(xgm_ctx* ctx, const xgm_plan_desc* d, xgm_plan** out
       return finish_status(ctx, XGM_ERR_INVALID);
     }
     if (pat == 0 || force_program) {
-      // no builtin: a set-operation program (connected patterns of up to 5 vertices)
+      // no builtin: a set-operation program (connected patterns of up to 6 vertices)
       Prog prog;
       std::string why;
       if (d->num_vertices > kProgMaxK) {
         set_thread_error("pattern not supported (builtins, or any connected pattern of up to "
-                         "5 vertices)");
+                         "6 vertices)");
         return finish_status(ctx, XGM_ERR_UNSUPPORTED);
       }
       if (!prog_compile(d->num_vertices, d->adj, d->induced != 0, &prog, &why)) {

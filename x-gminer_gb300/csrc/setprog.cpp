@@ -131,7 +131,7 @@ bool prog_glumin(int pid, Prog* p) {
 // non-neighbours when vertex-induced, with matched non-neighbours excluded
 // explicitly (a difference does not remove v_m itself).
 bool prog_compile(int k, const uint8_t adj[8][8], bool induced, Prog* out, std::string* why) {
-  if (k < 3 || k > kProgMaxK) return fail(why, "programs cover patterns of 3 to 5 vertices"), false;
+  if (k < 3 || k > kProgMaxK) return fail(why, "programs cover patterns of 3 to 6 vertices"), false;
   int deg[8] = {};
   for (int i = 0; i < k; ++i)
     for (int j = 0; j < k; ++j) {
@@ -324,14 +324,13 @@ bool prog_check(const Prog& p, std::string* why) {
 
 void prog_to_words(const Prog& p, int32_t* w) {
   std::memset(w, 0, sizeof(int32_t) * kProgWords);
-  w[0] = 1;
+  w[0] = kProgVersion;
   w[1] = p.k;
   w[2] = p.nslots;
   w[3] = p.flat;
   w[4] = p.v1lt;
   for (int l = 0; l < kProgLevels; ++l) w[5 + l] = p.nops[l];
-  w[8] = p.cand[2];
-  w[9] = p.cand[3];
+  for (int i = 2; i < kProgMaxK - 1; ++i) w[9 + i - 2] = p.cand[i];
   int32_t* o = w + kProgHeader;
   auto put = [&](const ProgOp& x) {
     o[0] = x.out, o[1] = x.kind, o[2] = x.a, o[3] = x.b, o[4] = x.bound, o[5] = x.excl;
@@ -343,15 +342,14 @@ void prog_to_words(const Prog& p, int32_t* w) {
 }
 
 bool prog_from_words(const int32_t* w, int n, Prog* p, std::string* why) {
-  if (n < kProgWords || w[0] != 1) return fail(why, "not a program (version word)"), false;
+  if (n < kProgWords || w[0] != kProgVersion) return fail(why, "not a program (version word)"), false;
   Prog q;
   q.k = (int8_t)w[1];
   q.nslots = (int8_t)w[2];
   q.flat = (int8_t)w[3];
   q.v1lt = (int8_t)w[4];
   for (int l = 0; l < kProgLevels; ++l) q.nops[l] = (int8_t)w[5 + l];
-  q.cand[2] = (int8_t)w[8];
-  q.cand[3] = (int8_t)w[9];
+  for (int i = 2; i < kProgMaxK - 1; ++i) q.cand[i] = (int8_t)w[9 + i - 2];
   const int32_t* o = w + kProgHeader;
   auto get = [&](ProgOp& x) {
     x = op(o[0], o[1], o[2], o[3], o[4], o[5]);

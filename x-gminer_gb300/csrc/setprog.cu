@@ -352,7 +352,8 @@ __device__ unsigned step_roots(const Prog& p) {
   for (int l = 1; l < kProgLevels; ++l)
     for (int i = 0; i < p.nops[l]; ++i) add(p.ops[l][i].a);
   add(p.fin.a);
-  if (p.k == 5) add(p.cand[3]);
+  if (p.k >= 5) add(p.cand[3]);
+  if (p.k == 6) add(p.cand[4]);
   return m;
 }
 
@@ -369,13 +370,15 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
   if (hi < 0 || hi > C2.n) hi = C2.n;
   if (may_split && C2.n > 1) {
     // lane-steps of one v2 step: the streams of the level-1 operations, then the
-    // final count over (v3, x) pairs (5 vertices) or over x (4 vertices)
+    // final count over (v3, x) pairs (5 vertices), over x (4 vertices), or a v3 loop
+    // of such counts (6 vertices)
     int len = 0;
     for (int j = 0; j < kProgMaxSlots; ++j)
       if ((roots >> j) & 1u) len = max(len, w.slen[j]);
     if ((roots >> 16) & 1u) len = max(len, w.vl[0]);
     if ((roots >> 17) & 1u) len = max(len, w.vl[1]);
-    const long long step = 1 + len / 32 + (K == 5 ? (long long)len * len / 64 : 0);
+    const long long step = 1 + len / 32 + (K >= 5 ? (long long)len * len / 64 : 0) *
+                                                (K == 6 ? 1 + len / 32 : 1);
     if ((long long)C2.n * step > kSplitWork) {
       // every candidate goes to the records, so a warp that claims a chunk of heavy
       // tasks only builds their level-0 slots
@@ -406,7 +409,7 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
       c += count_op(p.fin, w, a, slots, lane);
     }
     return c;
-  } else {
+  } else if constexpr (K == 5) {
     for (int i2 = lo; i2 < hi; ++i2) {
       set_vertex(w, 2, C2.p[i2], a, lane);
       for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
@@ -418,6 +421,27 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
           set_vertex(w, 3, C3.p[i3], a, lane);
           for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
           c += count_op(p.fin, w, a, slots, lane);
+        }
+      }
+    }
+    return c;
+  } else {  // 6 vertices: one more enumerated level (v3), then as 5 vertices with v4
+    for (int i2 = lo; i2 < hi; ++i2) {
+      set_vertex(w, 2, C2.p[i2], a, lane);
+      for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
+      const Operand C3 = operand(w, p.cand[3], a, slots);
+      for (int i3 = 0; i3 < C3.n; ++i3) {
+        set_vertex(w, 3, C3.p[i3], a, lane);
+        for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
+        const Operand C4 = operand(w, p.cand[4], a, slots);
+        if (p.flat) {
+          c += count_flat(p.fin, w, 4, C4, 0, C4.n, a, slots, big, lane);
+        } else {
+          for (int i4 = 0; i4 < C4.n; ++i4) {
+            set_vertex(w, 4, C4.p[i4], a, lane);
+            for (int i = 0; i < p.nops[3]; ++i) run_op(p.ops[3][i], w, a, slots, lane);
+            c += count_op(p.fin, w, a, slots, lane);
+          }
         }
       }
     }
@@ -1140,7 +1164,8 @@ int occupancy(int k) {
   int n = 0;
   cudaError_t e = k == 3   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<3>, kThreads, 0)
                   : k == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<4>, kThreads, 0)
-                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<5>, kThreads, 0);
+                  : k == 5 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<5>, kThreads, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_setprog<6>, kThreads, 0);
   return (e == cudaSuccess && n > 0) ? n : 1;
 }
 
@@ -1267,7 +1292,8 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
   if (g.ne > 0) {
     cudaError_t e = p.k == 3   ? launch_k<3>(p, a, grid, s)
                     : p.k == 4 ? launch_k<4>(p, a, grid, s)
-                               : launch_k<5>(p, a, grid, s);
+                    : p.k == 5 ? launch_k<5>(p, a, grid, s)
+                               : launch_k<6>(p, a, grid, s);
     if (e != cudaSuccess) return cuda_fail(e, "k_setprog", __FILE__, __LINE__);
     launches = p.k == 3 ? 1 : (a.lut_ok ? (a.lut_stream >= 0 ? 4 : 3) : 2);
   }

@@ -12,7 +12,7 @@
 // elements below a matched vertex's id (set_difference.cuh:44-86, 176-232).
 //
 // Here a plan is data, not code: the programs for GLUMIN's P6-P22 are tables
-// (setprog.cpp), and a compiler turns any other connected pattern of up to five
+// (setprog.cpp), and a compiler turns any other connected pattern of up to six
 // vertices into a program with exact symmetry breaking and explicit exclusion of the
 // vertices already matched.
 #pragma once
@@ -22,10 +22,10 @@
 
 namespace xgm {
 
-constexpr int kProgMaxK = 5;
+constexpr int kProgMaxK = 6;
 constexpr int kProgLevels = kProgMaxK - 2;  // level l runs after v_{l+1} is matched
 constexpr int kProgMaxOps = 6;              // per level
-constexpr int kProgMaxSlots = 12;
+constexpr int kProgMaxSlots = 16;
 constexpr int kOpList = 16;                 // operand kOpList + j: N(v_j); below: a slot
 
 enum ProgOpKind : int8_t { OP_INTERSECT = 0, OP_DIFFERENCE = 1, OP_FILTER = 2 };
@@ -43,7 +43,7 @@ struct ProgOp {
 };
 
 struct Prog {
-  int8_t k = 0;                  // pattern vertices, 3..5
+  int8_t k = 0;                  // pattern vertices, 3..6
   int8_t nslots = 0;
   int8_t flat = 0;               // last vertex loop merged with the final count
   int8_t v1lt = 0;               // tasks keep v1 < v0 only (v0, v1 interchangeable)
@@ -54,9 +54,10 @@ struct Prog {
 };
 
 // Flat word form shared with the C-ABI (xgm_plan_program) and the oracle:
-// [1, k, nslots, flat, v1lt, nops[0..2], cand[2..3], then 3 x kProgMaxOps ops and fin,
-// six words each: out, kind, a, b, bound, excl].
-constexpr int kProgHeader = 10;
+// [2 (format version), k, nslots, flat, v1lt, nops[0..3], cand[2..4], then
+// 4 x kProgMaxOps ops and fin, six words each: out, kind, a, b, bound, excl].
+constexpr int kProgVersion = 2;
+constexpr int kProgHeader = 12;
 constexpr int kProgWords = kProgHeader + (kProgLevels * kProgMaxOps + 1) * 6;
 void prog_to_words(const Prog& p, int32_t* w);
 bool prog_from_words(const int32_t* w, int n, Prog* p, std::string* why);
@@ -76,7 +77,7 @@ bool prog_lut(const Prog& p, ProgLut* out);
 
 // GLUMIN's P6..P22 (vertex-induced 5-vertex plans), exactly as generated.
 bool prog_glumin(int pid, Prog* p);
-// A program counting each occurrence of the pattern (k vertices, symmetric 0/1
+// A program counting each occurrence of the pattern (k <= 6 vertices, symmetric 0/1
 // adjacency, connected) once: vertex-induced or edge-induced.
 bool prog_compile(int k, const uint8_t adj[8][8], bool induced, Prog* p, std::string* why);
 
