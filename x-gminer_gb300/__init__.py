@@ -36,7 +36,7 @@ VIEW_UNDIRECTED, VIEW_DAG = 0, 1
 
 TRIANGLE, CLIQUE4, CLIQUE5, DIAMOND, CYCLE4, TAILED_TRIANGLE = 1, 2, 3, 4, 5, 6
 WEDGE, STAR3, PATH4, CLIQUE6, CLIQUE7 = 7, 8, 9, 10, 11
-PROGRAM = 12  # set-operation program: GLUMIN P6..P22 or a compiled 5-vertex pattern
+PROGRAM = 12  # set-operation program: GLUMIN P6..P22 or a compiled pattern of up to 6 vertices
 PROGRAM_WORDS = 162
 GLUMIN5_IDS = [f"P{i}" for i in range(6, 23)]
 # GLUMIN's 5-vertex .yml patterns (codegen/codegen/patterns/5-*.yml), `edges:` lists
