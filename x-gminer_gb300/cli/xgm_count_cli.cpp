@@ -7,8 +7,11 @@
 //
 // <prefix> names the reference's binary graph files (<prefix>.meta.txt / .vertex.bin /
 // .edge.bin).  --patternID follows xgminer's numbering (include/common.h:185-208 and
-// glumin.h:34-39): 1 triangle, 2 rectangle, 3 diamond, 11 pentagon, 13 house,
-// 14 hourglass, 17..40 GLUMIN P1..P24 (patternID - 16).  Every GPU algorithm name of
+// glumin.h:34-39): 1 triangle, 2 rectangle, 3 diamond, and the GraphPi shapes of
+// src/pattern_graphpi.cpp:60-146 by their names there — 10 QG3 (K4 minus an edge),
+// 11 pentagon, 13 house, 14 hourglass (two triangles joined by a perfect matching),
+// 15 Cycle_6_Tri — counted edge-induced as GraphPi does unless --vert-induced; 17..40
+// GLUMIN P1..P24 (patternID - 16).  Every GPU algorithm name of
 // xgminer selects this engine (it picks its own kernels per task); cpu_baseline is the
 // reference's CPU path and is not part of this engine.  Prints the count the way the
 // reference's solvers do ("Pattern P<k> count: N") and the device time.
@@ -35,8 +38,8 @@ void usage(const char* prog) {
       "  algorithms: glumin_g2miner, glumin_g2miner_lut, glumin_gf, glumin_gf_lut,\n"
       "              glumin_automine, glumin_automine_lut, glumin_cliques, glumin_cliques_lut,\n"
       "              bitmap_bigset_opt (all run this engine)\n"
-      "  patternID:  1 triangle, 2 rectangle, 3 diamond, 11 pentagon, 13 house, 14 hourglass,\n"
-      "              17..40 GLUMIN P1..P24\n",
+      "  patternID:  1 triangle, 2 rectangle, 3 diamond, 10 QG3, 11 pentagon, 13 house,\n"
+      "              14 hourglass, 15 Cycle_6_Tri, 17..40 GLUMIN P1..P24\n",
       prog);
 }
 
@@ -87,9 +90,9 @@ const char* id_name(int id) {
     case 1: return "triangle";
     case 2: return "rectangle";
     case 3: return "diamond";
-    case 11: return "5-cycle";
-    case 13: return "5-house";
-    case 14: return "5-double-triangle";
+    case 10: return "diamond";  // GraphPi QG3: edges 01 02 03 12 13
+    case 11: return "5-cycle";  // GraphPi Pentagon
+    case 13: return "5-house";  // GraphPi House
     default: break;
   }
   if (id >= 17 && id <= 40) {
@@ -97,6 +100,28 @@ const char* id_name(int id) {
     return buf;
   }
   return nullptr;
+}
+
+// The 6-vertex GraphPi shapes (src/pattern_graphpi.cpp:104-132) as adjacency strings.
+const char* id_adj(int id) {
+  switch (id) {
+    case 14:  // Hourglass: 01 02 04 12 15 23 34 35 45
+      return "011010"
+             "101001"
+             "110100"
+             "001011"
+             "100101"
+             "010110";
+    case 15:  // Cycle_6_Tri: 01 02 12 13 14 23 25 04 05
+      return "011011"
+             "101110"
+             "110101"
+             "011000"
+             "110000"
+             "101000";
+    default:
+      return nullptr;
+  }
 }
 
 int fail(xgm_ctx* ctx, xgm_status st, const char* what) {
@@ -124,6 +149,10 @@ int main(int argc, char** argv) {
   if (o.graph.empty()) {
     usage(argv[0]);
     return 2;
+  }
+  if (o.adj.empty() && o.pattern_size == 0 && o.pattern_name.empty() && id_adj(o.pattern_id)) {
+    o.adj = id_adj(o.pattern_id);
+    o.pattern_size = 6;
   }
   const bool by_adj = !o.adj.empty() || o.pattern_size > 0;
   if (!by_adj && o.pattern_name.empty() && !id_name(o.pattern_id)) {
