@@ -21,9 +21,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 xgm = importlib.import_module("x-gminer_gb300")
 
-# xgminer patternIDs of the GLUMIN patterns (xgminer/include/glumin.h:34-39 maps
-# patternID - 16 to GLUMIN's P-number): every one of P1-P24
-PATTERN_IDS = {i: f"P{i - 16}" for i in range(17, 41)}
+# xgminer patternIDs (xgminer/include/common.h:185-208): 1-3 the count-app shapes, the
+# GraphPi shapes by their names in xgminer/src/pattern_graphpi.cpp:60-146 (edge-induced,
+# as GraphPi counts them; 6-vertex ones as adjacency matrices), and GLUMIN's P1-P24
+# (glumin.h:34-39 maps patternID - 16 to the P-number)
+PATTERN_IDS = {1: "triangle", 2: "rectangle", 3: "diamond", 10: "diamond", 11: "5-cycle",
+               13: "5-house"}
+PATTERN_IDS.update({i: f"P{i - 16}" for i in range(17, 41)})
+GRAPHPI_6 = {14: [(0, 1), (0, 2), (0, 4), (1, 2), (1, 5), (2, 3), (3, 4), (3, 5), (4, 5)],
+             15: [(0, 1), (0, 2), (1, 2), (1, 3), (1, 4), (2, 3), (2, 5), (0, 4), (0, 5)]}
 
 
 def main() -> None:
@@ -34,14 +40,22 @@ def main() -> None:
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--pattern", default="4-clique")
     ap.add_argument("--patternID", type=int,
-                    help="xgminer pattern id: 17-40 = GLUMIN P1-P24")
+                    help="xgminer pattern id: 1-3, 10, 11, 13-15 (GraphPi shapes), "
+                         "17-40 = GLUMIN P1-P24")
     ap.add_argument("--policy", choices=["heuristic", "learned"], default="heuristic")
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
-    if args.patternID and args.patternID not in PATTERN_IDS:
+    if args.patternID and args.patternID not in PATTERN_IDS and args.patternID not in GRAPHPI_6:
         raise SystemExit(f"patternID {args.patternID} is not a supported plan "
-                         f"(supported: {sorted(PATTERN_IDS)})")
-    pattern = PATTERN_IDS[args.patternID] if args.patternID else args.pattern
+                         f"(supported: {sorted(list(PATTERN_IDS) + list(GRAPHPI_6))})")
+    if args.patternID in GRAPHPI_6:
+        import numpy as np
+
+        pattern = np.zeros((6, 6), dtype=np.uint8)
+        for u, v in GRAPHPI_6[args.patternID]:
+            pattern[u, v] = pattern[v, u] = 1
+    else:
+        pattern = PATTERN_IDS[args.patternID] if args.patternID else args.pattern
     ctx = xgm.Context(0)
     if args.graph:
         g = ctx.load_graph(args.graph)
@@ -63,7 +77,8 @@ def main() -> None:
               "margin": float(spec.get("margin", 0.0))}
     for _ in range(args.repeat):
         count, st = ctx.count(g, xgm.plan(pattern), with_stats=True, **kw)
-        print(json.dumps({"pattern": pattern, "count": count, "graph": g.info(), **st}))
+        name = pattern if isinstance(pattern, str) else f"patternID {args.patternID}"
+        print(json.dumps({"pattern": name, "count": count, "graph": g.info(), **st}))
     ctx.close()
 
 
