@@ -248,7 +248,7 @@ bool prog_compile(int k, const uint8_t adj[8][8], bool induced, Prog* out, std::
 // has that shape.
 bool prog_lut(const Prog& p, ProgLut* out) {
   ProgLut r;
-  if (p.k < 4 || p.k > 5) return *out = r, false;
+  if (p.k < 4 || p.k > 5 || p.nslots > kLutSlots) return *out = r, false;
   // space of each slot: 1 = subset of N(v0) (bitmap), 2 = the N(v1) \ N(v0) stream
   int8_t space[kProgMaxSlots] = {};
   auto n0 = [&](int code) { return code == G(0) || (code < kOpList && space[code] == 1); };

@@ -104,7 +104,7 @@ struct WarpState {
   // slots (one word per lane) and the row of a v2 outside N(v0)
   int idx[kProgMaxK];
   int pre[kProgMaxK];
-  uint32_t bits[kProgMaxSlots][32];
+  uint32_t bits[kLutSlots][32];
   uint32_t rowbuf[32];
   uint32_t fk[32];  // bits_flat_fin: the counted operand with the v3-independent masks
 };
@@ -144,28 +144,33 @@ __device__ __forceinline__ Operand operand(const WarpState& w, int code, const P
   return Operand{slots + (int64_t)code * a.slot_cap, w.slen[code]};
 }
 
+// The bound and exclusion masks of a program for K vertices name only v0..v_{K-2}
+// (prog_check), so the loops over matched vertices run over K - 1 entries.
+template <int K>
 __device__ __forceinline__ int bound_of(const WarpState& w, unsigned mask) {
   int b = INT_MAX;
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j)
+  for (int j = 0; j < K - 1; ++j)
     if ((mask >> j) & 1u) b = min(b, w.v[j]);
   return b;
 }
 
+template <int K>
 struct Excl {
-  int e[kProgMaxK];
+  int e[K - 1];
   __device__ __forceinline__ bool hit(int x) const {
     bool h = false;
 #pragma unroll
-    for (int j = 0; j < kProgMaxK; ++j) h |= x == e[j];
+    for (int j = 0; j < K - 1; ++j) h |= x == e[j];
     return h;
   }
 };
 
-__device__ __forceinline__ Excl excl_of(const WarpState& w, unsigned mask) {
-  Excl r;
+template <int K>
+__device__ __forceinline__ Excl<K> excl_of(const WarpState& w, unsigned mask) {
+  Excl<K> r;
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j) r.e[j] = ((mask >> j) & 1u) ? w.v[j] : -1;
+  for (int j = 0; j < K - 1; ++j) r.e[j] = ((mask >> j) & 1u) ? w.v[j] : -1;
   return r;
 }
 
@@ -180,11 +185,12 @@ __device__ __forceinline__ void set_vertex(WarpState& w, int j, int x, const Pro
 }
 
 // out slot <- op(a, b); warp-wide.
+template <int K>
 __device__ void run_op(const ProgOp& o, WarpState& w, const ProgArgs& a, int32_t* slots, int lane) {
   const Operand A = operand(w, o.a, a, slots);
   const Operand B = o.kind == OP_FILTER ? Operand{nullptr, 0} : operand(w, o.b, a, slots);
-  const int bnd = bound_of(w, o.bound);
-  const Excl ex = excl_of(w, o.excl);
+  const int bnd = bound_of<K>(w, o.bound);
+  const Excl<K> ex = excl_of<K>(w, o.excl);
   int32_t* out = slots + (int64_t)o.out * a.slot_cap;
   int written = 0;
   for (int base = 0; base < A.n; base += 32) {
@@ -204,12 +210,13 @@ __device__ void run_op(const ProgOp& o, WarpState& w, const ProgArgs& a, int32_t
 }
 
 // |op(a, b)| for the counted vertex; per-lane partial.
+template <int K>
 __device__ unsigned long long count_op(const ProgOp& o, const WarpState& w, const ProgArgs& a,
                                        const int32_t* slots, int lane) {
   const Operand A = operand(w, o.a, a, slots);
   const Operand B = o.kind == OP_FILTER ? Operand{nullptr, 0} : operand(w, o.b, a, slots);
-  const int bnd = bound_of(w, o.bound);
-  const Excl ex = excl_of(w, o.excl);
+  const int bnd = bound_of<K>(w, o.bound);
+  const Excl<K> ex = excl_of<K>(w, o.excl);
   unsigned long long c = 0;
   for (int base = 0; base < A.n; base += 32) {
     const int i = base + lane;
@@ -243,8 +250,9 @@ __device__ __forceinline__ int lower_index(const int32_t* A, int n, int x) {
 // next to A: each y in N(u) is searched in A instead of each x of A in N(u).  The
 // difference count is the number of A's elements that pass the bound and the
 // exclusions, minus the intersection.
+template <int K>
 __device__ unsigned long long count_short(const Operand& A, int u, long long rb, int du, int sbnd,
-                                          bool ubnd, const Excl& ex, bool uex, bool want,
+                                          bool ubnd, const Excl<K>& ex, bool uex, bool want,
                                           const int32_t* col) {
   const int bnd = ubnd ? min(sbnd, u) : sbnd;
   const int m = lower_index(A.p, A.n, bnd);
@@ -258,7 +266,7 @@ __device__ unsigned long long count_short(const Operand& A, int u, long long rb,
   if (want) return inter;
   long long pass = m;
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j) {
+  for (int j = 0; j < K - 1; ++j) {
     bool dup = false;
 #pragma unroll
     for (int i = 0; i < j; ++i) dup |= ex.e[i] == ex.e[j];
@@ -272,14 +280,15 @@ __device__ unsigned long long count_short(const Operand& A, int u, long long rb,
 // one item per (candidate u, element x of the counted operand).  When the second
 // operand is N(u) and A is long, candidates with short lists are counted one per lane
 // by count_short, and only the others (gathered into `big`) take the item walk.
+template <int K>
 __device__ unsigned long long count_flat(const ProgOp& o, const WarpState& w, int iv, Operand C,
                                          int lo, int hi, const ProgArgs& a, const int32_t* slots,
                                          int32_t* big, int lane) {
   const Operand A = operand(w, o.a, a, slots);
   const unsigned ivbit = 1u << iv;
-  const int sbnd = bound_of(w, o.bound & ~ivbit);
+  const int sbnd = bound_of<K>(w, o.bound & ~ivbit);
   const bool ubnd = (o.bound & ivbit) != 0;
-  const Excl ex = excl_of(w, o.excl & ~ivbit);
+  const Excl<K> ex = excl_of<K>(w, o.excl & ~ivbit);
   const bool uex = (o.excl & ivbit) != 0;
   const bool filter = o.kind == OP_FILTER;
   const bool b_u = !filter && o.b == kOpList + iv;
@@ -297,7 +306,7 @@ __device__ unsigned long long count_flat(const ProgOp& o, const WarpState& w, in
       const long long rb = in ? a.rowptr[u] : 0;
       const int du = in ? (int)(a.rowptr[u + 1] - rb) : 0;
       const bool small = in && 4 * du <= A.n;
-      if (small) c += count_short(A, u, rb, du, sbnd, ubnd, ex, uex, want, a.col);
+      if (small) c += count_short<K>(A, u, rb, du, sbnd, ubnd, ex, uex, want, a.col);
       const unsigned mb = __ballot_sync(0xffffffffu, in && !small);
       if (in && !small) big[nbig + __popc(mb & lanemask_lt())] = u;
       nbig += __popc(mb);
@@ -364,8 +373,8 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
   int32_t* big = slots + (int64_t)a.nslots * a.slot_cap;  // count_flat's long-list candidates
   set_vertex(w, 0, v0, a, lane);
   set_vertex(w, 1, v1, a, lane);
-  for (int i = 0; i < p.nops[0]; ++i) run_op(p.ops[0][i], w, a, slots, lane);
-  if constexpr (K == 3) return count_op(p.fin, w, a, slots, lane);
+  for (int i = 0; i < p.nops[0]; ++i) run_op<K>(p.ops[0][i], w, a, slots, lane);
+  if constexpr (K == 3) return count_op<K>(p.fin, w, a, slots, lane);
   const Operand C2 = operand(w, p.cand[2], a, slots);
   if (hi < 0 || hi > C2.n) hi = C2.n;
   if (may_split && C2.n > 1) {
@@ -402,25 +411,25 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
   }
   unsigned long long c = 0;
   if constexpr (K == 4) {
-    if (p.flat) return count_flat(p.fin, w, 2, C2, lo, hi, a, slots, big, lane);
+    if (p.flat) return count_flat<K>(p.fin, w, 2, C2, lo, hi, a, slots, big, lane);
     for (int i2 = lo; i2 < hi; ++i2) {
       set_vertex(w, 2, C2.p[i2], a, lane);
-      for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
-      c += count_op(p.fin, w, a, slots, lane);
+      for (int i = 0; i < p.nops[1]; ++i) run_op<K>(p.ops[1][i], w, a, slots, lane);
+      c += count_op<K>(p.fin, w, a, slots, lane);
     }
     return c;
   } else if constexpr (K == 5) {
     for (int i2 = lo; i2 < hi; ++i2) {
       set_vertex(w, 2, C2.p[i2], a, lane);
-      for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
+      for (int i = 0; i < p.nops[1]; ++i) run_op<K>(p.ops[1][i], w, a, slots, lane);
       const Operand C3 = operand(w, p.cand[3], a, slots);
       if (p.flat) {
-        c += count_flat(p.fin, w, 3, C3, 0, C3.n, a, slots, big, lane);
+        c += count_flat<K>(p.fin, w, 3, C3, 0, C3.n, a, slots, big, lane);
       } else {
         for (int i3 = 0; i3 < C3.n; ++i3) {
           set_vertex(w, 3, C3.p[i3], a, lane);
-          for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
-          c += count_op(p.fin, w, a, slots, lane);
+          for (int i = 0; i < p.nops[2]; ++i) run_op<K>(p.ops[2][i], w, a, slots, lane);
+          c += count_op<K>(p.fin, w, a, slots, lane);
         }
       }
     }
@@ -428,19 +437,19 @@ __device__ unsigned long long run_task(const Prog& p, unsigned roots, WarpState&
   } else {  // 6 vertices: one more enumerated level (v3), then as 5 vertices with v4
     for (int i2 = lo; i2 < hi; ++i2) {
       set_vertex(w, 2, C2.p[i2], a, lane);
-      for (int i = 0; i < p.nops[1]; ++i) run_op(p.ops[1][i], w, a, slots, lane);
+      for (int i = 0; i < p.nops[1]; ++i) run_op<K>(p.ops[1][i], w, a, slots, lane);
       const Operand C3 = operand(w, p.cand[3], a, slots);
       for (int i3 = 0; i3 < C3.n; ++i3) {
         set_vertex(w, 3, C3.p[i3], a, lane);
-        for (int i = 0; i < p.nops[2]; ++i) run_op(p.ops[2][i], w, a, slots, lane);
+        for (int i = 0; i < p.nops[2]; ++i) run_op<K>(p.ops[2][i], w, a, slots, lane);
         const Operand C4 = operand(w, p.cand[4], a, slots);
         if (p.flat) {
-          c += count_flat(p.fin, w, 4, C4, 0, C4.n, a, slots, big, lane);
+          c += count_flat<K>(p.fin, w, 4, C4, 0, C4.n, a, slots, big, lane);
         } else {
           for (int i4 = 0; i4 < C4.n; ++i4) {
             set_vertex(w, 4, C4.p[i4], a, lane);
-            for (int i = 0; i < p.nops[3]; ++i) run_op(p.ops[3][i], w, a, slots, lane);
-            c += count_op(p.fin, w, a, slots, lane);
+            for (int i = 0; i < p.nops[3]; ++i) run_op<K>(p.ops[3][i], w, a, slots, lane);
+            c += count_op<K>(p.fin, w, a, slots, lane);
           }
         }
       }
@@ -492,16 +501,17 @@ __device__ __forceinline__ uint32_t bits_row(const WarpState& w, const BitsCtx& 
   return w.rowbuf[lane];
 }
 
+template <int K>
 __device__ __forceinline__ uint32_t bits_keep(const WarpState& w, const BitsCtx& B, const ProgOp& o,
                                               int lane) {
   int pb = INT_MAX;
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j)
+  for (int j = 0; j < K - 1; ++j)
     if ((o.bound >> j) & 1u) pb = min(pb, w.pre[j]);
   const int lo = 32 * lane;
   uint32_t m = pb >= lo + 32 ? 0xffffffffu : (pb <= lo ? 0u : ((1u << (pb - lo)) - 1u));
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j)
+  for (int j = 0; j < K - 1; ++j)
     if (((o.excl >> j) & 1u) && w.idx[j] >= lo && w.idx[j] < lo + 32) m &= ~(1u << (w.idx[j] - lo));
   return m & B.valid;
 }
@@ -513,18 +523,20 @@ __device__ __forceinline__ uint32_t bits_operand(const WarpState& w, const BitsC
   return w.bits[code][lane];
 }
 
+template <int K>
 __device__ __forceinline__ uint32_t bits_apply(const WarpState& w, const BitsCtx& B, const ProgOp& o,
                                                uint32_t A, int lane) {
   if (o.kind == OP_INTERSECT) A &= bits_row(w, B, o.b, lane);
   else if (o.kind == OP_DIFFERENCE) A &= ~bits_row(w, B, o.b, lane);
-  return A & bits_keep(w, B, o, lane);
+  return A & bits_keep<K>(w, B, o, lane);
 }
 
+template <int K>
 __device__ __forceinline__ void bits_level(const Prog& p, int l, WarpState& w, const BitsCtx& B,
                                            int lane) {
   for (int i = 0; i < p.nops[l]; ++i) {
     const ProgOp& o = p.ops[l][i];
-    w.bits[o.out][lane] = bits_apply(w, B, o, bits_operand(w, B, o.a, lane), lane);
+    w.bits[o.out][lane] = bits_apply<K>(w, B, o, bits_operand(w, B, o.a, lane), lane);
   }
 }
 
@@ -544,6 +556,7 @@ __device__ __forceinline__ void bits_set(WarpState& w, int j, int x, int i, int 
 // is not v3's) is folded into fk[] once; per v3 and word that leaves one AND (with v3's
 // row) and a popc, plus v3's own bound / exclusion in its word.  For the programs whose
 // last level is the count alone.
+template <int K>
 __device__ unsigned long long bits_flat_fin(const Prog& p, WarpState& w, const BitsCtx& B,
                                             uint32_t c3w, int32_t* list, int lane) {
   const ProgOp& o = p.fin;
@@ -555,7 +568,7 @@ __device__ unsigned long long bits_flat_fin(const Prog& p, WarpState& w, const B
     o2.bound &= 0x7u;
     o2.excl &= 0x7u;
     if (per_v3) o2.kind = OP_FILTER;
-    w.fk[lane] = bits_apply(w, B, o2, bits_operand(w, B, o.a, lane), lane);
+    w.fk[lane] = bits_apply<K>(w, B, o2, bits_operand(w, B, o.a, lane), lane);
   }
   const int cnt = __popc(c3w);
   int incl = cnt;
@@ -594,18 +607,18 @@ __device__ unsigned long long bits_flat_fin(const Prog& p, WarpState& w, const B
 template <int K>
 __device__ unsigned long long bits_step2(const Prog& p, WarpState& w, const BitsCtx& B,
                                          int32_t* list, int lane) {
-  bits_level(p, 1, w, B, lane);
-  if (K == 4) return (unsigned long long)__popc(bits_apply(w, B, p.fin, bits_operand(w, B, p.fin.a, lane), lane));
+  bits_level<K>(p, 1, w, B, lane);
+  if (K == 4) return (unsigned long long)__popc(bits_apply<K>(w, B, p.fin, bits_operand(w, B, p.fin.a, lane), lane));
   __syncwarp();  // the level-1 slots are read across lanes below
   const uint32_t c3 = bits_operand(w, B, p.cand[3], lane);
-  if (p.nops[2] == 0) return bits_flat_fin(p, w, B, c3, list, lane);
+  if (p.nops[2] == 0) return bits_flat_fin<K>(p, w, B, c3, list, lane);
   unsigned long long c = 0;
   for (int wi = 0; wi < B.W; ++wi) {
     for (uint32_t m = __shfl_sync(0xffffffffu, c3, wi); m; m &= m - 1) {
       const int b = wi * 32 + __ffs(m) - 1;
       bits_set(w, 3, B.n0[b], b, b, lane);
-      bits_level(p, 2, w, B, lane);
-      c += __popc(bits_apply(w, B, p.fin, bits_operand(w, B, p.fin.a, lane), lane));
+      bits_level<K>(p, 2, w, B, lane);
+      c += __popc(bits_apply<K>(w, B, p.fin, bits_operand(w, B, p.fin.a, lane), lane));
     }
   }
   return c;
@@ -637,8 +650,8 @@ __device__ unsigned long long run_task_bits(const Prog& p, WarpState& w, const P
   __syncwarp();
   for (int i = 0; i < p.nops[0]; ++i) {
     const ProgOp& o = p.ops[0][i];
-    if (i == a.lut_stream) run_op(o, w, a, slots, lane);  // the v2 list N(v1) \ N(v0)
-    else w.bits[o.out][lane] = bits_apply(w, B, o, bits_operand(w, B, o.a, lane), lane);
+    if (i == a.lut_stream) run_op<K>(o, w, a, slots, lane);  // the v2 list N(v1) \ N(v0)
+    else w.bits[o.out][lane] = bits_apply<K>(w, B, o, bits_operand(w, B, o.a, lane), lane);
   }
   __syncwarp();
   const bool stream = a.lut_stream >= 0;
@@ -899,20 +912,22 @@ struct LutLane {
   uint32_t row[kProgMaxK];
 };
 
+template <int K>
 __device__ __forceinline__ uint32_t row_of_code(const LutLane& L, int code) {
   uint32_t r = 0;
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j)
+  for (int j = 0; j < K - 1; ++j)
     if (code == kOpList + j) r = L.row[j];
   return r;
 }
 
 // prefix mask of the bound (x < min v_j) and the exclusion mask, over matched vertices
+template <int K>
 __device__ __forceinline__ uint32_t keep_mask(const LutLane& L, const ProgOp& o, uint32_t valid) {
   int pb = 32;
   uint32_t ex = 0;
 #pragma unroll
-  for (int j = 0; j < kProgMaxK; ++j) {
+  for (int j = 0; j < K - 1; ++j) {
     if ((o.bound >> j) & 1u) pb = min(pb, L.pre[j]);
     if (((o.excl >> j) & 1u) && L.idx[j] >= 0) ex |= 1u << L.idx[j];
   }
@@ -920,12 +935,13 @@ __device__ __forceinline__ uint32_t keep_mask(const LutLane& L, const ProgOp& o,
   return valid & pm & ~ex;
 }
 
+template <int K>
 __device__ __forceinline__ uint32_t lut_apply(const LutLane& L, const ProgOp& o, uint32_t A,
                                               uint32_t valid) {
   uint32_t r = A;
-  if (o.kind == OP_INTERSECT) r &= row_of_code(L, o.b);
-  else if (o.kind == OP_DIFFERENCE) r &= ~row_of_code(L, o.b);
-  return r & keep_mask(L, o, valid);
+  if (o.kind == OP_INTERSECT) r &= row_of_code<K>(L, o.b);
+  else if (o.kind == OP_DIFFERENCE) r &= ~row_of_code<K>(L, o.b);
+  return r & keep_mask<K>(L, o, valid);
 }
 
 __device__ __forceinline__ uint32_t lut_operand(const LutLane& L, int code, const uint32_t* sl,
@@ -946,9 +962,9 @@ __device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, uint32
                                         uint32_t valid) {
   for (int i = 0; i < p.nops[l]; ++i) {
     const ProgOp& o = p.ops[l][i];
-    sl[o.out * 32] = lut_apply(L, o, lut_operand(L, o.a, sl, valid), valid);
+    sl[o.out * 32] = lut_apply<K>(L, o, lut_operand(L, o.a, sl, valid), valid);
   }
-  if (l == K - 3) return (unsigned long long)__popc(lut_apply(L, p.fin, lut_operand(L, p.fin.a, sl, valid), valid));
+  if (l == K - 3) return (unsigned long long)__popc(lut_apply<K>(L, p.fin, lut_operand(L, p.fin.a, sl, valid), valid));
   return 0;
 }
 
@@ -976,7 +992,7 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
   for (int i = 0; i < p.nops[0]; ++i) {
     if (i == a.lut_stream) continue;
     const ProgOp& o = p.ops[0][i];
-    sl[o.out * 32] = lut_apply(L, o, lut_operand(L, o.a, sl, valid), valid);
+    sl[o.out * 32] = lut_apply<K>(L, o, lut_operand(L, o.a, sl, valid), valid);
   }
   unsigned long long c = 0;
   // the count when the last level is the count alone: everything that does not depend
@@ -999,7 +1015,7 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
       o2.bound &= 0x7u;
       o2.excl &= 0x7u;
       if (f_v3) o2.kind = OP_FILTER;
-      const uint32_t fk = lut_apply(L, o2, lut_operand(L, fo.a, sl, valid), valid);
+      const uint32_t fk = lut_apply<K>(L, o2, lut_operand(L, fo.a, sl, valid), valid);
       for (uint32_t m = c3; m; m &= m - 1) {
         const int b = __ffs(m) - 1;
         uint32_t x = fk;
@@ -1060,7 +1076,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
   __shared__ Prog p;
   __shared__ int32_t n0s[kWarps][32];
   __shared__ uint32_t luts[kWarps][32];
-  __shared__ uint32_t sls[kWarps][kProgMaxSlots * 32];
+  __shared__ uint32_t sls[kWarps][kLutSlots * 32];
   __shared__ int32_t hkeys[kWarps][kMapSlots];
   __shared__ uint32_t hvals[kWarps][kMapSlots];
   if (threadIdx.x == 0) p = prog;

@@ -68,7 +68,9 @@ bool prog_check(const Prog& p, std::string* why);
 // Bitmap (LUT) form: whether the program runs in the index space of N(v0) — every
 // operand read after level 0, the v3 candidates and the counted operand descend from
 // N(v0); the v2 candidates may instead be the stream N(v1) \ N(v0) (one level-0
-// difference, `stream`), whose vertices get their rows built on the fly.
+// difference, `stream`), whose vertices get their rows built on the fly.  The bitmap
+// kernels hold kLutSlots slots per task (4- and 5-vertex programs use at most 5).
+constexpr int kLutSlots = 8;
 struct ProgLut {
   int8_t ok = 0;
   int8_t stream = -1;  // index of the level-0 operation giving cand[2] from N(v1), or -1
