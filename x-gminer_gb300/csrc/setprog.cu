@@ -944,11 +944,24 @@ __device__ __forceinline__ uint32_t lut_apply(const LutLane& L, const ProgOp& o,
   return r & keep_mask<K>(L, o, valid);
 }
 
-__device__ __forceinline__ uint32_t lut_operand(const LutLane& L, int code, const uint32_t* sl,
+// Slot columns of a bitmap task (stride 32 words): the slots of level 0 are read from
+// the column of the lane that ran the task's level-0 operations (`head`), the slots of
+// the later levels live in the running lane's own column.  A slot is defined once, so
+// the two sets of indices are disjoint.
+struct LutSlots {
+  uint32_t* own;
+  const uint32_t* head;
+  unsigned l0;  // slots defined at level 0
+  __device__ __forceinline__ uint32_t get(int code) const {
+    return ((l0 >> code) & 1u) ? head[code * 32] : own[code * 32];
+  }
+};
+
+__device__ __forceinline__ uint32_t lut_operand(const LutLane& L, int code, const LutSlots& S,
                                                 uint32_t valid) {
   if (code == kOpList) return valid;               // N(v0)
   if (code == kOpList + 1) return L.row[1];        // N(v1) n N(v0), the only use of N(v1)
-  return sl[code * 32];
+  return S.get(code);
 }
 
 __device__ __forceinline__ void lut_set(LutLane& L, int j, int x, int i, const int32_t* n0, int d0) {
@@ -958,14 +971,56 @@ __device__ __forceinline__ void lut_set(LutLane& L, int j, int x, int i, const i
 }
 
 template <int K>
-__device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, uint32_t* sl,
+__device__ unsigned long long lut_level(const Prog& p, int l, LutLane& L, const LutSlots& S,
                                         uint32_t valid) {
   for (int i = 0; i < p.nops[l]; ++i) {
     const ProgOp& o = p.ops[l][i];
-    sl[o.out * 32] = lut_apply<K>(L, o, lut_operand(L, o.a, sl, valid), valid);
+    S.own[o.out * 32] = lut_apply<K>(L, o, lut_operand(L, o.a, S, valid), valid);
   }
-  if (l == K - 3) return (unsigned long long)__popc(lut_apply<K>(L, p.fin, lut_operand(L, p.fin.a, sl, valid), valid));
+  if (l == K - 3) return (unsigned long long)__popc(lut_apply<K>(L, p.fin, lut_operand(L, p.fin.a, S, valid), valid));
   return 0;
+}
+
+// v0, v1, v2 matched (and the level-0 slots written): the level-1 operations, then the
+// count (4 vertices) or the v3 loop (5 vertices).  When the last level is the count
+// alone, everything that does not depend on v3 (operand, valid range, bounds /
+// exclusions of v0..v2, a row that is not v3's) is folded once per v2, then per v3 its
+// own bound, exclusion and row, and a popc.
+template <int K>
+__device__ unsigned long long lut_step2(const Prog& p, LutLane& L, const LutSlots& S,
+                                        uint32_t valid, const int32_t* n0, int d0,
+                                        const uint32_t* lut) {
+  if (K == 4) return lut_level<K>(p, 1, L, S, valid);
+  lut_level<K>(p, 1, L, S, valid);
+  const uint32_t c3 = lut_operand(L, p.cand[3], S, valid);
+  const ProgOp& fo = p.fin;
+  unsigned long long c = 0;
+  if (K == 5 && p.nops[2] == 0) {
+    const bool f_ub = (fo.bound >> 3) & 1u, f_ux = (fo.excl >> 3) & 1u;
+    const bool f_v3 = fo.kind != OP_FILTER && fo.b == kOpList + 3;
+    const bool f_is = fo.kind == OP_INTERSECT;
+    ProgOp o2 = fo;
+    o2.bound &= 0x7u;
+    o2.excl &= 0x7u;
+    if (f_v3) o2.kind = OP_FILTER;
+    const uint32_t fk = lut_apply<K>(L, o2, lut_operand(L, fo.a, S, valid), valid);
+    for (uint32_t m = c3; m; m &= m - 1) {
+      const int b = __ffs(m) - 1;
+      uint32_t x = fk;
+      if (f_ub) x &= (1u << b) - 1u;
+      if (f_ux) x &= ~(1u << b);
+      if (f_v3) x = f_is ? (x & lut[b]) : (x & ~lut[b]);
+      c += (unsigned long long)__popc(x);
+    }
+    return c;
+  }
+  for (uint32_t m = c3; m; m &= m - 1) {
+    const int b = __ffs(m) - 1;
+    lut_set(L, 3, n0[b], b, n0, d0);
+    L.row[3] = lut[b];
+    c += lut_level<K>(p, 2, L, S, valid);
+  }
+  return c;
 }
 
 // One (v0, v1) task on masks; sl = this lane's slots (stride 32).  A stream program's
@@ -989,50 +1044,13 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
   L.row[0] = valid;
   lut_set(L, 1, v1, i1, n0, d0);
   L.row[1] = lut[i1];
+  const LutSlots S{sl, sl, 0u};
   for (int i = 0; i < p.nops[0]; ++i) {
     if (i == a.lut_stream) continue;
     const ProgOp& o = p.ops[0][i];
-    sl[o.out * 32] = lut_apply<K>(L, o, lut_operand(L, o.a, sl, valid), valid);
+    sl[o.out * 32] = lut_apply<K>(L, o, lut_operand(L, o.a, S, valid), valid);
   }
   unsigned long long c = 0;
-  // the count when the last level is the count alone: everything that does not depend
-  // on v3 (operand, valid range, bounds / exclusions of v0..v2, a row that is not v3's)
-  // folded once per v2, then per v3 its own bound, exclusion and row, and a popc
-  const ProgOp& fo = p.fin;
-  const bool flat5 = K == 5 && p.nops[2] == 0;
-  const bool f_ub = (fo.bound >> 3) & 1u, f_ux = (fo.excl >> 3) & 1u;
-  const bool f_v3 = fo.kind != OP_FILTER && fo.b == kOpList + 3;
-  const bool f_is = fo.kind == OP_INTERSECT;
-  auto step2 = [&]() {
-    if (K == 4) {
-      c += lut_level<K>(p, 1, L, sl, valid);
-      return;
-    }
-    lut_level<K>(p, 1, L, sl, valid);
-    const uint32_t c3 = lut_operand(L, p.cand[3], sl, valid);
-    if (flat5) {
-      ProgOp o2 = fo;
-      o2.bound &= 0x7u;
-      o2.excl &= 0x7u;
-      if (f_v3) o2.kind = OP_FILTER;
-      const uint32_t fk = lut_apply<K>(L, o2, lut_operand(L, fo.a, sl, valid), valid);
-      for (uint32_t m = c3; m; m &= m - 1) {
-        const int b = __ffs(m) - 1;
-        uint32_t x = fk;
-        if (f_ub) x &= (1u << b) - 1u;
-        if (f_ux) x &= ~(1u << b);
-        if (f_v3) x = f_is ? (x & lut[b]) : (x & ~lut[b]);
-        c += (unsigned long long)__popc(x);
-      }
-      return;
-    }
-    for (uint32_t m = c3; m; m &= m - 1) {
-      const int b = __ffs(m) - 1;
-      lut_set(L, 3, n0[b], b, n0, d0);
-      L.row[3] = lut[b];
-      c += lut_level<K>(p, 2, L, sl, valid);
-    }
-  };
   if (a.lut_stream >= 0) {
     // v2 over N(v1) \ N(v0), below the operation's bound, minus its exclusions
     const ProgOp& o = p.ops[0][a.lut_stream];
@@ -1049,16 +1067,100 @@ __device__ unsigned long long lut_task(const Prog& p, const ProgArgs& a, int v0,
       if ((((o.excl >> 0) & 1u) && y == v0) || (((o.excl >> 1) & 1u) && y == v1)) continue;
       lut_set(L, 2, y, -1, n0, d0);
       L.row[2] = hkey ? map_row(hkey, hval, y) : row_over(n0, d0, y, a);
-      step2();
+      c += lut_step2<K>(p, L, S, valid, n0, d0, lut);
     }
   } else {
-    for (uint32_t m = lut_operand(L, p.cand[2], sl, valid); m; m &= m - 1) {
+    for (uint32_t m = lut_operand(L, p.cand[2], S, valid); m; m &= m - 1) {
       const int b = __ffs(m) - 1;
       lut_set(L, 2, n0[b], b, n0, d0);
       L.row[2] = lut[b];
-      step2();
+      c += lut_step2<K>(p, L, S, valid, n0, d0, lut);
     }
   }
+  return c;
+}
+
+// Phase 0 of a stream program for one v0 (d0 <= 32), as a warp: lane i runs the
+// level-0 operations of task (v0, N(v0)[i]) when `mine` (d(v1) within the bitmap
+// range, v1 allowed); then the (task, v2) pairs of all those tasks (v2 over the part of
+// N(v1) below the stream's bound) are dealt out to the lanes in turn, so that a lane's
+// work no longer follows the length of its own task's stream.  A pair reads its task's
+// level-0 slots from the task's lane (`sw` = the warp's slot columns, written before
+// the call).  All lanes call this.
+template <int K>
+__device__ unsigned long long lut_stream_pairs(const Prog& p, const ProgArgs& a, int v0, int d0,
+                                               const int32_t* n0, const uint32_t* lut,
+                                               uint32_t* sw, unsigned l0, bool mine,
+                                               const int32_t* hkey, const uint32_t* hval,
+                                               int lane) {
+  const uint32_t valid = d0 >= 32 ? 0xffffffffu : ((1u << d0) - 1u);
+  const int pre0 = lower_index(n0, d0, v0);
+  const ProgOp& so = p.ops[0][a.lut_stream];
+  LutLane L;
+#pragma unroll
+  for (int j = 0; j < kProgMaxK; ++j) L.v[j] = -1, L.idx[j] = -1, L.pre[j] = 0, L.row[j] = 0;
+  L.v[0] = v0;
+  L.pre[0] = pre0;
+  L.row[0] = valid;
+  long long rb1 = 0;
+  int n = 0;
+  if (mine) {
+    const int v1 = n0[lane];
+    if (!(p.v1lt && v1 >= v0)) {
+      lut_set(L, 1, v1, lane, n0, d0);
+      L.row[1] = lut[lane];
+      const LutSlots S{sw + lane, sw + lane, 0u};
+      for (int i = 0; i < p.nops[0]; ++i) {
+        if (i == a.lut_stream) continue;
+        const ProgOp& o = p.ops[0][i];
+        sw[o.out * 32 + lane] = lut_apply<K>(L, o, lut_operand(L, o.a, S, valid), valid);
+      }
+      int ub = INT_MAX;
+      if (so.bound & 1u) ub = min(ub, v0);
+      if ((so.bound >> 1) & 1u) ub = min(ub, v1);
+      rb1 = a.rowptr[v1];
+      n = lower_index(a.col + rb1, (int)(a.rowptr[v1 + 1] - rb1), ub);
+    }
+  }
+  __syncwarp();  // the level-0 slots are read by other lanes below
+  int incl = n;
+#pragma unroll
+  for (int k = 1; k < 32; k <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, k);
+    if (lane >= k) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const bool ex0 = so.excl & 1u, ex1 = (so.excl >> 1) & 1u;
+  unsigned long long c = 0;
+  for (int base = 0; base < total; base += 32) {
+    const int item = base + lane;
+    // the task of this item: the first lane whose inclusive count passes it
+    int t = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      const int v = __shfl_sync(0xffffffffu, incl, t + s - 1);
+      if (v <= item) t += s;
+    }
+    const int first = __shfl_sync(0xffffffffu, incl - n, t);
+    const long long rbt = __shfl_sync(0xffffffffu, rb1, t);
+    if (item >= total) continue;
+    const int v1 = n0[t];
+    const int y = a.col[rbt + (item - first)];
+    const int i = lower_index(n0, d0, y);
+    if (i < d0 && n0[i] == y) continue;  // in N(v0): not a stream vertex
+    if ((ex0 && y == v0) || (ex1 && y == v1)) continue;
+    L.v[1] = v1;
+    L.idx[1] = t;
+    L.pre[1] = t;
+    L.row[1] = lut[t];
+    L.v[2] = y;
+    L.idx[2] = -1;
+    L.pre[2] = i;
+    L.row[2] = hkey ? map_row(hkey, hval, y) : row_over(n0, d0, y, a);
+    const LutSlots S{sw + lane, sw + t, l0};
+    c += lut_step2<K>(p, L, S, valid, n0, d0, lut);
+  }
+  __syncwarp();
   return c;
 }
 
@@ -1083,6 +1185,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
   __syncthreads();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   SplitRec* srec = a.split + a.split_cap;  // stream records
+  unsigned l0 = 0;  // slots written by the level-0 operations
+  for (int i = 0; i < p.nops[0]; ++i)
+    if (i != a.lut_stream) l0 |= 1u << p.ops[0][i].out;
   int32_t* hk = hkeys[wib];
   uint32_t* hv = hvals[wib];
   unsigned long long c = 0;
@@ -1097,16 +1202,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_setlut(Prog prog, ProgArgs a) {
       if (d0 == 0 || d0 > kLutDeg) continue;
       lut_load(n0s[wib], luts[wib], rb, d0, a, lane);
       const bool mapped = a.lut_stream >= 0 && map_build(hk, hv, n0s[wib], d0, a, lane);
-      // one lane per task; stream tasks with a long N(v1) become stream records
+      // one lane per task (stream programs: one lane per (task, v2) pair); stream tasks
+      // with a long N(v1) become stream records
       int d1 = 0;
       if (lane < d0) {
         const int v1 = n0s[wib][lane];
         d1 = (int)(a.rowptr[v1 + 1] - a.rowptr[v1]);
-        if (a.lut_stream < 0 || d1 <= kLutStream)
+        if (a.lut_stream < 0)
           c += lut_task<K>(p, a, (int)v0, lane, d0, n0s[wib], luts[wib], &sls[wib][lane], 0, 1,
-                           0, 1 << 30, mapped ? hk : nullptr, hv);
+                           0, 1 << 30, nullptr, hv);
       }
       __syncwarp();
+      if (a.lut_stream >= 0)
+        c += lut_stream_pairs<K>(p, a, (int)v0, d0, n0s[wib], luts[wib], sls[wib], l0,
+                                 lane < d0 && d1 <= kLutStream, mapped ? hk : nullptr, hv, lane);
       if (a.lut_stream >= 0) {
         const bool lng = lane < d0 && d1 > kLutStream;
         const int nrec = lng ? (d1 + kStreamChunk - 1) / kStreamChunk : 0;
