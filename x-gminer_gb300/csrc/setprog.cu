@@ -690,10 +690,22 @@ __device__ unsigned long long run_task_bits(const Prog& p, WarpState& w, const P
       bits_set(w, 2, y, -1, lower_index(B.n0, B.d0, y), lane);
       if (lane < 32) w.rowbuf[lane] = 0u;
       __syncwarp();
-      for (int t = lane; t < w.vl[2]; t += 32) {
-        const int z = a.col[w.vb[2] + t];
-        const int k = lower_index(B.n0, B.d0, z);
-        if (k < B.d0 && B.n0[k] == z) atomicOr(&w.rowbuf[k >> 5], 1u << (k & 31));
+      const int dy = w.vl[2];
+      if (dy > B.d0) {
+        // N(y) the longer list: each lane tests entries of N(v0) against N(y), and a
+        // ballot gives each word of the row
+        const int32_t* ny = a.col + w.vb[2];
+        for (int base = 0; base < B.d0; base += 32) {
+          const int i = base + lane;
+          const unsigned word = __ballot_sync(0xffffffffu, i < B.d0 && member(ny, dy, B.n0[i]));
+          if (lane == 0) w.rowbuf[base >> 5] = word;
+        }
+      } else {
+        for (int t = lane; t < dy; t += 32) {
+          const int z = a.col[w.vb[2] + t];
+          const int k = lower_index(B.n0, B.d0, z);
+          if (k < B.d0 && B.n0[k] == z) atomicOr(&w.rowbuf[k >> 5], 1u << (k & 31));
+        }
       }
       __syncwarp();
       c += bits_step2<K>(p, w, B, list, lane);
