@@ -685,16 +685,26 @@ __device__ unsigned long long run_task_bits(const Prog& p, WarpState& w, const P
   unsigned long long c = 0;
   if (stream) {
     for (int i2 = lo; i2 < hi; ++i2) {
+      // y's list bounds and its rank in N(v0) into registers (independent loads that
+      // overlap), then into the warp state once every lane is done with the last v2
       const int y = C2.p[i2];
-      set_vertex(w, 2, y, a, lane);
-      bits_set(w, 2, y, -1, lower_index(B.n0, B.d0, y), lane);
-      if (lane < 32) w.rowbuf[lane] = 0u;
+      const long long rby = a.rowptr[y];
+      const int dy = (int)(a.rowptr[y + 1] - rby);
+      const int pre = lower_index(B.n0, B.d0, y);
       __syncwarp();
-      const int dy = w.vl[2];
+      if (lane == 0) {
+        w.v[2] = y;
+        w.vb[2] = rby;
+        w.vl[2] = dy;
+        w.idx[2] = -1;
+        w.pre[2] = pre;
+      }
+      w.rowbuf[lane] = 0u;
+      __syncwarp();
       if (dy > B.d0) {
         // N(y) the longer list: each lane tests entries of N(v0) against N(y), and a
         // ballot gives each word of the row
-        const int32_t* ny = a.col + w.vb[2];
+        const int32_t* ny = a.col + rby;
         for (int base = 0; base < B.d0; base += 32) {
           const int i = base + lane;
           const unsigned word = __ballot_sync(0xffffffffu, i < B.d0 && member(ny, dy, B.n0[i]));
@@ -702,7 +712,7 @@ __device__ unsigned long long run_task_bits(const Prog& p, WarpState& w, const P
         }
       } else {
         for (int t = lane; t < dy; t += 32) {
-          const int z = a.col[w.vb[2] + t];
+          const int z = a.col[rby + t];
           const int k = lower_index(B.n0, B.d0, z);
           if (k < B.d0 && B.n0[k] == z) atomicOr(&w.rowbuf[k >> 5], 1u << (k & 31));
         }
