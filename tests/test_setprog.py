@@ -169,6 +169,19 @@ def test_compiled_six_vertex_programs(xgm, orc):
                 (a.tolist(), induced)
 
 
+def test_program_slots_fit_bitmap_forms(xgm):
+    # the bitmap kernels hold 8 slots per task (kLutSlots); a 4- or 5-vertex program
+    # above that would run in the list form only.  Every GLUMIN plan and every compiled
+    # 4- and 5-vertex program stays within it; 6-vertex programs fit the 16 of the format
+    for pid in range(6, 23):
+        assert xgm.plan(f"P{pid}").program[2] <= 8, pid
+    for k, cap in ((4, 8), (5, 8), (6, 16)):
+        for a in _connected_patterns(k):
+            for induced in (True, False):
+                assert xgm.plan(a, induced=induced, program=True).program[2] <= cap, \
+                    (a.tolist(), induced)
+
+
 def test_program_plan_api(xgm):
     # 5-vertex non-clique patterns compile without asking; the 5-clique stays a builtin
     bull = _adj([(0, 1), (0, 2), (0, 4), (1, 2), (1, 3)])
