@@ -392,6 +392,8 @@ def batch_arm(args, dist: Dist) -> None:
     if model is not None:
         runs["learned"] = {"policy": xgm.SCHED_LEARNED, "model": model, **mkw}
     res, ref, kernels = {}, None, {}
+    clocks = ClockSampler(dist.local)
+    clocks.start()
     for name, kw in runs.items():
         for _ in range(args.warmup):
             ctx.count_batched(b, BATCH_PATTERNS, **kw)
@@ -405,6 +407,7 @@ def batch_arm(args, dist: Dist) -> None:
             ref = out
         assert np.array_equal(out, ref), f"{name} schedule changed a count"
         res[name] = statistics.mean(ms)
+    clk = clocks.stop()
     total = float(ref.astype(np.float64).sum())
     best = min(res, key=res.get)
     # per-graph calls on a sample of graphs, scaled to the whole batch
@@ -434,7 +437,8 @@ def batch_arm(args, dist: Dist) -> None:
             "schedules_ms": res, "tuned_variants": tune["variants"],
             "per_graph_calls_ms_estimate": loop_ms_full,
             "speedup_vs_per_graph_calls": loop_ms_full / res[best],
-            "count_total": int(total), "gpu_launches": kernels[best] * args.steps}
+            "count_total": int(total), "gpu_launches": kernels[best] * args.steps,
+            "clocks": clk}
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -497,7 +501,9 @@ def motifs_arm(args, dist: Dist) -> None:
               "chung_lu": xgm.gen_chung_lu(n, 2.1, 50000.0, 32.0, seed=32)}
     model, mkw = load_model(xgm, ctx) if args.policy == "learned" else (None, {})
     kw = {"policy": xgm.SCHED_LEARNED, "model": model, **mkw} if model is not None else {}
-    per, total_ms, total_matches, info = {}, 0.0, 0, {}
+    per, total_ms, total_matches, info, launches = {}, 0.0, 0, {}, 0
+    clocks = ClockSampler(dist.local)
+    clocks.start()
     for gname, (nv, src, dst) in graphs.items():
         g = ctx.graph_from_edges(nv, src, dst)
         info[gname] = g.info()
@@ -509,10 +515,12 @@ def motifs_arm(args, dist: Dist) -> None:
             for _ in range(args.steps):
                 cnt, st = ctx.count(g, pat, with_stats=True, **kw)
                 ms.append(st["kernel_ms"] + st["prep_ms"])
+                launches += st["launches"]
             per[f"{gname}/{pat}"] = {"count": cnt, "ms": statistics.mean(ms)}
             total_ms += statistics.mean(ms)
             total_matches += cnt
         g.close()
+    clk = clocks.stop()
     line = {"metric": "matches_per_sec", "value": total_matches / (total_ms / 1e3),
             "unit": "matches/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
@@ -522,7 +530,7 @@ def motifs_arm(args, dist: Dist) -> None:
                                    "Chung-Lu 2^21 gamma 2.1 dmax 50k",
                        "schedule": "learned" if model is not None else "heuristic",
                        "graphs": info},
-            "per_pattern": per}
+            "gpu_launches": launches // max(1, args.steps), "clocks": clk, "per_pattern": per}
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -541,6 +549,8 @@ def patterns5_arm(args, dist: Dist) -> None:
     graphs = {"rmat_s12_ef8": xgm.gen_rmat(12, 8, seed=3),
               "er_2^16_deg16": xgm.gen_er(1 << 16, 1 << 19, seed=3)}
     per, total_ms, total_matches, info, launches = {}, 0.0, 0, {}, 0
+    clocks = ClockSampler(dist.local)
+    clocks.start()
     for gname, (nv, src, dst) in graphs.items():
         g = ctx.graph_from_edges(nv, src, dst)
         info[gname] = g.info()
@@ -558,6 +568,7 @@ def patterns5_arm(args, dist: Dist) -> None:
             total_ms += statistics.mean(ms)
             total_matches += cnt
         g.close()
+    clk = clocks.stop()
     line = {"metric": "matches_per_sec", "value": total_matches / (total_ms / 1e3),
             "unit": "matches/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
@@ -565,7 +576,8 @@ def patterns5_arm(args, dist: Dist) -> None:
             "data": "synthetic (seeded R-MAT and Erdos-Renyi)",
             "config": {"workload": "GLUMIN P6-P22 (vertex-induced 5-vertex plans), R-MAT s12 "
                                    "ef8 and ER 2^16 deg 16", "graphs": info},
-            "gpu_launches": launches // max(1, args.steps), "per_pattern": per}
+            "gpu_launches": launches // max(1, args.steps), "clocks": clk,
+            "per_pattern": per}
     if dist.rank == 0 and not args.no_cpu_baseline:
         import oracle
 
