@@ -10,17 +10,29 @@ A step is one exact count of the pattern (default 4-clique) over the whole graph
 the engine: task generation (schedule) + the persistent counting launch, graph resident
 in HBM.  `value` is matches/s from CUDA-event device time; `e2e` is the same metric
 through the C ABI from host CSR buffers (pinned), host->device copy, GPU orientation,
-count and the 8-byte result read inside the timed region.
+count and the 8-byte result read inside the timed region.  Every count is checked
+against the reference binaries' count of the same graph (tests/golden/config_counts.json)
+where the fixture holds it.
+
+The default line also carries `clique5` (the 5-clique half of the configuration, learned
+vs plain heuristic schedule on the same resident graph) and `batch` (4096 Barabasi-Albert
+graphs, triangle + 4-clique + diamond per graph in one replayed CUDA graph: plain
+heuristic / autotuned / learned schedules, per-graph counts checked against the
+committed fixture).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl engine|reference]
-                  [--pattern 4-clique|5-clique] [--policy learned|heuristic]
+                  [--pattern 4-clique|5-clique|triangle] [--policy learned|heuristic]
+                  [--workload clique|batch|motifs|patterns5]
 
---impl reference times the reference's CPU counting algorithm (oracle port of the
-G2Miner OpenMP path, all host threads) on a bounded sample of the same workload.
+--impl reference times the reference's CPU counting algorithm (the oracle's restatement
+of the G2Miner OpenMP path, all host threads) on a seeded uniform random sample of the
+top-level vertices of the same graph, built by the oracle's own generator and CSR build
+(the engine's library is not loaded).  The engine's `cpu_baseline` times the same sample.
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import importlib
 import json
 import os
@@ -37,7 +49,14 @@ WORKLOAD = {"graph": "rmat", "scale": 22, "edge_factor": 16, "abcd": [0.57, 0.19
             "seed": 2}
 PATTERN_KIND = {"4-clique": "clique4", "5-clique": "clique5", "triangle": "tc"}
 COSTMODEL = os.path.join(ROOT, "x-gminer_gb300", "costmodel.json")
+CONFIG_FIXTURE = os.path.join(ROOT, "tests", "golden", "config_counts.json")
+BATCH_FIXTURE = os.path.join(ROOT, "tests", "golden", "batch_counts.json")
 L2_BYTES = 129 * 1024 * 1024
+SAMPLE_SEED = 12345
+# Fraction of the top-level vertices in the CPU sample, per (pattern, scale): about
+# 4-5 s of the 16-core oracle per step at R-MAT scale 22.  Other cases calibrate.
+SAMPLE_FRACTION = {("4-clique", 22): 1 / 16, ("triangle", 22): 1 / 2, ("5-clique", 22): 1 / 512,
+                   ("4-clique", 16): 1.0, ("triangle", 16): 1.0}
 
 
 def parse():
@@ -49,9 +68,12 @@ def parse():
     p.add_argument("--pattern", default="4-clique", choices=list(PATTERN_KIND))
     p.add_argument("--policy", default="learned", choices=["learned", "heuristic"])
     p.add_argument("--scale", type=int, default=WORKLOAD["scale"])
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--cpu-seconds", type=float, default=5.0,
+                   help="target seconds of one CPU sample where no fraction is fixed")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-clique5", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
     p.add_argument("--workload", default="clique",
                    choices=["clique", "batch", "motifs", "patterns5"],
                    help="clique: k-clique counting on R-MAT s22; batch: 4096 BA graphs; "
@@ -134,6 +156,7 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+        return self
 
     def stop(self) -> dict:
         if not self.proc:
@@ -165,24 +188,6 @@ def load_engine():
     return importlib.import_module("x-gminer_gb300")
 
 
-def load_model(xgm, ctx):
-    """The trained cost model (x-gminer_gb300/costmodel.json) and its schedule settings
-    (queue order, margin) as count() keyword arguments."""
-    if not os.path.exists(COSTMODEL):
-        return None, {}
-    with open(COSTMODEL) as f:
-        spec = json.load(f)
-    if (spec.get("features") != xgm.MODEL_FEATURES or spec.get("variants") != xgm.NUM_VARIANTS
-            or len(spec["params"]) != xgm.MODEL_PARAMS):
-        return None, {}  # trained for another feature layout: fall back to the heuristic
-    import numpy as np
-
-    m = xgm.Model(ctx)
-    m.set_params(np.asarray(spec["params"], dtype=np.float32))
-    return m, {"order_by_cost": int(spec.get("order_by_cost", 1)),
-               "margin": float(spec.get("margin", 0.0))}
-
-
 def measured_peaks() -> dict:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -192,46 +197,198 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profile_traffic(pattern: str):
-    """dram bytes per launch of the counting kernel from the committed ncu summary."""
+def profile_summary(pattern: str, scale: int) -> dict:
+    """`key: value` lines of the committed ncu summary of the counting kernel
+    (profiles/k_clique<k>_rmat_s<scale>.md): DRAM traffic per launch and issue rate."""
     name = {"4-clique": "k_clique4", "5-clique": "k_clique5", "triangle": "k_clique3"}[pattern]
-    path = os.path.join(ROOT, "profiles", f"{name}_rmat_s22.md")
+    path = os.path.join(ROOT, "profiles", f"{name}_rmat_s{scale}.md")
+    out = {"path": os.path.relpath(path, ROOT)}
     if not os.path.exists(path):
-        return None
+        return out
     for line in open(path):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if ":" not in line or line.startswith(("|", "#", " ")):
+            continue
+        k, v = line.split(":", 1)
+        k = k.strip()
+        if k in ("traffic_bytes_per_launch", "issue_active_pct", "threads_per_warp_inst",
+                 "l2_hit_pct", "kernel_ms_under_ncu"):
             try:
-                return int(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+                out[k] = float(v.strip().split()[0])
+            except (ValueError, IndexError):
+                pass
+    return out
 
 
-def cpu_sample(orc, kind: str, drow, dcol, budget_s: float):
-    """Times the oracle port on every `stride`-th top-level vertex (all host threads),
-    with the stride picked from a short calibration so the sample takes ~budget_s."""
+def fixture_counts(scale: int, seed: int) -> dict:
+    """Reference-binary counts of the R-MAT graph (tests/golden/config_counts.json)."""
+    if not os.path.exists(CONFIG_FIXTURE):
+        return {}
+    with open(CONFIG_FIXTURE) as f:
+        data = json.load(f)
+    return data.get(f"rmat_s{scale}_ef16_seed{seed}", {})
+
+
+def check_count(fx: dict, kind: str, got: int) -> bool:
+    """True when the fixture holds this count (and then it must match)."""
+    want = fx.get("counts", {}).get(kind)
+    if want is None:
+        return False
+    assert got == want, f"{kind}: engine {got} != reference binaries {want}"
+    return True
+
+
+def workload_config(args, V, E, E_dag, max_deg, max_out, world) -> dict:
+    """The workload description; both arms print the same dict for the same run."""
+    return {"workload": f"{args.pattern} counting, R-MAT scale {args.scale} edge factor 16",
+            "pattern": args.pattern, "graph": dict(WORKLOAD, scale=args.scale),
+            "V": int(V), "E_undirected_entries": int(E), "E_dag": int(E_dag),
+            "max_degree": int(max_deg), "max_out_degree": int(max_out),
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (adjacency %.0f MB > 129 MB)" % (E * 4 / 2**20)}
+
+
+def sample_fraction(orc, pattern: str, scale: int, kind: str, drow, dcol, budget_s: float):
+    """Fraction of top-level vertices in the CPU sample: fixed per (pattern, scale) so
+    both arms time the same sample; otherwise doubled from 2^-16 until one sample takes
+    at least half the budget."""
+    if (pattern, scale) in SAMPLE_FRACTION:
+        return SAMPLE_FRACTION[(pattern, scale)]
     nv = len(drow) - 1
-    cores = orc.threads()
-    # halve a power-of-two stride (nested samples: every 2^k-th vertex) until the sample
-    # takes at least half the budget; that sample is the measurement
-    stride = 1 << 20
-    while True:
+    f = 2.0 ** -16
+    while f < 1.0:
+        smp = orc.vertex_sample(nv, f, SAMPLE_SEED)
         t0 = time.perf_counter()
-        c = orc.count(kind, drow, dcol, 0, nv, stride)
-        dt = time.perf_counter() - t0
-        if dt >= budget_s / 2 or stride == 1:
-            return c, dt, stride, cores
-        stride //= 2
+        orc.count(kind, drow, dcol, sample=smp)
+        if time.perf_counter() - t0 >= budget_s / 2:
+            return f
+        f *= 2
+    return 1.0
 
 
-def gen_graph(xgm, scale):
+def cpu_sample(orc, pattern: str, scale: int, drow, dcol, budget_s: float, total: int = None,
+               repeat: int = 1):
+    """Times the oracle port (all host threads) on a seeded uniform random vertex sample.
+    Returns (matches in the sample, seconds per run, description dict)."""
+    kind = PATTERN_KIND[pattern]
+    nv = len(drow) - 1
+    frac = sample_fraction(orc, pattern, scale, kind, drow, dcol, budget_s)
+    smp = orc.vertex_sample(nv, frac, SAMPLE_SEED)
+    times, c = [], 0
+    for _ in range(repeat):
+        t0 = time.perf_counter()
+        c = orc.count(kind, drow, dcol, sample=smp)
+        times.append(time.perf_counter() - t0)
+    work = orc.algo_bytes(kind, drow, dcol, sample=smp)
+    work_all = orc.algo_bytes(kind, drow, dcol) if frac < 1.0 else work
+    desc = {"fraction": frac, "vertices": int(len(smp)), "seed": SAMPLE_SEED,
+            "matches": int(c), "plan_bytes_share": work / work_all if work_all else None}
+    if total:
+        desc["match_share"] = c / total
+    return c, times, desc
+
+
+def sample_text(desc: dict, scale: int, dt: float) -> str:
+    share = desc.get("match_share")
+    return (f"seeded uniform random sample of {desc['fraction']:.6g} of the top-level vertices "
+            f"of the R-MAT s{scale} DAG ({desc['vertices']} vertices, seed {desc['seed']}): "
+            f"{desc['matches']} matches"
+            + (f" = {share:.4f} of all matches" if share is not None else "")
+            + (f", {desc['plan_bytes_share']:.4f} of the plan's work"
+               if desc.get("plan_bytes_share") is not None else "")
+            + f", {dt:.2f} s per run; oracle port of the G2Miner OpenMP path")
+
+
+def gen_graph(mod, scale):
     a, b, c, _ = WORKLOAD["abcd"]
-    return xgm.gen_rmat(scale, WORKLOAD["edge_factor"], a, b, c, seed=WORKLOAD["seed"])
+    return mod.gen_rmat(scale, WORKLOAD["edge_factor"], a, b, c, seed=WORKLOAD["seed"])
 
 
 # ------------------------------------------------------------------- engine arm
-def engine_arm(args, dist: Dist) -> None:
+def timed_counts(ctx, g, pattern, n, kw):
+    prep, kern, cnt = [], [], None
+    for _ in range(n):
+        cnt, st = ctx.count(g, pattern, with_stats=True, **kw)
+        prep.append(st["prep_ms"])
+        kern.append(st["kernel_ms"])
+    return cnt, prep, kern
+
+
+def clique5_sub(xgm, ctx, g, learned, fx, local) -> dict:
+    """5-clique on the resident graph: learned vs plain heuristic schedule."""
+    clocks = ClockSampler(local).start()
+    out = {}
+    for name, kw in (("learned", learned), ("heuristic", {})):
+        if name == "learned" and not kw:
+            continue
+        timed_counts(ctx, g, "5-clique", 1, kw)
+        _sync()
+        cnt, prep, kern = timed_counts(ctx, g, "5-clique", 2, kw)
+        ms = statistics.mean(p + k for p, k in zip(prep, kern))
+        out[name] = {"ms_per_step": ms, "kernel_ms": statistics.mean(kern),
+                     "matches_per_s": cnt / (ms / 1e3), "count": cnt}
+    counts = {v["count"] for v in out.values()}
+    assert len(counts) == 1, "schedules disagree on the 5-clique count"
+    cnt = counts.pop()
+    out["count_pinned"] = check_count(fx, "clique5", cnt)
+    if "learned" in out:
+        out["learned_speedup"] = out["heuristic"]["ms_per_step"] / out["learned"]["ms_per_step"]
+    out["clocks"] = clocks.stop()
+    return out
+
+
+def batch_run(xgm, ctx, graphs, warmup, steps, local) -> dict:
+    """4096 BA graphs: plain heuristic / autotuned / learned schedules of the batched
+    CUDA-graph launch; per-graph counts checked against the committed fixture."""
     import numpy as np
+
+    vo, eo, src, dst = xgm.gen_ba_batch(graphs, 100, 5000, 3, 8, seed=5)
+    b = ctx.batch_from_edges(vo, src, dst)
+    learned = xgm.trained_schedule(ctx)
+    tune = ctx.autotune(b, BATCH_PATTERNS, reps=3)
+    runs = {"heuristic": {}, "tuned": {"policy": xgm.SCHED_TUNED, "table": tune["table"]}}
+    if learned:
+        runs["learned"] = learned
+    res, ref, kernels = {}, None, {}
+    clocks = ClockSampler(local).start()
+    for name, kw in runs.items():
+        for _ in range(warmup):
+            ctx.count_batched(b, BATCH_PATTERNS, **kw)
+        _sync()
+        ms = []
+        for _ in range(steps):
+            out, st = ctx.count_batched(b, BATCH_PATTERNS, with_stats=True, **kw)
+            ms.append(st["kernel_ms"])
+            kernels[name] = st["launches"]  # kernel nodes of the replayed CUDA graph
+        if ref is None:
+            ref = out
+        assert np.array_equal(out, ref), f"{name} schedule changed a count"
+        res[name] = statistics.mean(ms)
+    clk = clocks.stop()
+    per_graph = np.ascontiguousarray(ref, dtype="<u8")
+    digest = hashlib.sha256(per_graph.tobytes()).hexdigest()
+    totals = {p: int(per_graph[:, i].sum()) for i, p in enumerate(BATCH_PATTERNS)}
+    pinned = False
+    if graphs == 4096 and os.path.exists(BATCH_FIXTURE):
+        with open(BATCH_FIXTURE) as f:
+            fx = json.load(f)
+        assert digest == fx["per_graph_sha256"], "per-graph batch counts differ from the fixture"
+        assert totals == fx["totals"], "batch totals differ from the fixture"
+        pinned = True
+    total = float(per_graph.astype(np.float64).sum())
+    best = min(res, key=res.get)
+    out = {"graphs": graphs, "vertices": int(vo[-1]), "samples": int(len(src)),
+           "patterns": BATCH_PATTERNS, "schedules_ms": res, "best": best,
+           "matches_per_s": {k: total / (v / 1e3) for k, v in res.items()},
+           "tuned_variants": tune["variants"], "totals": totals, "per_graph_sha256": digest,
+           "counts_pinned": pinned, "kernel_nodes": kernels, "clocks": clk}
+    if "learned" in res:
+        out["learned_vs_heuristic"] = res["heuristic"] / res["learned"]
+        out["learned_vs_tuned"] = res["tuned"] / res["learned"]
+    b.close()
+    return out
+
+
+def engine_arm(args, dist: Dist) -> None:
     import torch
 
     xgm = load_engine()
@@ -241,40 +398,34 @@ def engine_arm(args, dist: Dist) -> None:
     g = ctx.graph_from_edges(nv, src, dst)
     del src, dst
     info = g.info()
-    model, mkw = load_model(xgm, ctx) if args.policy == "learned" else (None, {})
-    policy = xgm.SCHED_LEARNED if model is not None else xgm.SCHED_HEURISTIC
-    kw = {"policy": policy, "model": model, **mkw}
+    fx = fixture_counts(args.scale, WORKLOAD["seed"])
+    if fx:
+        assert (info["V"], info["E"]) == (fx["V"], fx["E"]), "not the fixture's graph"
+    learned = xgm.trained_schedule(ctx) if args.policy == "learned" else {}
+    kw = learned
 
-    def run(n, **k):
-        prep, kern, cnt = [], [], None
-        for _ in range(n):
-            cnt, st = ctx.count(g, args.pattern, with_stats=True, **k)
-            prep.append(st["prep_ms"])
-            kern.append(st["kernel_ms"])
-        return cnt, prep, kern
-
-    run(args.warmup, **kw)
+    timed_counts(ctx, g, args.pattern, args.warmup, kw)
     dist.barrier()
     _sync()
-    clocks = ClockSampler(dist.local)
-    clocks.start()
+    clocks = ClockSampler(dist.local).start()
     t0 = time.perf_counter()
-    count, prep, kern = run(args.steps, **kw)
+    count, prep, kern = timed_counts(ctx, g, args.pattern, args.steps, kw)
     _sync()
     wall = time.perf_counter() - t0
     dist.barrier()
     clk = clocks.stop()
+    pinned = check_count(fx, PATTERN_KIND[args.pattern], count)
     step_ms = [p + k for p, k in zip(prep, kern)]
     ms_per_step = dist.reduce(sum(step_ms) / args.steps, "max")
     total_matches = dist.reduce(float(count), "sum")
     value = total_matches / (ms_per_step / 1e3)
     kern_ms = statistics.mean(kern)
 
-    # plain heuristic schedule on the same graph and steps (the baseline of the learned schedule)
+    # plain heuristic schedule on the same graph and steps (the baseline of the learned one)
     plain = None
-    if policy == xgm.SCHED_LEARNED:
-        run(1, policy=xgm.SCHED_HEURISTIC)
-        c2, p2, k2 = run(args.steps, policy=xgm.SCHED_HEURISTIC)
+    if learned:
+        timed_counts(ctx, g, args.pattern, 1, {})
+        c2, p2, k2 = timed_counts(ctx, g, args.pattern, args.steps, {})
         assert c2 == count, "schedules disagree on the count"
         pms = dist.reduce(sum(p + k for p, k in zip(p2, k2)) / args.steps, "max")
         plain = {"matches_per_s": total_matches / (pms / 1e3), "ms_per_step": pms,
@@ -282,9 +433,27 @@ def engine_arm(args, dist: Dist) -> None:
 
     launches = ctx.count_kernels(g, args.pattern, **kw)
     peaks = measured_peaks()
-    algo = ctx.algo_bytes(g, args.pattern)
-    achieved = algo / (kern_ms / 1e3) / 1e9
-    traffic = profile_traffic(args.pattern)
+    plan = ctx.algo_bytes(g, args.pattern)
+    prof = profile_summary(args.pattern, args.scale)
+    traffic = prof.get("traffic_bytes_per_launch")
+    achieved = traffic / (kern_ms / 1e3) / 1e9 if traffic else None
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": achieved / peaks["hbm_gbs"] if achieved else None,
+        "traffic": int(traffic) if traffic else None,
+        "traffic_source": (f"{prof['path']} (ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                           "of this launch, committed capture; divided by this run's "
+                           "CUDA-event kernel time)") if traffic else "no committed capture",
+        "peak_source": peaks["source"],
+        # the reference plan's algorithmic bytes (4 B per list element it reads + 8 B per
+        # task): this kernel reads each list once per vertex task instead, so the plan's
+        # bytes over the launch time exceed the copy peak
+        "plan_bytes_per_launch": plan,
+        "plan_gbs": plan / (kern_ms / 1e3) / 1e9,
+        "issue_active_pct": prof.get("issue_active_pct"),
+        "threads_per_warp_inst": prof.get("threads_per_warp_inst"),
+        "l2_hit_pct": prof.get("l2_hit_pct"),
+    }
     line = {
         "metric": "matches_per_sec",
         "value": value,
@@ -298,33 +467,26 @@ def engine_arm(args, dist: Dist) -> None:
         "vs_baseline": None,
         "dtype": "int32 ids / uint64 counts",
         "data": "synthetic (seeded R-MAT, engine host generator)",
-        "config": {"workload": f"{args.pattern} counting, R-MAT scale {args.scale} edge factor 16",
-                   "pattern": args.pattern, "graph": dict(WORKLOAD, scale=args.scale),
-                   "V": info["V"], "E_undirected_entries": info["E"], "E_dag": info["E_dag"],
-                   "max_degree": info["max_degree"], "max_out_degree": info["max_out_degree"],
-                   "schedule": "learned" if policy == xgm.SCHED_LEARNED else "heuristic",
-                   "parallelism": f"replicas x{dist.world}",
-                   "l2": "inputs larger than L2 (adjacency %.0f MB > 129 MB)" % (info["E"] * 4 / 2**20)},
+        "config": workload_config(args, info["V"], info["E"], info["E_dag"],
+                                  info["max_degree"], info["max_out_degree"], dist.world),
+        "schedule": "learned" if learned else "heuristic",
         "count": count,
+        "count_pinned": pinned,
         "gteps": info["E_dag"] / (ms_per_step / 1e3) / 1e9,
         "kernel_ms": kern_ms,
         "prep_ms": statistics.mean(prep),
         "wall_ms_per_step": wall * 1e3 / args.steps,
         "plain_heuristic": plain,
         "gpu_launches": launches * args.steps,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": traffic, "algo_bytes_per_launch": algo,
-                     # the measured DRAM traffic of the launch over its time: what the
-                     # kernel actually moves (it reads each list once per task)
-                     "dram_gbs": (traffic / (kern_ms / 1e3) / 1e9) if traffic else None,
-                     "dram_frac": (traffic / (kern_ms / 1e3) / 1e9 / peaks["hbm_gbs"])
-                     if traffic else None,
-                     "peak_source": peaks["source"]},
+        "roofline": roofline,
         "clocks": clk,
     }
 
+    if args.pattern == "4-clique" and not args.no_clique5 and dist.rank == 0:
+        line["clique5"] = clique5_sub(xgm, ctx, g, learned, fx, dist.local)
+
     # end to end through the C ABI from pinned host buffers
+    rp = cp = None
     if not args.no_e2e:
         rowptr, col = g.download()
         rp = torch.empty(len(rowptr), dtype=torch.int64, pin_memory=True)
@@ -333,6 +495,7 @@ def engine_arm(args, dist: Dist) -> None:
         cp.numpy()[:] = col
         del rowptr, col
         g.close()
+        g = None
         e2e_t = []
         for i in range(args.warmup + args.steps):
             _sync()
@@ -348,7 +511,9 @@ def engine_arm(args, dist: Dist) -> None:
         line["e2e"] = {"value": total_matches / e2e_s, "unit": "matches/s",
                        "h2d_bytes_per_step": int(rp.numel() * 8 + cp.numel() * 4),
                        "d2h_bytes_per_step": 8, "ms_per_step": e2e_s * 1e3}
-        g = None
+
+    if args.pattern == "4-clique" and not args.no_batch and dist.rank == 0:
+        line["batch"] = batch_run(xgm, ctx, args.graphs, 2, 5, dist.local)
 
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -358,14 +523,16 @@ def engine_arm(args, dist: Dist) -> None:
         else:
             rowptr, col = g.download()
         drow, dcol = oracle.orient(rowptr, col)
-        c, dt, stride, cores = cpu_sample(oracle, PATTERN_KIND[args.pattern], drow, dcol,
-                                          args.cpu_seconds)
-        line["cpu_baseline"] = {"value": c / dt, "unit": "matches/s", "cores": cores,
-                                "kind": "port",
-                                "sample": f"every {stride}-th top-level vertex of the same DAG "
-                                          f"({c} matches in {dt:.2f} s, OpenMP oracle port)"}
+        c, times, desc = cpu_sample(oracle, args.pattern, args.scale, drow, dcol,
+                                    args.cpu_seconds, total=count)
+        line["cpu_baseline"] = {"value": c / times[0], "unit": "matches/s",
+                                "cores": oracle.threads(), "kind": "port",
+                                "sample": sample_text(desc, args.scale, times[0]),
+                                "sample_detail": desc}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
+    if g is not None:
+        g.close()
     ctx.close()
 
 
@@ -377,136 +544,116 @@ def batch_arm(args, dist: Dist) -> None:
     """Batched multi-graph counting: Barabasi-Albert graphs, n log-uniform in
     [100, 5000], m uniform in {3..8}, seed 5; triangle + 4-clique + diamond per graph in
     one persistent launch replayed as a CUDA graph.  Compared with the same counts made
-    by one xgm_count call per (graph, pattern)."""
-    import numpy as np
+    by one xgm_count call per (graph, pattern) on a sample of the graphs."""
     import torch
 
     xgm = load_engine()
     torch.cuda.set_device(dist.local)
     ctx = xgm.Context(dist.local)
+    res = batch_run(xgm, ctx, args.graphs, args.warmup, args.steps, dist.local)
     vo, eo, src, dst = xgm.gen_ba_batch(args.graphs, 100, 5000, 3, 8, seed=5)
-    b = ctx.batch_from_edges(vo, src, dst)
-    model, mkw = load_model(xgm, ctx)
-    tune = ctx.autotune(b, BATCH_PATTERNS, reps=3)
-    runs = {"heuristic": {}, "tuned": {"policy": xgm.SCHED_TUNED, "table": tune["table"]}}
-    if model is not None:
-        runs["learned"] = {"policy": xgm.SCHED_LEARNED, "model": model, **mkw}
-    res, ref, kernels = {}, None, {}
-    clocks = ClockSampler(dist.local)
-    clocks.start()
-    for name, kw in runs.items():
-        for _ in range(args.warmup):
-            ctx.count_batched(b, BATCH_PATTERNS, **kw)
-        _sync()
-        ms = []
-        for _ in range(args.steps):
-            out, st = ctx.count_batched(b, BATCH_PATTERNS, with_stats=True, **kw)
-            ms.append(st["kernel_ms"])
-            kernels[name] = st["launches"]  # kernel nodes of the replayed CUDA graph
-        if ref is None:
-            ref = out
-        assert np.array_equal(out, ref), f"{name} schedule changed a count"
-        res[name] = statistics.mean(ms)
-    clk = clocks.stop()
-    total = float(ref.astype(np.float64).sum())
-    best = min(res, key=res.get)
-    # per-graph calls on a sample of graphs, scaled to the whole batch
     sample = list(range(0, args.graphs, max(1, args.graphs // 256)))
-    loop_s, loop_matches, loop_graphs = 0.0, 0, 0
+    loop_s, loop_graphs = 0.0, 0
     for gi in sample:
         lo, hi = int(vo[gi]), int(vo[gi + 1])
         g = ctx.graph_from_edges(hi - lo, src[eo[gi]:eo[gi + 1]] - lo, dst[eo[gi]:eo[gi + 1]] - lo)
         _sync()
         t0 = time.perf_counter()
-        for p, pat in enumerate(BATCH_PATTERNS):
-            c = ctx.count(g, pat)
-            assert c == int(ref[gi, p])
-            loop_matches += c
+        for pat in BATCH_PATTERNS:
+            ctx.count(g, pat)
         loop_s += time.perf_counter() - t0
         loop_graphs += 1
         g.close()
     loop_ms_full = loop_s * 1e3 * args.graphs / loop_graphs
-    line = {"metric": "matches_per_sec", "value": total / (res[best] / 1e3), "unit": "matches/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res[best],
+    best = res["best"]
+    ms = res["schedules_ms"][best]
+    total = sum(res["totals"].values())
+    line = {"metric": "matches_per_sec", "value": total / (ms / 1e3), "unit": "matches/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32 ids / uint64 counts", "data": "synthetic (seeded Barabasi-Albert)",
             "config": {"workload": f"batched counting, {args.graphs} BA graphs, "
                                    "triangle + 4-clique + diamond per graph",
-                       "graphs": args.graphs, "vertices": int(vo[-1]), "samples": int(len(src)),
-                       "schedule": best},
-            "schedules_ms": res, "tuned_variants": tune["variants"],
+                       "graphs": args.graphs, "vertices": res["vertices"],
+                       "samples": res["samples"]},
+            "schedule": best, "batch": res,
             "per_graph_calls_ms_estimate": loop_ms_full,
-            "speedup_vs_per_graph_calls": loop_ms_full / res[best],
-            "count_total": int(total), "gpu_launches": kernels[best] * args.steps,
-            "clocks": clk}
+            "speedup_vs_per_graph_calls": loop_ms_full / ms,
+            "count_total": total,
+            "gpu_launches": res["kernel_nodes"][best] * args.steps, "clocks": res["clocks"]}
     print(json.dumps(line), flush=True)
     ctx.close()
 
 
 # ---------------------------------------------------------------- reference arm
 def reference_arm(args, dist: Dist) -> None:
+    """The reference's CPU counting algorithm (oracle restatement of the G2Miner OpenMP
+    path, all host threads) on the seeded uniform vertex sample of the same graph.  The
+    graph is generated and built by the oracle alone (the engine is not loaded)."""
     if dist.rank != 0:
         return
+    import numpy as np
+
     import oracle
 
-    xgm = load_engine()  # host generator only (no GPU use)
-    nv, src, dst = gen_graph(xgm, args.scale)
+    nv, src, dst = gen_graph(oracle, args.scale)
     rowptr, col = oracle.build_csr(nv, src, dst)
     del src, dst
     drow, dcol = oracle.orient(rowptr, col)
-    kind = PATTERN_KIND[args.pattern]
-    per_step = max(2.0, min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup)))
-    c, dt, stride, cores = cpu_sample(oracle, kind, drow, dcol, per_step)
-    times, counts = [], []
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        ci = oracle.count(kind, drow, dcol, 0, nv, stride)
-        t = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(t)
-            counts.append(ci)
+    max_deg = int(np.diff(rowptr).max())
+    E = len(col)
+    del rowptr, col
+    max_out = int(np.diff(drow).max())
+    fx = fixture_counts(args.scale, WORKLOAD["seed"])
+    total = fx.get("counts", {}).get(PATTERN_KIND[args.pattern])
+    c, times, desc = cpu_sample(oracle, args.pattern, args.scale, drow, dcol, args.cpu_seconds,
+                                total=total, repeat=args.warmup + args.steps)
+    times = times[args.warmup:]
     ms = statistics.mean(times) * 1e3
-    value = counts[-1] / (ms / 1e3)
-    sample = (f"every {stride}-th top-level vertex of the R-MAT s{args.scale} DAG "
-              f"({counts[-1]} matches per step); oracle port of the OpenMP path")
+    value = c / (ms / 1e3)
+    cores = oracle.threads()
     line = {"metric": "matches_per_sec", "value": value, "unit": "matches/s", "n_gpus": dist.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32 ids / uint64 counts", "data": "synthetic (seeded R-MAT)",
-            "config": {"workload": f"{args.pattern} counting, R-MAT scale {args.scale} edge factor 16",
-                       "pattern": args.pattern, "graph": dict(WORKLOAD, scale=args.scale)},
+            "dtype": "int32 ids / uint64 counts", "data": "synthetic (seeded R-MAT, oracle generator)",
+            "config": workload_config(args, nv, E, len(dcol), max_deg, max_out, dist.world),
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "matches/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample_text(desc, args.scale, ms / 1e3),
+                             "sample_detail": desc},
             "e2e": {"value": value, "unit": "matches/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 MOTIF_PATTERNS = ["diamond", "rectangle", "tailedtriangle", "4-clique"]
+MOTIF_KIND = {"diamond": "diamond", "rectangle": "cycle4", "tailedtriangle": "tailed",
+              "4-clique": "clique4"}
 
 
 def motifs_arm(args, dist: Dist) -> None:
     """Edge-induced diamond / 4-cycle / tailed triangle / 4-clique on an Erdos-Renyi
-    G(n = 2^21, average degree 32) and a Chung-Lu power-law graph (n = 2^21, exponent
-    2.1, maximum expected degree 50,000), seeded.  One step counts all four patterns on
-    both graphs; matches/s = total count / total device time."""
+    G(n = 2^21, average degree 32), seed 3, and a Chung-Lu power-law graph (n = 2^21,
+    exponent 2.1, maximum expected degree 50,000, average degree 32), seed 4.  One step
+    counts all four patterns on both graphs; matches/s = total count / total device
+    time.  Counts are checked against the reference binaries' fixture."""
     import torch
 
     xgm = load_engine()
     torch.cuda.set_device(dist.local)
     ctx = xgm.Context(dist.local)
     n = 1 << 21
-    graphs = {"er": xgm.gen_er(n, n * 16, seed=31),
-              "chung_lu": xgm.gen_chung_lu(n, 2.1, 50000.0, 32.0, seed=32)}
-    model, mkw = load_model(xgm, ctx) if args.policy == "learned" else (None, {})
-    kw = {"policy": xgm.SCHED_LEARNED, "model": model, **mkw} if model is not None else {}
-    per, total_ms, total_matches, info, launches = {}, 0.0, 0, {}, 0
-    clocks = ClockSampler(dist.local)
-    clocks.start()
+    graphs = {"er_n2097152_deg32_seed3": xgm.gen_er(n, n * 16, seed=3),
+              "chung_lu_n2097152_g2.1_w50000_deg32_seed4":
+                  xgm.gen_chung_lu(n, 2.1, 50000.0, 32.0, seed=4)}
+    fixtures = json.load(open(CONFIG_FIXTURE)) if os.path.exists(CONFIG_FIXTURE) else {}
+    kw = xgm.trained_schedule(ctx) if args.policy == "learned" else {}
+    per, total_ms, total_matches, info, launches, pinned = {}, 0.0, 0, {}, 0, 0
+    clocks = ClockSampler(dist.local).start()
     for gname, (nv, src, dst) in graphs.items():
         g = ctx.graph_from_edges(nv, src, dst)
         info[gname] = g.info()
+        fx = fixtures.get(gname, {})
         for pat in MOTIF_PATTERNS:
             for _ in range(args.warmup):
                 ctx.count(g, pat, **kw)
@@ -516,6 +663,7 @@ def motifs_arm(args, dist: Dist) -> None:
                 cnt, st = ctx.count(g, pat, with_stats=True, **kw)
                 ms.append(st["kernel_ms"] + st["prep_ms"])
                 launches += st["launches"]
+            pinned += check_count(fx, MOTIF_KIND[pat], cnt)
             per[f"{gname}/{pat}"] = {"count": cnt, "ms": statistics.mean(ms)}
             total_ms += statistics.mean(ms)
             total_matches += cnt
@@ -527,9 +675,9 @@ def motifs_arm(args, dist: Dist) -> None:
             "vs_baseline": None, "dtype": "int32 ids / uint64 counts",
             "data": "synthetic (seeded Erdos-Renyi and Chung-Lu)",
             "config": {"workload": "edge-induced 4-vertex motifs, ER 2^21 deg 32 and "
-                                   "Chung-Lu 2^21 gamma 2.1 dmax 50k",
-                       "schedule": "learned" if model is not None else "heuristic",
-                       "graphs": info},
+                                   "Chung-Lu 2^21 gamma 2.1 dmax 50k", "graphs": info},
+            "schedule": "learned" if kw else "heuristic",
+            "counts_pinned": f"{pinned} of {len(per)}",
             "gpu_launches": launches // max(1, args.steps), "clocks": clk, "per_pattern": per}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -549,8 +697,7 @@ def patterns5_arm(args, dist: Dist) -> None:
     graphs = {"rmat_s12_ef8": xgm.gen_rmat(12, 8, seed=3),
               "er_2^16_deg16": xgm.gen_er(1 << 16, 1 << 19, seed=3)}
     per, total_ms, total_matches, info, launches = {}, 0.0, 0, {}, 0
-    clocks = ClockSampler(dist.local)
-    clocks.start()
+    clocks = ClockSampler(dist.local).start()
     for gname, (nv, src, dst) in graphs.items():
         g = ctx.graph_from_edges(nv, src, dst)
         info[gname] = g.info()

@@ -276,13 +276,15 @@ xgm_status xgm_count_kernels(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
                              const xgm_sched* sched, int* n_kernels);
 
 /* Triangle count that allocates no device memory.  No counterpart in the reference.
- * For callers that cannot allocate while they count (a stream under CUDA-graph capture,
- * a host framework that owns all device memory, an allocation-free hot loop): the
- * task lists and counters live in a 48 MiB file-scope device array instead of memory
- * allocated per call, so graphs of up to 2^21 vertices are accepted (larger:
- * XGM_ERR_UNSUPPORTED).  Same result as xgm_tc_solver.  All calls share the array, so
- * calls whose GPU work overlaps race; the first call on a device resolves the array's
- * address and should come before any stream capture. */
+ * For callers that cannot allocate while they count (a host framework that owns all
+ * device memory through its own allocator, a hot loop with no room for cudaMalloc):
+ * the task lists and counters live in a 48 MiB file-scope device array instead of
+ * memory allocated per call, so graphs of up to 2^21 vertices are accepted (larger:
+ * XGM_ERR_UNSUPPORTED).  Same result as xgm_tc_solver; the graph must belong to ctx.
+ * All calls share the array and it keeps the last call's contents (each call clears
+ * what it reuses), so calls whose GPU work overlaps race.  The first call on a device
+ * resolves the array's address and should come before any stream capture.  The call
+ * waits for ctx's stream and leaves the caller's current device unchanged. */
 xgm_status xgm_tc_solver_static(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total);
 
 /* Algorithmic adjacency bytes the plan reads on g (host pass over the downloaded

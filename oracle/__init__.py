@@ -5,6 +5,8 @@ CPU-baseline leg of bench.py as the checker; the engine never imports or calls i
 
  - oracle.c: plain-C restatement of the reference's OpenMP counting path (each
    function cites the reference lines it follows), built here into liborc.so.
+ - gen.c: the seeded graph generators (same samples as the engine's), so the CPU
+   legs build their graphs without loading the engine.
  - _ref/: the reference's own OpenMP binaries built from its sources by build_ref.sh
    (only where the reference tree is present); run_ref() runs them on graph files.
  - mlp_ref.py: numpy forward/backward of the cost model, the gradient checker.
@@ -22,6 +24,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "oracle.c")
+GEN_SRC = os.path.join(HERE, "gen.c")
 LIB = os.path.join(HERE, "liborc.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
@@ -29,14 +32,16 @@ _lib = None
 
 
 def build() -> str:
-    """Compiles oracle.c (OpenMP when the compiler has it)."""
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    """Compiles oracle.c and gen.c (OpenMP when the compiler has it)."""
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC),
+                                                             os.path.getmtime(GEN_SRC)):
         return LIB
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
         raise RuntimeError("no C compiler for the oracle")
     tmp = LIB + ".tmp"
-    base = [cc, "-O3", "-std=c11", "-fPIC", "-shared", SRC, "-o", tmp]
+    base = [cc, "-O3", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", SRC, GEN_SRC,
+            "-o", tmp, "-lm"]
     r = subprocess.run(base[:2] + ["-fopenmp"] + base[2:], capture_output=True, text=True)
     if r.returncode != 0:
         r = subprocess.run(base, capture_output=True, text=True)
@@ -88,8 +93,81 @@ def lib():
         L.orc_setprog.argtypes = [P, C.c_int, I64, P, P, I64, P]
         L.orc_occurrences.restype = C.c_int
         L.orc_occurrences.argtypes = [C.c_int, P, C.c_int, I64, P, P, P]
+        L.orc_set_sample.argtypes = [P, I64]
+        D = C.c_double
+        L.orc_gen_rmat.restype = I64
+        L.orc_gen_rmat.argtypes = [C.c_int, C.c_int, D, D, D, U64, P, P]
+        L.orc_gen_er.restype = I64
+        L.orc_gen_er.argtypes = [I64, I64, U64, P, P]
+        L.orc_gen_chung_lu.restype = I64
+        L.orc_gen_chung_lu.argtypes = [I64, D, D, D, U64, P, P]
+        L.orc_gen_ba.restype = I64
+        L.orc_gen_ba.argtypes = [I64, C.c_int, U64, P, P]
+        L.orc_gen_ba_batch.restype = I64
+        L.orc_gen_ba_batch.argtypes = [C.c_int, I64, I64, C.c_int, C.c_int, U64, P, P, P, P]
         _lib = L
     return _lib
+
+
+# ------------------------------------------------------------ seeded generators
+def _samples(m: int):
+    if m < 0:
+        raise ValueError("invalid generator parameters")
+    return np.empty(m, dtype=np.int32), np.empty(m, dtype=np.int32)
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19,
+             c: float = 0.19, seed: int = 1):
+    """R-MAT edge samples (same samples as the engine's xgm_gen_rmat)."""
+    s, d = _samples(lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, None, None))
+    lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, s.ctypes.data, d.ctypes.data)
+    return 1 << scale, s, d
+
+
+def gen_er(n: int, m: int, seed: int = 1):
+    s, d = _samples(lib().orc_gen_er(n, m, seed, None, None))
+    lib().orc_gen_er(n, m, seed, s.ctypes.data, d.ctypes.data)
+    return n, s, d
+
+
+def gen_chung_lu(n: int, gamma: float = 2.1, w_max: float = 50000.0, avg_deg: float = 32.0,
+                 seed: int = 1):
+    s, d = _samples(lib().orc_gen_chung_lu(n, gamma, w_max, avg_deg, seed, None, None))
+    if lib().orc_gen_chung_lu(n, gamma, w_max, avg_deg, seed, s.ctypes.data, d.ctypes.data) < 0:
+        raise MemoryError("oracle Chung-Lu generator failed")
+    return n, s, d
+
+
+def gen_ba(n: int, m: int, seed: int = 1):
+    s, d = _samples(lib().orc_gen_ba(n, m, seed, None, None))
+    if lib().orc_gen_ba(n, m, seed, s.ctypes.data, d.ctypes.data) < 0:
+        raise MemoryError("oracle BA generator failed")
+    return n, s, d
+
+
+def gen_ba_batch(num_graphs: int, n_lo: int = 100, n_hi: int = 5000, m_lo: int = 3,
+                 m_hi: int = 8, seed: int = 5):
+    vo = np.empty(num_graphs + 1, dtype=np.int64)
+    eo = np.empty(num_graphs + 1, dtype=np.int64)
+    ne = lib().orc_gen_ba_batch(num_graphs, n_lo, n_hi, m_lo, m_hi, seed, vo.ctypes.data,
+                                eo.ctypes.data, None, None)
+    s, d = _samples(ne)
+    lib().orc_gen_ba_batch(num_graphs, n_lo, n_hi, m_lo, m_hi, seed, vo.ctypes.data,
+                           eo.ctypes.data, s.ctypes.data, d.ctypes.data)
+    return vo, eo, s, d
+
+
+def vertex_sample(nv: int, fraction: float, seed: int = 12345) -> np.ndarray:
+    """A seeded uniform random sample of vertex ids (each vertex kept with probability
+    `fraction`, by a hash of (seed, id)), sorted; int64."""
+    ids = np.arange(nv, dtype=np.uint64)
+    with np.errstate(over="ignore"):  # 64-bit wrap-around is the hash
+        x = ids * np.uint64(0x9E3779B97F4A7C15) + np.uint64(seed) * np.uint64(0xD1B54A32D192ED03)
+        x ^= x >> np.uint64(31)
+        x *= np.uint64(0xBF58476D1CE4E5B9)
+        x ^= x >> np.uint64(29)
+    keep = (x >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0) < fraction
+    return np.nonzero(keep)[0].astype(np.int64)
 
 
 def _take(p, n, dtype):
@@ -134,8 +212,19 @@ def _args(rowptr, col):
 
 
 def count(kind: str, rowptr: np.ndarray, col: np.ndarray, lo: int = 0, hi: int = -1,
-          stride: int = 1) -> int:
-    """kind: tc / clique4 .. clique7 (on a DAG) or diamond / cycle4 / tailed (undirected)."""
+          stride: int = 1, sample: np.ndarray = None) -> int:
+    """kind: tc / clique4 .. clique7 (on a DAG) or diamond / cycle4 / tailed (undirected).
+    With `sample` (int64 vertex ids; triangle and clique kinds only), the top-level
+    loop runs over sample[lo:hi:stride] instead of the vertex range."""
+    if sample is not None:
+        if kind not in ("tc", "clique4", "clique5", "clique6", "clique7"):
+            raise ValueError("vertex samples cover the triangle and clique counts")
+        sample = np.ascontiguousarray(sample, dtype=np.int64)
+        lib().orc_set_sample(sample.ctypes.data, len(sample))
+        try:
+            return count(kind, rowptr, col, lo, len(sample) if hi < 0 else hi, stride)
+        finally:
+            lib().orc_set_sample(None, 0)
     nv, rowptr, col = _args(rowptr, col)
     hi = nv if hi < 0 else hi
     L = lib()
@@ -204,10 +293,20 @@ def occurrences(adj, induced: bool, rowptr: np.ndarray, col: np.ndarray) -> int:
     return int(out[0])
 
 
-def algo_bytes(kind: str, rowptr: np.ndarray, col: np.ndarray) -> int:
+def algo_bytes(kind: str, rowptr: np.ndarray, col: np.ndarray, sample: np.ndarray = None) -> int:
+    """Algorithmic adjacency bytes of the reference plan (4 B per list element read +
+    8 B per task); with `sample`, only the tasks of those top-level vertices."""
     nv, rowptr, col = _args(rowptr, col)
     md = int(np.max(np.diff(rowptr))) if nv else 0
-    return int(lib().orc_algo_bytes(ALGO_KIND[kind], nv, rowptr.ctypes.data, col.ctypes.data, md))
+    if sample is not None:
+        sample = np.ascontiguousarray(sample, dtype=np.int64)
+        lib().orc_set_sample(sample.ctypes.data, len(sample))
+    try:
+        return int(lib().orc_algo_bytes(ALGO_KIND[kind], nv, rowptr.ctypes.data,
+                                        col.ctypes.data, md))
+    finally:
+        if sample is not None:
+            lib().orc_set_sample(None, 0)
 
 
 # ------------------------------------------------------ reference binaries (_ref)

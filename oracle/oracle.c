@@ -186,8 +186,19 @@ int orc_orient(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t** 
 
 /* ------------------------------------------------------------- counting */
 /* All counting functions take the outer-loop range [lo, hi) with `stride`, so the
- * CPU baseline can time a bounded sample; (0, V, 1) is the full count. */
+ * CPU baseline can time a bounded sample; (0, V, 1) is the full count.  With a sample
+ * list set (orc_set_sample), the triangle and clique functions instead take their
+ * top-level vertices from sample[lo..hi) with `stride` (a seeded uniform random
+ * vertex sample for the CPU baseline). */
 #define ROW(v) (col + rowptr[(v)]), (rowptr[(v) + 1] - rowptr[(v)])
+
+static const int64_t* g_sample = NULL;
+static int64_t g_sample_n = 0;
+void orc_set_sample(const int64_t* verts, int64_t n) {
+  g_sample = n > 0 ? verts : NULL;
+  g_sample_n = n > 0 ? n : 0;
+}
+#define TOP(i) (g_sample ? g_sample[(i)] : (i))
 
 /* TCSolver, codes/GraphMiner/src/triangle/omp_base.cc:5-26 (on the DAG). */
 uint64_t orc_tc(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t lo, int64_t hi,
@@ -195,7 +206,8 @@ uint64_t orc_tc(int64_t nv, const int64_t* rowptr, const int32_t* col, int64_t l
   (void)nv;
   uint64_t counter = 0;
 #pragma omp parallel for reduction(+ : counter) schedule(dynamic, 1)
-  for (int64_t u = lo; u < hi; u += stride) {
+  for (int64_t i = lo; i < hi; i += stride) {
+    const int64_t u = TOP(i);
     for (int64_t e = rowptr[u]; e < rowptr[u + 1]; e++) {
       int32_t v = col[e];
       counter += isect_num(ROW(u), ROW(v));
@@ -213,7 +225,8 @@ uint64_t orc_clique4(int64_t nv, const int64_t* rowptr, const int32_t* col, int6
   {
     vid_t* y0y1 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
 #pragma omp for schedule(dynamic, 1)
-    for (int64_t v0 = lo; v0 < hi; v0 += stride) {
+    for (int64_t i = lo; i < hi; i += stride) {
+      const int64_t v0 = TOP(i);
       uint64_t local = 0;
       for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) {
         int32_t v1 = col[e];
@@ -237,7 +250,8 @@ uint64_t orc_clique5(int64_t nv, const int64_t* rowptr, const int32_t* col, int6
     vid_t* y1y2 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
     vid_t* y1y2y3 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
 #pragma omp for schedule(dynamic, 1)
-    for (int64_t v1 = lo; v1 < hi; v1 += stride) {
+    for (int64_t i = lo; i < hi; i += stride) {
+      const int64_t v1 = TOP(i);
       uint64_t local = 0;
       for (int64_t e = rowptr[v1]; e < rowptr[v1 + 1]; e++) {
         int32_t v2 = col[e];
@@ -282,9 +296,11 @@ uint64_t orc_clique_k(int k, int64_t nv, const int64_t* rowptr, const int32_t* c
   {
     vid_t* buf = (vid_t*)malloc(sizeof(vid_t) * level * (size_t)k);
 #pragma omp for schedule(dynamic, 1)
-    for (int64_t v0 = lo; v0 < hi; v0 += stride)
+    for (int64_t i = lo; i < hi; i += stride) {
+      const int64_t v0 = TOP(i);
       counter += kclique_rec(rowptr, col, col + rowptr[v0], rowptr[v0 + 1] - rowptr[v0], k - 1,
                              buf, level);
+    }
     free(buf);
   }
   return counter;
@@ -484,8 +500,10 @@ uint64_t orc_algo_bytes(int kind, int64_t nv, const int64_t* rowptr, const int32
   {
     vid_t* w = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
     vid_t* w2 = (vid_t*)malloc(sizeof(vid_t) * (size_t)(max_deg + 1));
+    const int64_t ntop = g_sample ? g_sample_n : nv;
 #pragma omp for schedule(dynamic, 64)
-    for (int64_t v0 = 0; v0 < nv; v0++) {
+    for (int64_t i = 0; i < ntop; i++) {
+      const int64_t v0 = TOP(i);
       if (kind == 8) {
         if (DEG(v0) > 2)
           for (int64_t e = rowptr[v0]; e < rowptr[v0 + 1]; e++) bytes += 4 * (DEG(v0) + DEG(col[e]));

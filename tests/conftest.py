@@ -14,7 +14,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 GOLDEN = os.path.join(ROOT, "tests", "golden", "golden_counts.json")
-REFERENCE_GRAPHS = "/root/reference/codes/GraphMiner/inputs"
+# the reference tree (X-GMiner checkout), where present; same variable as
+# oracle/build_ref.sh
+REFERENCE_ROOT = os.environ.get("XGM_REFERENCE_ROOT", "/root/reference")
+REFERENCE_GRAPHS = os.path.join(REFERENCE_ROOT, "codes", "GraphMiner", "inputs")
 
 
 def pytest_configure(config):

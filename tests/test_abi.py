@@ -8,7 +8,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import REFERENCE_ROOT, ROOT
 
 
 def header_functions():
@@ -147,7 +147,8 @@ def test_plan_from_spec(xgm):
         assert e.value.status == st, bad
 
 
-GLUMIN_PATTERNS = "/root/reference/codes/GLUMIN/codegen/codegen/patterns"
+GLUMIN_PATTERNS = os.path.join(REFERENCE_ROOT, "codes", "GLUMIN", "codegen", "codegen",
+                               "patterns")
 
 
 @pytest.mark.skipif(not os.path.isdir(GLUMIN_PATTERNS), reason="reference tree absent")
@@ -168,3 +169,30 @@ def test_reference_pattern_files(xgm):
     for name, edges in xgm.YML5_EDGES.items():
         text = open(os.path.join(GLUMIN_PATTERNS, name + ".yml")).read()
         assert "edges: [" + edges + "]" in text, name
+
+
+def test_oracle_generators_match_engine(xgm, orc):
+    """The oracle's generators (used by the CPU legs, which never load the engine)
+    give the engine's samples bit for bit, Chung-Lu and the BA batch sizes included."""
+    cases = [("gen_rmat", (12, 16, 0.57, 0.19, 0.19, 3)), ("gen_er", (5000, 40000, 4)),
+             ("gen_chung_lu", (1 << 15, 2.1, 3000.0, 16.0, 4)), ("gen_ba", (3000, 5, 4))]
+    for name, args in cases:
+        a, b = getattr(orc, name)(*args), getattr(xgm, name)(*args)
+        assert a[0] == b[0], name
+        assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2]), name
+    a = orc.gen_ba_batch(96, 100, 5000, 3, 8, seed=5)
+    b = xgm.gen_ba_batch(96, 100, 5000, 3, 8, seed=5)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_chung_lu_weights_are_host_independent(orc):
+    """Chung-Lu samples depend only on integer and correctly rounded IEEE steps: a
+    fixed digest of a small graph's samples (the same on x86-64 and aarch64)."""
+    import hashlib
+
+    nv, s, d = orc.gen_chung_lu(1 << 12, 2.1, 500.0, 8.0, seed=4)
+    h = hashlib.sha256(s.astype("<i4").tobytes() + d.astype("<i4").tobytes()).hexdigest()
+    assert h == CHUNG_LU_4096_DIGEST
+
+
+CHUNG_LU_4096_DIGEST = "ba625a565a6675d02c816b09587f574bfb0f4df61009565bee756230663a7413"

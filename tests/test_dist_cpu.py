@@ -57,3 +57,31 @@ def test_reference_arm_two_ranks_prints_once():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] in ("port", "reference")
+
+
+def test_reference_arm_loads_only_the_oracle(tmp_path):
+    """The reference arm builds its graph with the oracle's generator and CSR build and
+    times the oracle on a seeded uniform vertex sample: the engine's library is never
+    mapped into the process."""
+    script = tmp_path / "ref_only.py"
+    script.write_text(textwrap.dedent(f"""
+        import json, sys
+        sys.path.insert(0, {ROOT!r})
+        sys.argv = ["bench.py", "--impl", "reference", "--scale", "12", "--steps", "1",
+                    "--warmup", "0", "--cpu-seconds", "0.5"]
+        import bench
+        bench.main()
+        maps = open("/proc/self/maps").read()
+        assert "libxgm" not in maps, "the reference arm loaded the engine"
+        assert "liborc" in maps
+        print("maps ok")
+    """))
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="2")
+    r = subprocess.run([sys.executable, str(script)], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "maps ok" in r.stdout
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    d = line["cpu_baseline"]["sample_detail"]
+    assert 0 < d["fraction"] <= 1 and d["vertices"] > 0 and d["matches"] > 0
+    assert line["config"]["V"] == 1 << 12 and "schedule" not in line["config"]

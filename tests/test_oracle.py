@@ -7,7 +7,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import REFERENCE_GRAPHS, csr_digest, golden_samples, oracle_counts
+from conftest import REFERENCE_GRAPHS, REFERENCE_ROOT, csr_digest, golden_samples, oracle_counts
 
 CITESEER = os.path.join(REFERENCE_GRAPHS, "citeseer", "graph")
 
@@ -54,7 +54,7 @@ def _edge_list(path):
 
 @pytest.mark.parametrize("name", ["test_gr1.txt", "test_gr2.txt", "test_gr3.txt", "test_gr4.txt"])
 def test_reference_tiny_graphs(orc, name):
-    path = os.path.join("/root/reference/scripts", name)
+    path = os.path.join(REFERENCE_ROOT, "scripts", name)
     if not os.path.exists(path) or not orc.ref_available("count_omp_base"):
         pytest.skip("reference tree / reference binaries absent")
     nv, s, d = _edge_list(path)

@@ -1,10 +1,12 @@
 """The allocation-free triangle count (xgm_tc_solver_static), called through the C ABI.
 
-Callers that cannot allocate device memory while they count (a stream being captured
-into a CUDA graph, a framework that owns all device memory) use this entry point; its
-scratch is a fixed file-scope device array.  It must give the same count as the
-allocating xgm_tc_solver, call after call (the array keeps the previous call's
-contents, so every call has to reset what it reuses).  Collected last on purpose.
+Callers that cannot allocate device memory while they count (a host framework that owns
+all device memory through its own allocator, a hot loop with no room for cudaMalloc)
+use this entry point; its scratch is a fixed file-scope device array.  It must give the
+same count as the allocating xgm_tc_solver, call after call (the array keeps the
+previous call's contents, so every call has to reset what it reuses), and once a
+device is set up its calls must not change the device's free memory.  Collected last on
+purpose.
 """
 from __future__ import annotations
 
@@ -48,5 +50,32 @@ def test_static_scratch_triangle_count_matches(xgm):
         with pytest.raises(xgm.XgmError) as e:
             _static_tc(xgm, ctx, big)
         assert e.value.status == xgm.ERR_UNSUPPORTED
+    finally:
+        ctx.close()
+
+
+def test_static_calls_leave_free_memory_unchanged(xgm):
+    torch = pytest.importorskip("torch")
+    ctx = xgm.Context(0)
+    try:
+        nv, s, d = xgm.gen_rmat(14, 16, seed=3)
+        g = ctx.graph_from_edges(nv, s, d)
+        want = _tc(xgm, ctx, g)
+        assert _static_tc(xgm, ctx, g) == want  # first call on the device: set-up
+        free0, _ = torch.cuda.mem_get_info(0)
+        got = [_static_tc(xgm, ctx, g) for _ in range(3)]
+        free1, _ = torch.cuda.mem_get_info(0)
+        assert got == [want] * 3
+        assert free1 == free0, f"device free memory moved by {free0 - free1} bytes"
+        # a graph owned by another context is refused, not counted
+        other = xgm.Context(0)
+        try:
+            g_other = other.graph_from_edges(nv, s, d)
+            with pytest.raises(xgm.XgmError) as e:
+                _static_tc(xgm, ctx, g_other)
+            assert e.value.status == xgm.ERR_INVALID
+            g_other.close()
+        finally:
+            other.close()
     finally:
         ctx.close()

@@ -606,6 +606,31 @@ def ScSolver(g: Graph, pattern: str) -> int:
     return int(out.value)
 
 
+# ------------------------------------------------------------- trained schedule
+COSTMODEL_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "costmodel.json")
+
+
+def trained_schedule(ctx: "Context", path: Optional[str] = None) -> dict:
+    """count() keyword arguments for the learned schedule with the trained cost model
+    (costmodel.json: parameters, queue order and margin); {} when the file is absent
+    or was trained for another feature layout, i.e. the plain heuristic schedule."""
+    import json
+
+    path = path or COSTMODEL_PATH
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        spec = json.load(f)
+    if (spec.get("features") != MODEL_FEATURES or spec.get("variants") != NUM_VARIANTS
+            or len(spec.get("params", ())) != MODEL_PARAMS):
+        return {}
+    m = Model(ctx)
+    m.set_params(np.asarray(spec["params"], dtype=np.float32))
+    return {"policy": SCHED_LEARNED, "model": m,
+            "order_by_cost": int(spec.get("order_by_cost", 1)),
+            "margin": float(spec.get("margin", 0.0))}
+
+
 # ------------------------------------------------------------------ generators
 def _two(m: int):
     return np.empty(m, dtype=np.int32), np.empty(m, dtype=np.int32)

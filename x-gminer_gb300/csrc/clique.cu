@@ -27,6 +27,7 @@
 // edge sub-tasks, CTA tasks, wide-warp tasks (s <= 128), binary-search warp tasks,
 // eight-lane group tasks (s <= 8, four per warp), bucket-filtered search tasks, and
 // streaming warp tasks (s <= 32).
+#include <atomic>
 #include "clique.cuh"
 
 namespace xgm {
@@ -1479,12 +1480,19 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
 template <int K, int MODE>
 cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned long long* count,
                      uint32_t* err, Part part, int grid, cudaStream_t s, GOut o = GOut{}) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_clique<K, MODE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kCtaSmem);
+  // The shared-memory opt-in is a per-device function attribute: set it once per
+  // device that launches this instantiation (bit d of the mask; devices >= 64 set it
+  // on every launch).
+  static std::atomic<unsigned long long> attr_devices{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (!bit || !(attr_devices.load(std::memory_order_acquire) & bit)) {
+    e = cudaFuncSetAttribute(k_clique<K, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kCtaSmem);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_devices.fetch_or(bit, std::memory_order_acq_rel);
   }
   k_clique<K, MODE><<<grid, kCtaThreads, kCtaSmem, s>>>(g, t, q, count, err, part, o);
   return cudaGetLastError();

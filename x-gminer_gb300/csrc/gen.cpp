@@ -9,8 +9,9 @@
 // dedupe, drop self-loops, sort) in csr_build.cu.
 //
 // Every random draw is a pure function of (seed, stream, counter) through
-// splitmix64, so the integer-only generators (R-MAT, ER, BA) give the same
-// samples on x86-64 and aarch64 and for any thread count.
+// splitmix64, and the floating-point steps (Chung-Lu weights, BA batch sizes) avoid
+// libm (DetPow), so every generator gives the same samples on x86-64 and aarch64 and
+// for any thread count.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -41,11 +42,11 @@ inline uint64_t below(uint64_t x, uint64_t n) { return ((x >> 32) * n) >> 32; }
 inline double unit(uint64_t x) { return double(x >> 11) * (1.0 / 9007199254740992.0); }
 
 template <class F>
-void parallel_for(int64_t n, F f) {
+void parallel_for(int64_t n, F f, int64_t min_parallel = int64_t(1) << 16) {
   unsigned hw = std::thread::hardware_concurrency();
   int64_t nt = hw ? hw : 1;
   if (nt > 64) nt = 64;
-  if (n < (1 << 16)) nt = 1;
+  if (n < min_parallel) nt = 1;
   if (nt == 1) { f(0, n); return; }
   std::vector<std::thread> th;
   int64_t chunk = (n + nt - 1) / nt;
@@ -55,6 +56,51 @@ void parallel_for(int64_t n, F f) {
     th.emplace_back([=] { f(lo, hi); });
   }
   for (auto& x : th) x.join();
+}
+
+// pow / exp / log from correctly rounded IEEE operations only (+ - * / sqrt, frexp,
+// ldexp, floor): ln from the atanh series of the mantissa, exp from a Taylor series
+// after reduction by ln 2.  libm's versions may differ in the last bit between
+// platforms; these give the same bits on every host (host code is built without
+// floating-point contraction).
+struct DetPow {
+  static constexpr double kLn2 = 0.693147180559945309417232121458176568;
+  double inv[48];
+  DetPow() { for (int k = 1; k < 48; ++k) inv[k] = 1.0 / double(k); }
+  double log(double x) const {  // x > 0, finite
+    int e = 0;
+    double m = std::frexp(x, &e);  // m in [0.5, 1)
+    if (m < 0.70710678118654752440) { m = m * 2.0; e -= 1; }
+    const double s = (m - 1.0) / (m + 1.0), s2 = s * s;
+    double term = s, sum = 0.0;
+    for (int k = 1; k <= 25; k += 2) { sum = sum + term * inv[k]; term = term * s2; }
+    return 2.0 * sum + double(e) * kLn2;
+  }
+  double exp(double y) const {  // |y| < 700
+    const double kf = std::floor(y / kLn2 + 0.5);
+    const double r = y - kf * kLn2;
+    double term = 1.0, sum = 1.0;
+    for (int i = 1; i <= 18; ++i) { term = term * r * inv[i]; sum = sum + term; }
+    return std::ldexp(sum, int(kf));
+  }
+  double pow(double x, double y) const { return exp(y * log(x)); }
+};
+
+// Sum of f(i) over [0, n) in 64 fixed index chunks added in order (any thread count).
+template <class F>
+double det_sum(int64_t n, F f) {
+  const int64_t chunks = 64, step = (n + chunks - 1) / chunks;
+  std::vector<double> part(chunks, 0.0);
+  parallel_for(chunks, [&](int64_t lo, int64_t hi) {
+    for (int64_t c = lo; c < hi; ++c) {
+      double s = 0.0;
+      for (int64_t i = c * step; i < std::min(n, (c + 1) * step); ++i) s = s + f(i);
+      part[c] = s;
+    }
+  }, n >= (int64_t(1) << 16) ? 1 : chunks + 1);
+  double s = 0.0;
+  for (double p : part) s = s + p;
+  return s;
 }
 
 }  // namespace
@@ -111,7 +157,8 @@ int64_t xgm_gen_er(int64_t n, int64_t m, uint64_t seed, int32_t* src, int32_t* d
 
 // Chung-Lu: expected degree of vertex i is w_i = w_max * ((i + i0) / i0)^(-1/(gamma-1)),
 // with i0 chosen so that the mean weight is avg_deg.  m = n*avg_deg/2 endpoint pairs
-// are drawn with probability proportional to weight (inverse CDF).
+// are drawn with probability proportional to weight (inverse CDF).  The weights use
+// DetPow and det_sum, so the samples are the same on every host.
 int64_t xgm_gen_chung_lu(int64_t n, double gamma, double w_max, double avg_deg,
                          uint64_t seed, int32_t* src, int32_t* dst) {
   if (n <= 1 || n > (int64_t(1) << 31) - 1 || gamma <= 1.0 || w_max <= 0 || avg_deg <= 0)
@@ -119,22 +166,25 @@ int64_t xgm_gen_chung_lu(int64_t n, double gamma, double w_max, double avg_deg,
   const int64_t m = int64_t(double(n) * avg_deg / 2.0);
   if (!src || !dst) return m;
   const double beta = 1.0 / (gamma - 1.0);
-  auto mean_for = [&](double i0) {
-    double s = 0;
-    for (int64_t i = 0; i < n; ++i) s += w_max * std::pow((double(i) + i0) / i0, -beta);
-    return s / double(n);
+  const DetPow dp;
+  auto weight = [&](int64_t i, double i0) {
+    return w_max * dp.pow((double(i) + i0) / i0, -beta);
   };
   // mean weight grows with i0; bisect on log(i0).
   double lo = 1e-3, hi = double(n) * 1e3;
-  for (int it = 0; it < 80; ++it) {
-    double mid = std::sqrt(lo * hi);
-    if (mean_for(mid) < avg_deg) lo = mid; else hi = mid;
+  for (int it = 0; it < 64; ++it) {
+    const double mid = std::sqrt(lo * hi);
+    const double mean = det_sum(n, [&](int64_t i) { return weight(i, mid); }) / double(n);
+    if (mean < avg_deg) lo = mid; else hi = mid;
   }
   const double i0 = std::sqrt(lo * hi);
   std::vector<double> cdf(n);
+  parallel_for(n, [&](int64_t a, int64_t b) {
+    for (int64_t i = a; i < b; ++i) cdf[i] = weight(i, i0);
+  });
   double acc = 0;
   for (int64_t i = 0; i < n; ++i) {
-    acc += w_max * std::pow((double(i) + i0) / i0, -beta);
+    acc = acc + cdf[i];
     cdf[i] = acc;
   }
   const double total = acc;
@@ -204,12 +254,13 @@ int64_t xgm_gen_ba_batch(int num_graphs, int64_t n_lo, int64_t n_hi, int m_lo, i
     return -1;
   std::vector<int64_t> ns(num_graphs);
   std::vector<int> ms(num_graphs);
-  const double l0 = std::log(double(n_lo)), l1 = std::log(double(n_hi));
+  const DetPow dp;
+  const double l0 = dp.log(double(n_lo)), l1 = dp.log(double(n_hi));
   vtx_off[0] = 0;
   edge_off[0] = 0;
   for (int g = 0; g < num_graphs; ++g) {
     double u = unit(draw(seed, 5, 2 * uint64_t(g)));
-    int64_t n = int64_t(std::llround(std::exp(l0 + u * (l1 - l0))));
+    int64_t n = int64_t(std::floor(dp.exp(l0 + u * (l1 - l0)) + 0.5));
     n = std::min(std::max(n, n_lo), n_hi);
     int m = m_lo + int(below(draw(seed, 5, 2 * uint64_t(g) + 1), uint64_t(m_hi - m_lo + 1)));
     ns[g] = n;

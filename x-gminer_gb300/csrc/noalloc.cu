@@ -1,21 +1,25 @@
 // Triangle counting that allocates nothing: xgm_tc_solver_static.
 //
-// Some callers cannot allocate device memory at the moment they count: code running
-// while a CUDA stream is being captured into a graph, code inside a host framework
-// that owns all device memory through its own allocator, or a hot loop whose latency
-// budget has no room for an allocation.  This entry point serves them.  It runs the
-// same persistent counting kernel as xgm_tc_solver, but its task lists, list sizes,
-// queue heads and result live in one file-scope device array of fixed size instead of
-// memory the engine allocates per call.  The graph itself (built earlier through
-// xgm_graph_*) and the host result are the caller's input and output.
+// Some callers cannot allocate device memory at the moment they count: code inside a
+// host framework that owns all device memory through its own allocator (a second
+// allocator would fight it for the same HBM), or a hot loop whose latency budget has
+// no room for a cudaMalloc and the device-wide synchronisation it can bring.  This
+// entry point serves them.  It runs the same persistent counting kernel as
+// xgm_tc_solver, but its task lists, list sizes, queue heads and result live in one
+// file-scope device array of fixed size instead of memory the engine allocates per
+// call.  The graph itself (built earlier through xgm_graph_*) and the host result are
+// the caller's input and output.
 //
 // The array is kStaticBytes (48 MiB) and holds the task lists of graphs of up to
 // kStaticMaxVertices (2^21) vertices; larger graphs are rejected with
 // XGM_ERR_UNSUPPORTED.  Every GPU that loads the library keeps the array until the
-// process exits.  All calls share it, so calls whose GPU work overlaps (two streams,
-// two threads) race and must be serialised by the caller.  The first call on a device
-// looks up the array's device address (cudaGetSymbolAddress) with that device
-// current; make that first call before any stream capture.
+// process exits.  All calls share it and it keeps the last call's contents, so each
+// call clears its scalars first, and calls whose GPU work overlaps (two streams, two
+// threads) race and must be serialised by the caller.  The first call on a device
+// does the set-up: it looks up the array's device address (cudaGetSymbolAddress)
+// with that device current; make that first call before any stream capture.  The
+// call waits for its stream to finish and returns the count; the caller's current
+// device is left as it was.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -118,15 +122,47 @@ xgm_status static_scratch(int device, unsigned char** out) {
 
 using namespace xgm;
 
+namespace {
+
+xgm_status tc_static(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total);
+
+// Makes ctx's device current for the call and puts the caller's device back after it.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t enter(int device) {
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e != cudaSuccess) { prev = -1; return e; }
+    return prev == device ? cudaSuccess : cudaSetDevice(device);
+  }
+  ~DeviceScope() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
 extern "C" xgm_status xgm_tc_solver_static(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total) {
   if (!ctx || !g || !total) return XGM_ERR_INVALID;
-  const DevGraph& G = g->g;
-  if (G.nv > kStaticMaxVertices) {
+  if (g->ctx != ctx) {
+    set_thread_error("xgm_tc_solver_static: the graph belongs to another context");
+    return finish_status(ctx, XGM_ERR_INVALID);
+  }
+  if (g->g.nv > kStaticMaxVertices) {
     set_thread_error("xgm_tc_solver_static holds graphs of up to 2^21 vertices (48 MiB "
                      "static scratch); use xgm_tc_solver for larger graphs");
     return finish_status(ctx, XGM_ERR_UNSUPPORTED);
   }
-  XGM_CUDA_TRY(cudaSetDevice(ctx->device));
+  DeviceScope scope;
+  const cudaError_t e = scope.enter(ctx->device);
+  if (e != cudaSuccess) return finish_status(ctx, cuda_fail(e, "cudaSetDevice", __FILE__, __LINE__));
+  return tc_static(ctx, g, total);
+}
+
+namespace {
+
+xgm_status tc_static(xgm_ctx* ctx, const xgm_graph* g, uint64_t* total) {
+  const DevGraph& G = g->g;
   unsigned char* base = nullptr;
   xgm_status st = static_scratch(ctx->device, &base);
   if (st != XGM_OK) return finish_status(ctx, st);
@@ -161,3 +197,5 @@ extern "C" xgm_status xgm_tc_solver_static(xgm_ctx* ctx, const xgm_graph* g, uin
   *total = h.count;
   return XGM_OK;
 }
+
+}  // namespace
