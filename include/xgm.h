@@ -237,6 +237,11 @@ typedef struct {
   int group_max;          /* heuristic: out-degree <= group_max -> GROUP (0: none; <= 8) */
   float margin;           /* learned: predicted log2-cost saving a task needs to leave the
                              heuristic's variant (0: default 0.2) */
+  int hub_max;            /* 3- to 5-clique counts: a hub task (out-degree above the CTA
+                             capacity, 1024) of out-degree <= hub_max runs whole in the hub kernel
+                             (one 1024-thread CTA, shared-memory bitmap) instead of being
+                             split into one sub-task per out-edge (0: default 1536, the
+                             largest it holds; -1: every hub split) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };

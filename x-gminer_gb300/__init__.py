@@ -95,7 +95,7 @@ class Sched(C.Structure):
                 ("warp_max", C.c_int), ("cta_max", C.c_int), ("order_by_cost", C.c_int),
                 ("table", C.c_void_p), ("flags", C.c_int), ("wide_max", C.c_int),
                 ("search_max", C.c_int), ("bucket_max", C.c_int), ("group_max", C.c_int),
-                ("margin", C.c_float)]
+                ("margin", C.c_float), ("hub_max", C.c_int)]
 
 
 class TuneResult(C.Structure):
@@ -268,10 +268,11 @@ class Context:
     @staticmethod
     def _sched(policy=SCHED_HEURISTIC, variant=0, model=None, warp_max=0, cta_max=0,
                order_by_cost=1, table=None, flags=0, wide_max=0, search_max=0, bucket_max=0,
-               group_max=0, margin=0.0):
+               group_max=0, margin=0.0, hub_max=0):
         sp = Sched(policy, variant, model._h if model is not None else None, warp_max, cta_max,
                    order_by_cost, C.cast(C.pointer(table), C.c_void_p) if table is not None
-                   else None, flags, wide_max, search_max, bucket_max, group_max, margin)
+                   else None, flags, wide_max, search_max, bucket_max, group_max, margin,
+                   hub_max)
         sp._keep = table  # keep the table alive with the struct
         return sp
 
@@ -279,11 +280,12 @@ class Context:
               model: Optional["Model"] = None, warp_max: int = 0, cta_max: int = 0,
               order_by_cost: int = 1, table: Optional[TuneTable] = None,
               wide_max: int = 0, search_max: int = 0, bucket_max: int = 0,
-              group_max: int = 0, margin: float = 0.0, with_stats: bool = False):
+              group_max: int = 0, margin: float = 0.0, hub_max: int = 0,
+              with_stats: bool = False):
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
         sp = self._sched(policy, variant, model, warp_max, cta_max, order_by_cost, table,
                          wide_max=wide_max, search_max=search_max, bucket_max=bucket_max,
-                         group_max=group_max, margin=margin)
+                         group_max=group_max, margin=margin, hub_max=hub_max)
         out = C.c_uint64()
         st = Stats()
         _check(lib().xgm_count(self._h, graph._h, plan._h, C.byref(sp), C.byref(out),

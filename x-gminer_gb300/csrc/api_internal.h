@@ -104,8 +104,9 @@ xgm_status count_program(xgm_ctx* ctx, const DevGraph& g, const Prog& p, uint64_
                          xgm_stats& st);
 void program_buffers_free(xgm_ctx* ctx);
 // k_feat: clique size the learned model's features describe (default k).
+// hub: the launch is a clique count that runs the hub kernel (sp.hub_max applies).
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
-                         cudaStream_t s, int k_feat = 0);
+                         cudaStream_t s, int k_feat = 0, bool hub = false);
 bool sched_may_bucket(const xgm_sched& sp);  // the policy can assign the BUCKET variant
 int ensure_clique_grid(xgm_ctx* ctx);
 int match_pattern(const xgm_plan_desc* d);  // builtin id, 0 unsupported, -1 malformed

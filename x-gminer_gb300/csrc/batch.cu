@@ -254,7 +254,7 @@ xgm_status batch_sequence(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P,
   }
   if (sl.k5 >= 0) {
     XGM_CUDA_TRY(cudaMemsetAsync(&b->d_sc->q, 0, sizeof(QueueHeads), s));
-    xgm_status r = schedule_into(b->tb, g, 5, sp, s);
+    xgm_status r = schedule_into(b->tb, g, 5, sp, s, 0, true);
     if (r != XGM_OK) return r;
     GOut o{g.gid, b->d_out, P, sl.k5, -1};
     XGM_CUDA_TRY(launch_clique(5, view, b->tb.lists(false), &b->d_sc->q, nullptr, &b->d_sc->err,

@@ -34,23 +34,48 @@ namespace xgm {
 
 namespace {
 
-// ---------------------------------------------------------------- smem layout
-// CTA region (bytes): lb[kCtaCap] i64 | S[kCtaCap] i32 | pre[kCtaCap+8] i32 |
-//                     hkey[kHashSize] i32 | hval[kHashSize] u16 | cnt[kCtaCap] u32 |
-//                     rows[tri_words(kCtaCap)] u32 | misc[16] i64
-constexpr int kOffLb = 0;
-constexpr int kOffS = kOffLb + 8 * kCtaCap;
-constexpr int kOffPre = kOffS + 4 * kCtaCap;
-constexpr int kOffHkey = kOffPre + 4 * (kCtaCap + 8);
-constexpr int kOffHval = kOffHkey + 4 * kHashSize;
-constexpr int kOffCnt = kOffHval + 2 * kHashSize;
-constexpr int kOffRows = kOffCnt + 4 * kCtaCap;
-constexpr int kRowsWords = 16896;  // tri_words(1024)
-constexpr int kBloomWords = 512;  // 16 Kbit membership pre-filter of the local set
-constexpr int kOffBloom = kOffRows + 4 * kRowsWords;
-constexpr int kOffRowOff = kOffBloom + 4 * kBloomWords;  // int32[kCtaCap] row offsets
-constexpr int kOffMisc = kOffRowOff + 4 * kCtaCap;
-constexpr int kCtaSmem = kOffMisc + 8 * 16;
+// ---------------------------------------------------------------- CTA shapes
+// A CTA task holds its local set S in shared memory.  Layout (bytes):
+//   lb[cap] i64 | S[cap + 4] i32 | pre[cap + 8] i32 | hkey[hash] i32 | hval[hash] u16 |
+//   cnt[cap] u32 | rows[tri_words(cap)] u32 | bloom[512] u32 | roff[cap] i32 | misc[32] i64
+// S has four words of slack: a bulk copy lands a list at its own 16-byte phase.
+// CtaMain is the persistent counting kernel's CTA (512 threads, 2 CTAs per SM, local
+// sets of up to 1024); CtaHub is the hub kernel's (1024 threads, 1 CTA per SM, up to
+// 1536: hub vertices just above the main CTA's capacity run whole instead of split).
+constexpr int tri_words_c(int s) {
+  return s * ((s + 31) >> 5) - (16 * (s >> 5) * ((s >> 5) - 1) + (s & 31) * (s >> 5));
+}
+template <int NT, int CAP, int HBITS>
+struct CtaShape {
+  static constexpr int kThreads = NT, kWarps = NT / 32, kCap = CAP;
+  static constexpr int kHashBits = HBITS, kHash = 1 << HBITS;
+  static constexpr int kBloomWords = 512;  // 16 Kbit membership pre-filter of the local set
+  static constexpr int kRowsWords = tri_words_c(CAP);
+  static constexpr int kOffLb = 0;
+  static constexpr int kOffS = kOffLb + 8 * CAP;
+  static constexpr int kOffPre = kOffS + 4 * (CAP + 4);
+  static constexpr int kOffHkey = kOffPre + 4 * (CAP + 8);
+  static constexpr int kOffHval = kOffHkey + 4 * kHash;
+  static constexpr int kOffCnt = kOffHval + 2 * kHash;
+  static constexpr int kOffRows = kOffCnt + 4 * CAP;
+  static constexpr int kOffBloom = kOffRows + 4 * kRowsWords;
+  static constexpr int kOffRowOff = kOffBloom + 4 * kBloomWords;  // int32[cap] row offsets
+  static constexpr int kOffMisc = kOffRowOff + 4 * CAP;
+  static constexpr int kOffBar = kOffMisc + 8 * 31;  // mbarrier of the bulk copies
+  static constexpr int kSmem = kOffMisc + 8 * 32;
+  static_assert(2 * NT >= CAP, "the length scan gives each thread two members");
+  static_assert(kHash >= 2 * CAP, "hash load factor at most one half");
+  static_assert(kOffS % 16 == 0 && kOffMisc % 8 == 0 && 4 * kWarps <= 8 * 31,
+                "aligned regions; warp totals below the barrier");
+};
+using CtaMain = CtaShape<kCtaThreads, kCtaCap, 11>;
+using CtaHub = CtaShape<kHubThreads, kHubCap, 12>;
+static_assert(CtaMain::kRowsWords == 16896 && CtaMain::kHash == kHashSize, "main CTA shape");
+constexpr int kOffS = CtaMain::kOffS;
+constexpr int kOffMisc = CtaMain::kOffMisc;
+constexpr int kCtaSmem = CtaMain::kSmem;
+constexpr int kHubSmem = CtaHub::kSmem;
+static_assert(kHubSmem <= 227 * 1024, "hub CTA fits one SM's shared memory");
 constexpr int kClipMin = 96;    // lists longer than this are clipped at max(S)
 constexpr int kClipLoMin = 8;   // lists longer than this start at the next member of S
 
@@ -93,8 +118,9 @@ static_assert(kOffWarpRegion + sizeof(WarpSmem) * kCtaWarps <= kCtaSmem, "warp r
 static_assert(sizeof(WideSmem) % 16 == 0, "wide regions stay 16-byte aligned");
 static_assert(kWarpBloomWords == 32 && kWideBloomWords == 64, "filters are cleared lane-wise");
 
+template <class Sh = CtaMain>
 __device__ __forceinline__ uint32_t hash_slot(int32_t x) {
-  return ((uint32_t)x * 2654435761u) >> (32 - 11);  // kHashSize = 2^11
+  return ((uint32_t)x * 2654435761u) >> (32 - Sh::kHashBits);
 }
 
 // Bloom bit of x (independent of hash_slot's multiplier): 14 bits for the CTA filter,
@@ -103,21 +129,23 @@ __device__ __forceinline__ uint32_t bloom_bit(int32_t x) {
   return ((uint32_t)x * 0x85EBCA6Bu) >> 18;
 }
 
+template <class Sh = CtaMain>
 __device__ __forceinline__ int hash_find(const int32_t* hkey, const uint16_t* hval, int32_t x) {
-  uint32_t slot = hash_slot(x);
+  uint32_t slot = hash_slot<Sh>(x);
 #pragma unroll 1
-  for (int probe = 0; probe < kHashSize; ++probe) {
+  for (int probe = 0; probe < Sh::kHash; ++probe) {
     int32_t k = hkey[slot];
     if (k == x) return hval[slot];
     if (k == -1) return -1;
-    slot = (slot + 1) & (kHashSize - 1);
+    slot = (slot + 1) & (Sh::kHash - 1);
   }
   return -1;
 }
 
-// Block-wide exclusive scan of values v[i], i < n <= kCtaCap, into pre[0..n]; CTA-wide.
+// Block-wide exclusive scan of values v[i], i < n <= Sh::kCap, into pre[0..n]; CTA-wide.
+template <class Sh = CtaMain>
 __device__ void cta_scan_lengths(int32_t* pre, int n, int32_t* warp_tot) {
-  // each thread owns items [tid*2, tid*2+1] (kCtaCap = 2 * kCtaThreads)
+  // each thread owns items [tid*2, tid*2+1] (Sh::kCap <= 2 * Sh::kThreads)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int a = 2 * tid < n ? pre[2 * tid] : 0;
   int b = 2 * tid + 1 < n ? pre[2 * tid + 1] : 0;
@@ -130,13 +158,13 @@ __device__ void cta_scan_lengths(int32_t* pre, int n, int32_t* warp_tot) {
   if (lane == 31) warp_tot[warp] = inc;
   __syncthreads();
   if (warp == 0) {
-    int w = lane < kCtaWarps ? warp_tot[lane] : 0, wi = w;
+    int w = lane < Sh::kWarps ? warp_tot[lane] : 0, wi = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(kFull, wi, o);
       if (lane >= o) wi += y;
     }
-    if (lane < kCtaWarps) warp_tot[lane] = wi - w;
+    if (lane < Sh::kWarps) warp_tot[lane] = wi - w;
   }
   __syncthreads();
   int ex = warp_tot[warp] + inc - s;
@@ -161,14 +189,14 @@ enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 // at tri_row_off(32 qj, W) + (j % 32)(W - qj): the walk takes one base pointer per word
 // and reaches row j's word w with one multiply-add (no per-member offset load), and adds
 // the word's popcounts in 32 bits.
-template <int Q, bool WGT>
+template <int Q, bool WGT, class Sh = CtaMain>
 __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, const int32_t* pre,
                                                    const int32_t* roff, int W = 0) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = n;
   if (W == 0) W = (n + 31) >> 5;
   uint64_t acc = 0;
-  for (int i = warp; i < s; i += kCtaWarps) {
+  for (int i = warp; i < s; i += Sh::kWarps) {
     const int qi = i >> 5, nwi = W - qi;
     const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
     const int w = qi + lane;
@@ -235,7 +263,7 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
 // warp has work (__any_sync), so all 32 lanes meet at every warp-synchronous call.
 // Row offsets of the members of one word come from one base pointer, as in
 // cta_count_rows.
-template <int Q, int G>
+template <int Q, int G, class Sh = CtaMain>
 __device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff, int W,
                                        int row_lo, int row_hi) {
   static_assert(Q == 3 || Q == 4, "grouped rows cover the 4- and 5-clique count phases");
@@ -244,7 +272,7 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane % G, gbase = lane - sub;
   uint64_t acc = 0;
-  for (int i0 = row_lo + warp * kGroups; i0 < row_hi; i0 += kCtaWarps * kGroups) {
+  for (int i0 = row_lo + warp * kGroups; i0 < row_hi; i0 += Sh::kWarps * kGroups) {
     const int i = i0 + lane / G;
     const bool live = i < row_hi;
     const int qi = live ? (i >> 5) : 0, nwi = W - qi;
@@ -296,11 +324,72 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff
   return acc;
 }
 
+// cta_count_rows (unweighted, Q = 3 or 4) for rows spanning up to 64 words (local sets
+// above 1024, the hub CTA): lane holds words qi + lane and qi + lane + 32 of row i, and
+// each enumeration runs over the two halves in turn.
+template <int Q, class Sh>
+__device__ uint64_t cta_count_rows2(const uint32_t* rows, int nrows, const int32_t* roff, int W) {
+  static_assert(Q == 3 || Q == 4, "two-word rows cover the 4- and 5-clique count phases");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t acc = 0;
+  for (int i = warp; i < nrows; i += Sh::kWarps) {
+    const int qi = i >> 5, nwi = W - qi;
+    const uint32_t wa = lane < nwi ? rows[roff[i] + lane] : 0u;
+    const uint32_t wb = lane + 32 < nwi ? rows[roff[i] + lane + 32] : 0u;
+    const int wA = qi + lane, wB = wA + 32;
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      unsigned nz = __ballot_sync(kFull, (half ? wb : wa) != 0u);
+      while (nz) {
+        const int src = __ffs(nz) - 1;
+        nz &= nz - 1;
+        uint32_t bits = __shfl_sync(kFull, half ? wb : wa, src);
+        const int qj = qi + src + 32 * half;
+        const bool onA = lane < nwi && wA >= qj, onB = lane + 32 < nwi && wB >= qj;
+        const uint32_t* Bj = rows + tri_row_off(qj << 5, W);  // + b (W - qj) + (w - qj)
+        const int sj = W - qj;
+        while (bits) {
+          const int b = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const uint32_t ma = onA ? (wa & Bj[b * sj + (wA - qj)]) : 0u;
+          const uint32_t mb = onB ? (wb & Bj[b * sj + (wB - qj)]) : 0u;
+          if constexpr (Q == 3) {
+            acc += (uint32_t)(__popc(ma) + __popc(mb));
+          } else {
+            uint32_t part = 0;
+#pragma unroll 1
+            for (int h2 = 0; h2 < 2; ++h2) {
+              unsigned nz2 = __ballot_sync(kFull, (h2 ? mb : ma) != 0u);
+              while (nz2) {
+                const int src2 = __ffs(nz2) - 1;
+                nz2 &= nz2 - 1;
+                uint32_t bits2 = __shfl_sync(kFull, h2 ? mb : ma, src2);
+                const int ql = qi + src2 + 32 * h2;
+                const bool onA2 = ma != 0u && wA >= ql, onB2 = mb != 0u && wB >= ql;
+                const uint32_t* Bl = rows + tri_row_off(ql << 5, W);
+                const int sl = W - ql;
+                while (bits2) {
+                  const int b2 = __ffs(bits2) - 1;
+                  bits2 &= bits2 - 1;
+                  if (onA2) part += __popc(ma & Bl[b2 * sl + (wA - ql)]);
+                  if (onB2) part += __popc(mb & Bl[b2 * sl + (wB - ql)]);
+                }
+              }
+            }
+            acc += part;
+          }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
 // The 4- and 5-clique count phases (unweighted) with the rows split into tiers by how
 // many words they span (row i spans W - floor(i/32)): rows spanning more than 16 words
 // keep the full-warp walk of cta_count_rows, the others run 2, 4 or 8 to a warp
 // (count_rows_grouped) so no lane idles on words past its row's end.
-template <int Q>
+template <int Q, class Sh = CtaMain>
 __device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int32_t* pre,
                                           const int32_t* roff) {
   const int W = (s + 31) >> 5;
@@ -308,10 +397,14 @@ __device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int
   auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
   const int r16 = first(16), r8 = first(8), r4 = first(4);
   uint64_t acc = 0;
-  if (r16 > 0) acc += cta_count_rows<Q, false>(rows, r16, pre, roff, W);
-  acc += count_rows_grouped<Q, 16>(rows, roff, W, r16, r8);
-  acc += count_rows_grouped<Q, 8>(rows, roff, W, r8, r4);
-  acc += count_rows_grouped<Q, 4>(rows, roff, W, r4, s);
+  if constexpr (Sh::kCap > 1024) {  // rows may span more than 32 words
+    if (r16 > 0) acc += cta_count_rows2<Q, Sh>(rows, r16, roff, W);
+  } else {
+    if (r16 > 0) acc += cta_count_rows<Q, false, Sh>(rows, r16, pre, roff, W);
+  }
+  acc += count_rows_grouped<Q, 16, Sh>(rows, roff, W, r16, r8);
+  acc += count_rows_grouped<Q, 8, Sh>(rows, roff, W, r8, r4);
+  acc += count_rows_grouped<Q, 4, Sh>(rows, roff, W, r4, s);
   return acc;
 }
 
@@ -372,14 +465,14 @@ __device__ uint64_t rows_deep_grouped(const uint32_t* rows, const int32_t* roff,
   }
 }
 
-template <int Q, int G>
+template <int Q, int G, class Sh = CtaMain>
 __device__ uint64_t count_deep_grouped(const uint32_t* rows, const int32_t* roff, int W,
                                        int row_lo, int row_hi) {
   constexpr int kGroups = 32 / G;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane % G, gbase = lane - sub;
   uint64_t acc = 0;
-  for (int i0 = row_lo + warp * kGroups; i0 < row_hi; i0 += kCtaWarps * kGroups) {
+  for (int i0 = row_lo + warp * kGroups; i0 < row_hi; i0 += Sh::kWarps * kGroups) {
     const int i = i0 + lane / G;
     const bool live = i < row_hi;
     const int qi = live ? (i >> 5) : 0, nwi = W - qi;
@@ -390,21 +483,21 @@ __device__ uint64_t count_deep_grouped(const uint32_t* rows, const int32_t* roff
 }
 
 // Q-cliques for Q >= 5, rows tiered by the words they span as in cta_count_rows_tiered.
-template <int Q>
+template <int Q, class Sh = CtaMain>
 __device__ uint64_t cta_count_deep(const uint32_t* rows, int s, const int32_t* roff) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = (s + 31) >> 5;
   auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
   const int r16 = first(16), r8 = first(8), r4 = first(4);
   uint64_t acc = 0;
-  for (int i = warp; i < r16; i += kCtaWarps) {
+  for (int i = warp; i < r16; i += Sh::kWarps) {
     const int qi = i >> 5, nwi = W - qi;
     const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
     acc += rows_deep<Q - 1>(rows, roff, wi, qi + lane, qi);
   }
-  acc += count_deep_grouped<Q, 16>(rows, roff, W, r16, r8);
-  acc += count_deep_grouped<Q, 8>(rows, roff, W, r8, r4);
-  acc += count_deep_grouped<Q, 4>(rows, roff, W, r4, s);
+  acc += count_deep_grouped<Q, 16, Sh>(rows, roff, W, r16, r8);
+  acc += count_deep_grouped<Q, 8, Sh>(rows, roff, W, r8, r4);
+  acc += count_deep_grouped<Q, 4, Sh>(rows, roff, W, r4, s);
   return acc;
 }
 
@@ -459,48 +552,48 @@ struct Part {
 // sbase): every local edge (i, j) is the triangle (root, S[i], S[j]); it is credited to
 // vertices S[i], S[j] and edges (root,S[i]), (root,S[j]), (S[i],S[j]).  The root's own
 // credit is the returned count.
-template <int Q, int MODE>
+template <int Q, int MODE, class Sh = CtaMain>
 __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long long sbase,
-                              uint64_t* q2out = nullptr) {
+                              uint64_t* q2out = nullptr, int s_off = 0) {
   constexpr bool MULTI = MODE == kModeMulti;  // Q == 3: also local edges + participation
   constexpr bool PART = MODE == kModePart || MULTI;
   constexpr bool WGT = MODE == kModeWeight;
-  int32_t* S = (int32_t*)(sm + kOffS);
+  int32_t* S = (int32_t*)(sm + Sh::kOffS) + s_off;
   if (Q == 1) {
     if (!WGT) return (uint64_t)s;  // same value in every thread
     uint64_t a = 0;                // per-thread partial sums
-    for (int i = threadIdx.x; i < s; i += kCtaThreads) {
+    for (int i = threadIdx.x; i < s; i += Sh::kThreads) {
       const longlong2 d = ldg_ll2(g.dptr + S[i]);
       a += (uint64_t)(d.y - d.x);
     }
     return a;
   }
-  long long* lb = (long long*)(sm + kOffLb);
-  int32_t* pre = (int32_t*)(sm + kOffPre);
-  int32_t* hkey = (int32_t*)(sm + kOffHkey);
-  uint16_t* hval = (uint16_t*)(sm + kOffHval);
-  uint32_t* cnt = (uint32_t*)(sm + kOffCnt);
-  uint32_t* rows = (uint32_t*)(sm + kOffRows);
-  int32_t* wtot = (int32_t*)(sm + kOffMisc);
+  long long* lb = (long long*)(sm + Sh::kOffLb);
+  int32_t* pre = (int32_t*)(sm + Sh::kOffPre);
+  int32_t* hkey = (int32_t*)(sm + Sh::kOffHkey);
+  uint16_t* hval = (uint16_t*)(sm + Sh::kOffHval);
+  uint32_t* cnt = (uint32_t*)(sm + Sh::kOffCnt);
+  uint32_t* rows = (uint32_t*)(sm + Sh::kOffRows);
+  int32_t* wtot = (int32_t*)(sm + Sh::kOffMisc);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = (s + 31) >> 5;
 
-  uint32_t* bloom = (uint32_t*)(sm + kOffBloom);
-  int32_t* roff = (int32_t*)(sm + kOffRowOff);  // word offset of row i (triangular layout)
+  uint32_t* bloom = (uint32_t*)(sm + Sh::kOffBloom);
+  int32_t* roff = (int32_t*)(sm + Sh::kOffRowOff);  // word offset of row i (triangular layout)
   if (Q >= 3)
-    for (int i = tid; i < s; i += kCtaThreads) roff[i] = tri_row_off(i, W);
-  for (int h = tid; h < kHashSize; h += kCtaThreads) hkey[h] = -1;
-  for (int h = tid; h < kBloomWords; h += kCtaThreads) bloom[h] = 0u;
+    for (int i = tid; i < s; i += Sh::kThreads) roff[i] = tri_row_off(i, W);
+  for (int h = tid; h < Sh::kHash; h += Sh::kThreads) hkey[h] = -1;
+  for (int h = tid; h < Sh::kBloomWords; h += Sh::kThreads) bloom[h] = 0u;
   if (Q >= 3)
-    for (int x = tid; x < tri_words(s); x += kCtaThreads) rows[x] = 0u;
+    for (int x = tid; x < tri_words(s); x += Sh::kThreads) rows[x] = 0u;
   if (PART)
-    for (int i = tid; i < s; i += kCtaThreads) cnt[i] = 0u;
+    for (int i = tid; i < s; i += Sh::kThreads) cnt[i] = 0u;
   // Only members S[i+1] .. max(S) can hit in row i: each list starts at the first
   // element >= S[i+1] and long lists end at max(S) (binary searches in the sorted global
   // row), so the walk streams no element that cannot match.  At R-MAT scale 22 the
   // start clip removes ~58 % of the CTA tasks' elements, the end clip ~0.4 %.
   const int32_t smax0 = S[s - 1];
-  for (int i = tid; i < s; i += kCtaThreads) {
+  for (int i = tid; i < s; i += Sh::kThreads) {
     const longlong2 d = ldg_ll2(g.dptr + S[i]);
     long long lo = d.x, hi = d.y;
     // (not in weighted mode: its weights are the full out-degrees pre[j+1] - pre[j])
@@ -514,17 +607,17 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
     pre[i] = (int32_t)(hi - lo);
   }
   __syncthreads();
-  for (int i = tid; i < s; i += kCtaThreads) {
+  for (int i = tid; i < s; i += Sh::kThreads) {
     const int32_t x = S[i];
-    uint32_t slot = hash_slot(x);
-    // s <= kCtaCap < kHashSize members: an empty slot always exists
-    for (int probe = 0; probe < kHashSize && atomicCAS(&hkey[slot], -1, x) != -1; ++probe)
-      slot = (slot + 1) & (kHashSize - 1);
+    uint32_t slot = hash_slot<Sh>(x);
+    // s <= Sh::kCap < Sh::kHash members: an empty slot always exists
+    for (int probe = 0; probe < Sh::kHash && atomicCAS(&hkey[slot], -1, x) != -1; ++probe)
+      slot = (slot + 1) & (Sh::kHash - 1);
     hval[slot] = (uint16_t)i;
     const uint32_t b = bloom_bit(x);
     atomicOr(&bloom[b >> 5], 1u << (b & 31));
   }
-  cta_scan_lengths(pre, s, wtot);  // ends with __syncthreads
+  cta_scan_lengths<Sh>(pre, s, wtot);  // ends with __syncthreads
   const int total = pre[s];
   const int32_t smax = S[s - 1];
   uint64_t acc = 0, q2 = 0;
@@ -532,18 +625,22 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   // elements, lanes contiguous within a chunk so row reads are coalesced.  Each lane
   // keeps its segment's base in registers, issues four loads before using them, and
   // rejects most non-members with one Bloom-filter probe before the hash lookup.
-  for (int c = warp; c * 256 < total; c += kCtaWarps) {
+  for (int c = warp; c * 256 < total; c += Sh::kWarps) {
     const int kb = c * 256 + lane;
     int i;
     {  // segment of the chunk start (largest i < s with pre[i] <= c * 256): a two-round
-       // 32-way search by the warp (s <= 1024), then each lane steps to its own segment
+       // 32-way search by the warp (strides kR1 then kR1 / 32), then each lane steps to
+       // its own segment
+      constexpr int kR1 = Sh::kCap <= 1024 ? 32 : 64;
+      static_assert(32 * kR1 >= Sh::kCap, "two search rounds cover the local set");
+      constexpr int kR2 = kR1 / 32;
       const int k0 = c * 256;
-      const int c1 = lane << 5;
+      const int c1 = lane * kR1;
       const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
       const int r1 = 31 - __clz(b1);  // b1 has bit 0: pre[0] = 0 <= k0
-      const int c2 = (r1 << 5) + lane;
+      const int c2 = r1 * kR1 + lane * kR2;
       const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
-      i = (r1 << 5) + 31 - __clz(b2);
+      i = r1 * kR1 + (31 - __clz(b2)) * kR2;
       while (i + 1 < s && pre[i + 1] <= kb) ++i;  // stays below s past the end
     }
     int seg_end = pre[i + 1];
@@ -576,7 +673,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
         if (x > smax) continue;
         const uint32_t b = bloom_bit(x);
         if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
-        const int j = hash_find(hkey, hval, x);
+        const int j = hash_find<Sh>(hkey, hval, x);
         if (j < 0) continue;
         const int ii = iv[t];
         if (Q == 2) {
@@ -601,16 +698,16 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   if (MULTI) *q2out = q2;
   __syncthreads();
   if (PART) {
-    for (int i = tid; i < s; i += kCtaThreads)
+    for (int i = tid; i < s; i += Sh::kThreads)
       if (cnt[i]) {
         atomicAdd(&part.v[S[i]], (unsigned long long)cnt[i]);
         atomicAdd(&part.e[sbase + i], cnt[i]);
       }
   }
-  if (Q == 3) acc = WGT ? cta_count_rows<3, true>(rows, s, pre, roff)
-                        : cta_count_rows_tiered<3>(rows, s, pre, roff);
-  if (Q == 4) acc = cta_count_rows_tiered<4>(rows, s, pre, roff);
-  if constexpr (Q >= 5) acc = cta_count_deep<Q>(rows, s, roff);
+  if (Q == 3) acc = WGT ? cta_count_rows<3, true, Sh>(rows, s, pre, roff)
+                        : cta_count_rows_tiered<3, Sh>(rows, s, pre, roff);
+  if (Q == 4) acc = cta_count_rows_tiered<4, Sh>(rows, s, pre, roff);
+  if constexpr (Q >= 5) acc = cta_count_deep<Q, Sh>(rows, s, roff);
   return acc;
 }
 
@@ -1522,23 +1619,143 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
   }
 }
 
-template <int K, int MODE>
-cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned long long* count,
-                     uint32_t* err, Part part, int grid, cudaStream_t s, GOut o = GOut{}) {
-  // The shared-memory opt-in is a per-device function attribute: set it once per
-  // device that launches this instantiation (bit d of the mask; devices >= 64 set it
-  // on every launch).
-  static std::atomic<unsigned long long> attr_devices{0};
+// ------------------------------------------------------------------ hub kernel
+// Bulk copy (TMA, cp.async.bulk) global -> this CTA's shared memory, completing on an
+// mbarrier; both addresses and the size are multiples of 16 bytes.
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+// Bounded wait for the phase `parity` of the barrier (try_wait suspends the thread for
+// a while each call): false when the limit ran out.
+constexpr int kBarSpin = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < kBarSpin; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Hub vertices just above the main CTA's capacity (kCtaCap < s <= t.hub_max <= kHubCap)
+// run whole: one 1024-thread CTA per SM holds N+(v0) and the bitmap of the DAG induced
+// on it (cta_local on the CtaHub layout, ~209 KB of shared memory) instead of splitting
+// the hub into s edge sub-tasks that each intersect two global lists (the role of
+// GLUMIN's per-hub LUT, glumin_GM_solver.cu:490-503, codegen_bitmap.cuh:884-968).  The
+// hub's list is staged by one bulk copy (TMA) from its 16-byte-aligned start; the first
+// member sits `off` words in.  Count mode, k <= 5 only (otherwise every hub is split).
+template <int K>
+__global__ void __launch_bounds__(kHubThreads, 1)
+    k_clique_hub(GView g, TaskLists t, QueueHeads* q, unsigned long long* count, uint32_t* err,
+                 GOut o) {
+  static_assert(K >= 3 && K <= 5, "the hub CTA counts up to 5-cliques (rows of <= 64 words)");
+  extern __shared__ __align__(128) char sm[];
+  __shared__ long long task_s;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(sm + CtaHub::kOffBar);
+  const uint32_t sdst = (uint32_t)__cvta_generic_to_shared(sm + CtaHub::kOffS);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  uint64_t acc = 0;
+  const long long n_hubs = t.n[3];
+  for (;;) {
+    if (tid == 0) task_s = (long long)atomicAdd(&q->hub, 1ull);
+    __syncthreads();
+    const long long ti = task_s;
+    __syncthreads();
+    if (ti >= n_hubs) break;
+    const int32_t v0 = t.split_v[ti];
+    const longlong2 d0 = ldg_ll2(g.dptr + v0);
+    const int s = (int)(d0.y - d0.x);
+    if (s <= kCtaCap || s > t.hub_max) continue;  // split sub-tasks (main kernel) or none
+    const long long a0 = d0.x & ~3ll;
+    const int off = (int)(d0.x - a0);
+    const uint32_t bytes = (uint32_t)(((off + s) * 4 + 15) & ~15);  // <= 4 (kHubCap + 4)
+    if (tid == 0) {
+      // the previous task's generic-proxy accesses to S come before this async write
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(bar, bytes);
+      bulk_g2s(sdst, g.col + a0, bytes, bar);  // col has 16 bytes of slack at its end
+    }
+    const bool ok = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(ok)) {  // the copy did not land: report it, stop this CTA
+      if (tid == 0) {
+        atomicOr(err, ERR_TIMEOUT);
+        mbar_wait(bar, phase ^ 1u);  // bounded: let a late copy finish before exit
+      }
+      break;
+    }
+    const uint64_t r = cta_local<K - 1, kModeCount, CtaHub>(g, sm, s, Part{nullptr, nullptr}, -1,
+                                                            nullptr, off);
+    emit(o, v0, r, 0, acc);
+    __syncthreads();
+  }
+  if (count) {
+    acc = warp_sum_u64(acc);
+    if (lane == 0 && acc) atomicAdd(count, (unsigned long long)acc);
+  }
+}
+
+// Sets the dynamic shared-memory opt-in of `fn` once per device (bit d of `mask`;
+// devices >= 64 set it on every launch).
+template <class F>
+cudaError_t smem_optin(F fn, int bytes, std::atomic<unsigned long long>& mask) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
-  if (!bit || !(attr_devices.load(std::memory_order_acquire) & bit)) {
-    e = cudaFuncSetAttribute(k_clique<K, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kCtaSmem);
+  if (!bit || !(mask.load(std::memory_order_acquire) & bit)) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    attr_devices.fetch_or(bit, std::memory_order_acq_rel);
+    mask.fetch_or(bit, std::memory_order_acq_rel);
   }
+  return cudaSuccess;
+}
+
+template <int K>
+cudaError_t launch_hub(const GView& g, const TaskLists& t, QueueHeads* q,
+                       unsigned long long* count, uint32_t* err, cudaStream_t s, const GOut& o) {
+  static std::atomic<unsigned long long> attr_devices{0};
+  cudaError_t e = smem_optin(k_clique_hub<K>, kHubSmem, attr_devices);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  k_clique_hub<K><<<sms, kHubThreads, kHubSmem, s>>>(g, t, q, count, err, o);
+  return cudaGetLastError();
+}
+
+template <int K, int MODE>
+cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned long long* count,
+                     uint32_t* err, Part part, int grid, cudaStream_t s, GOut o = GOut{}) {
+  // The shared-memory opt-in is a per-device function attribute.
+  static std::atomic<unsigned long long> attr_devices{0};
+  cudaError_t e = smem_optin(k_clique<K, MODE>, kCtaSmem, attr_devices);
+  if (e != cudaSuccess) return e;
   k_clique<K, MODE><<<grid, kCtaThreads, kCtaSmem, s>>>(g, t, q, count, err, part, o);
   return cudaGetLastError();
 }
@@ -1561,13 +1778,21 @@ cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads*
                           unsigned long long* count, uint32_t* err, int grid, cudaStream_t s,
                           const GOut& o) {
   const Part none{nullptr, nullptr};
+  cudaError_t e;
   switch (k) {
-    case 3: return launch_k<3, kModeCount>(g, t, q, count, err, none, grid, s, o);
-    case 4: return launch_k<4, kModeCount>(g, t, q, count, err, none, grid, s, o);
-    case 5: return launch_k<5, kModeCount>(g, t, q, count, err, none, grid, s, o);
-    case 6: return launch_k<6, kModeCount>(g, t, q, count, err, none, grid, s, o);
-    case 7: return launch_k<7, kModeCount>(g, t, q, count, err, none, grid, s, o);
+    case 3: e = launch_k<3, kModeCount>(g, t, q, count, err, none, grid, s, o); break;
+    case 4: e = launch_k<4, kModeCount>(g, t, q, count, err, none, grid, s, o); break;
+    case 5: e = launch_k<5, kModeCount>(g, t, q, count, err, none, grid, s, o); break;
+    case 6: e = launch_k<6, kModeCount>(g, t, q, count, err, none, grid, s, o); break;
+    case 7: e = launch_k<7, kModeCount>(g, t, q, count, err, none, grid, s, o); break;
     default: return cudaErrorInvalidValue;
+  }
+  if (e != cudaSuccess || t.hub_max <= kCtaCap) return e;
+  switch (k) {
+    case 3: return launch_hub<3>(g, t, q, count, err, s, o);
+    case 4: return launch_hub<4>(g, t, q, count, err, s, o);
+    case 5: return launch_hub<5>(g, t, q, count, err, s, o);
+    default: return cudaErrorInvalidValue;  // schedule_into leaves hub_max at 0 for k > 5
   }
 }
 

@@ -13,6 +13,8 @@ constexpr int kWideCap = 128;               // largest local set a wide-warp tas
 constexpr int kWideWords = 4;               // bitmap words per row of a wide-warp task
 constexpr int kGroupCap = 8;                // largest local set of an eight-lane group task
 constexpr int kGroupsPerWarp = 32 / kGroupCap;
+constexpr int kHubThreads = 1024;           // threads of the hub kernel's CTA (one per SM)
+constexpr int kHubCap = 1536;               // largest local set a hub task holds
 
 // Task lists of one counting launch.  Sizes live on the device (`n`), so task
 // generation and counting run without a host round trip and can be graph-captured:
@@ -32,6 +34,9 @@ struct TaskLists {
   const int32_t* split_v = nullptr;
   const int64_t* split_off = nullptr;
   const int64_t* n = nullptr;
+  // hubs (split_v) with kCtaCap < out-degree <= hub_max run whole in the hub kernel and
+  // have no sub-tasks in split_off (0: every hub is split)
+  int hub_max = 0;
   long long* log_cta = nullptr;
   long long* log_warp = nullptr;
   long long* log_split = nullptr;
@@ -53,14 +58,15 @@ struct GOut {
 
 // Work-queue heads, zeroed before each launch.
 struct QueueHeads {
-  unsigned long long split, cta, warp, wide, search, bucket, group, pad;
+  unsigned long long split, cta, warp, wide, search, bucket, group, hub;
 };
 
 size_t clique_smem_bytes();
 // Resident counting CTAs per SM (dynamic shared memory bound).
 cudaError_t clique_occupancy(int* per_sm);
 
-// k in {3, ..., 7}: adds the k-clique count of g (DAG) over the listed tasks to *count.
+// k in {3, ..., 7}: adds the k-clique count of g (DAG) over the listed tasks to *count;
+// with t.hub_max set, a second launch (the hub kernel) counts the whole hubs.
 cudaError_t launch_clique(int k, const GView& g, const TaskLists& t, QueueHeads* q,
                           unsigned long long* count, uint32_t* err, int grid, cudaStream_t s,
                           const GOut& o = GOut{});

@@ -63,7 +63,7 @@ bool sched_may_bucket(const xgm_sched& sp) {
 // when the policy can pick BUCKET (outside stream capture: callers that capture call
 // ensure_bucket_index before they begin).
 xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched& sp,
-                         cudaStream_t s, int k_feat) {
+                         cudaStream_t s, int k_feat, bool hub) {
   bool order = false;
   if (sp.policy == XGM_SCHED_LEARNED) {
     if (!sp.model) {
@@ -111,14 +111,18 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
     if (bmax > 0) XGM_CUDA_TRY(ensure_bucket_index(g, s));
     XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax, bmax, gmax));
   }
-  XGM_CUDA_TRY(build_lists(g, tb, order, s));
+  // the hub kernel counts up to 5-cliques; deeper plans split every hub
+  const int hub_max =
+      (!hub || k > 5 || sp.hub_max < 0) ? 0 : (sp.hub_max == 0 ? kHubCap : sp.hub_max);
+  XGM_CUDA_TRY(build_lists(g, tb, order, s, hub_max));
   return XGM_OK;
 }
 
 namespace {
 
-xgm_status schedule_tasks(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp) {
-  return schedule_into(ctx->tb, g, k, sp, ctx->stream);
+xgm_status schedule_tasks(xgm_ctx* ctx, const DevGraph& g, int k, const xgm_sched& sp,
+                          bool hub = false) {
+  return schedule_into(ctx->tb, g, k, sp, ctx->stream, 0, hub);
 }
 
 xgm_status ensure_c4(xgm_ctx* ctx, const DevGraph& g) {
@@ -291,12 +295,12 @@ xgm_status count_dispatch(xgm_ctx* ctx, const DevGraph& g, int pattern, const xg
   const GView view = g.view();
   int launches = 0;
   if (k) {
-    xgm_status r = schedule_tasks(ctx, g, k, sp);
+    xgm_status r = schedule_tasks(ctx, g, k, sp, true);
     if (r != XGM_OK) return r;
     XGM_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
     XGM_CUDA_TRY(launch_clique(k, view, ctx->tb.lists(false), &ctx->d_sc->q, &ctx->d_sc->count,
                                &ctx->d_sc->err, ensure_clique_grid(ctx), s));
-    launches = 1;
+    launches = ctx->tb.hub_max > kCtaCap ? 2 : 1;  // + the hub kernel
   } else if (pattern == XGM_PATTERN_DIAMOND || pattern == XGM_PATTERN_TAILED_TRIANGLE) {
     xgm_sched tri = sp;
     if (tri.policy == XGM_SCHED_LEARNED && !tri.model) tri.policy = XGM_SCHED_HEURISTIC;
@@ -378,7 +382,7 @@ xgm_status count_kernels(xgm_ctx* ctx, const DevGraph& g, int pattern, const xgm
   if (sched_may_bucket(sp)) XGM_CUDA_TRY(ensure_bucket_index(g, s));
   XGM_CUDA_TRY(cudaStreamSynchronize(s));
   XGM_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  xgm_status r = schedule_tasks(ctx, g, k, sp);
+  xgm_status r = schedule_tasks(ctx, g, k, sp, true);
   cudaError_t e = cudaSuccess;
   if (r == XGM_OK)
     e = launch_clique(k, g.view(), ctx->tb.lists(false), &ctx->d_sc->q, &ctx->d_sc->count,

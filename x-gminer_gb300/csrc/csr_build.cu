@@ -423,7 +423,7 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
   TRY(dalloc(&g.rank, nv, s));
   TRY(dalloc(&g.perm, nv, s));
   TRY(dalloc(&g.rowptr, nv + 1, s));
-  TRY(dalloc(&g.col, ne, s));
+  TRY(dalloc(&g.col, ne + 4, s));  // 16 bytes of slack: bulk copies round a list up to 16 B
   TRY(dalloc(&g.dptr, nv, s));
   if (group) TRY(dalloc(&g.gid, nv, s));
   if (nv > 0) {

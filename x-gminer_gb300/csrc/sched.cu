@@ -206,13 +206,15 @@ __global__ void k_compact_sizes(const int64_t* cnt, int64_t tiles, int64_t* n) {
   }
 }
 
-// Hub sub-task offsets in hub-list order.
+// Hub sub-task offsets in hub-list order; hubs the hub kernel runs whole
+// (kCtaCap < out-degree <= hub_max) have none.
 __global__ void k_hub_weights_list(const int32_t* hubs, const int64_t* n, const longlong2* dptr,
-                                   int64_t* w) {
+                                   int hub_max, int64_t* w) {
   const int64_t nh = n[3];
   GRID_STRIDE(h, nh) {
     const longlong2 d = dptr[hubs[h]];
-    w[h] = d.y - d.x;
+    const int64_t s = d.y - d.x;
+    w[h] = (s > kCtaCap && s <= hub_max) ? 0 : s;
   }
 }
 
@@ -240,6 +242,7 @@ TaskLists TaskBuf::lists(bool with_log) const {
   t.split_v = split_v;
   t.split_off = split_off;
   t.n = n;
+  t.hub_max = hub_max;
   if (with_log && log) {
     t.log_cta = log;
     t.log_warp = log + cap_v;
@@ -304,8 +307,11 @@ cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& ta
   return cudaGetLastError();
 }
 
-cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s) {
+cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s,
+                        int hub_max) {
   const int64_t nv = g.nv;
+  tb.hub_max = hub_max > kHubCap ? kHubCap : (hub_max > kCtaCap ? hub_max : 0);
+  hub_max = tb.hub_max;
   TRY(cudaMemsetAsync(tb.n, 0, 8 * sizeof(int64_t), s));
   if (nv == 0) return cudaMemsetAsync(tb.split_off, 0, sizeof(int64_t), s);
   if (!order) {
@@ -327,7 +333,8 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
     cudaFreeAsync(cnt, s);
     // hub offsets in hub-list order (at most nv hubs; the rest of w stays zero)
     TRY(cudaMemsetAsync(tb.w, 0, sizeof(int64_t) * nv, s));
-    k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, tb.w);
+    k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, hub_max,
+                                                         tb.w);
     TRY(cudaGetLastError());
     TRY(scan_excl(tb.w, tb.split_off, nv, tb.n + 0, s));
   } else {
@@ -343,7 +350,8 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
     // hub offsets follow the ordered hub list (at most nv hubs; the unused tail of w
     // is zero so the scan total is the number of hub sub-tasks)
     TRY(cudaMemsetAsync(tb.w, 0, sizeof(int64_t) * nv, s));
-    k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, tb.w);
+    k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, hub_max,
+                                                         tb.w);
     TRY(cudaGetLastError());
     TRY(scan_excl(tb.w, tb.split_off, nv, tb.n + 0, s));
   }

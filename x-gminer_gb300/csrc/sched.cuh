@@ -29,6 +29,7 @@ struct TaskBuf {
   float* cost = nullptr;      // [cap_v] predicted log-cost (learned policy)
   long long* log = nullptr;   // [6 * cap_v + split cap] per-task timing log (optional)
   int64_t log_cap = 0;
+  int hub_max = 0;            // hubs left whole for the hub kernel (TaskLists::hub_max)
 
   TaskLists lists(bool with_log) const;
 };
@@ -52,7 +53,9 @@ cudaError_t classify_table(const DevGraph& g, int kmin, const xgm_tune_table& ta
                            cudaStream_t s);
 
 // Compacts tb.var into the task lists.  With `order` (learned policy) each list is
-// ordered by descending tb.cost (binned), heaviest predicted tasks first.
-cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s);
+// ordered by descending tb.cost (binned), heaviest predicted tasks first.  Hubs with
+// kCtaCap < out-degree <= hub_max get no sub-tasks (the hub kernel runs them whole).
+cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t s,
+                        int hub_max = 0);
 
 }  // namespace xgm
