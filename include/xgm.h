@@ -240,8 +240,9 @@ typedef struct {
   int hub_max;            /* 3- to 5-clique counts: a hub task (out-degree above the CTA
                              capacity, 1024) of out-degree <= hub_max runs whole in the hub kernel
                              (one 1024-thread CTA, shared-memory bitmap) instead of being
-                             split into one sub-task per out-edge (0: default 1536, the
-                             largest it holds; -1: every hub split) */
+                             split into one sub-task per out-edge (0: default, 1536 for
+                             3- and 4-cliques and every hub split for 5-cliques; -1: every
+                             hub split) */
 } xgm_sched;
 
 enum { XGM_SCHED_NO_GRAPH = 1 };

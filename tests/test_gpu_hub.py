@@ -27,7 +27,8 @@ def test_hub_kernel_complete_graph(xgm, ctx):
     try:
         assert g.info()["max_out_degree"] == n - 1
         for k, pat in ((3, "triangle"), (4, "4-clique"), (5, "5-clique")):
-            got, st = ctx.count(g, pat, with_stats=True)
+            # 5-cliques use the hub kernel only when asked (split by default)
+            got, st = ctx.count(g, pat, with_stats=True, hub_max=1536)
             assert got == math.comb(n, k), pat
             assert st["launches"] == 2, "the hub kernel ran"
         # split hubs: a triangle sub-task only counts its intersection ...
@@ -54,9 +55,9 @@ def test_hub_kernel_complete_multipartite(xgm, ctx):
         learned = xgm.trained_schedule(ctx)
         for k, pat in ((3, "triangle"), (4, "4-clique"), (5, "5-clique")):
             want = math.comb(r, k) * p ** k
-            assert ctx.count(g, pat) == want, pat
+            assert ctx.count(g, pat, hub_max=1536) == want, pat
             if learned:
-                assert ctx.count(g, pat, **learned) == want, pat
+                assert ctx.count(g, pat, **dict(learned, hub_max=1536)) == want, pat
         # split hub sub-tasks hold intersections of up to 1080 members: triangles only
         assert ctx.count(g, "triangle", hub_max=-1) == math.comb(r, 3) * p ** 3
     finally:
@@ -71,9 +72,10 @@ def test_hub_kernel_matches_split_on_random_graph(xgm, ctx):
         assert 1024 < g.info()["max_out_degree"] <= 1536
         learned = xgm.trained_schedule(ctx)
         for pat in ("triangle", "4-clique", "5-clique"):
-            whole, st = ctx.count(g, pat, with_stats=True)
+            whole, st = ctx.count(g, pat, with_stats=True, hub_max=1536)
             assert st["launches"] == 2
             assert ctx.count(g, pat, hub_max=-1) == whole, pat
+            assert ctx.count(g, pat) == whole, pat  # default: hub kernel up to 4-cliques
             if learned:
                 assert ctx.count(g, pat, **learned) == whole, pat
         # 6-cliques never use the hub kernel: every hub is split

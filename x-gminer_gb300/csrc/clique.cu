@@ -1689,7 +1689,8 @@ __global__ void __launch_bounds__(kHubThreads, 1)
     const int32_t v0 = t.split_v[ti];
     const longlong2 d0 = ldg_ll2(g.dptr + v0);
     const int s = (int)(d0.y - d0.x);
-    if (s <= kCtaCap || s > t.hub_max) continue;  // split sub-tasks (main kernel) or none
+    // hubs with sub-tasks run split in the main kernel; those without run here
+    if (s <= kCtaCap || s > t.hub_max || t.split_off[ti + 1] != t.split_off[ti]) continue;
     const long long a0 = d0.x & ~3ll;
     const int off = (int)(d0.x - a0);
     const uint32_t bytes = (uint32_t)(((off + s) * 4 + 15) & ~15);  // <= 4 (kHubCap + 4)

@@ -34,8 +34,9 @@ struct TaskLists {
   const int32_t* split_v = nullptr;
   const int64_t* split_off = nullptr;
   const int64_t* n = nullptr;
-  // hubs (split_v) with kCtaCap < out-degree <= hub_max run whole in the hub kernel and
-  // have no sub-tasks in split_off (0: every hub is split)
+  // hubs (split_v) with kCtaCap < out-degree <= hub_max may run whole in the hub kernel:
+  // those with no sub-tasks in split_off (split_off[h + 1] == split_off[h]) do (0: every
+  // hub is split)
   int hub_max = 0;
   long long* log_cta = nullptr;
   long long* log_warp = nullptr;

@@ -111,9 +111,12 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
     if (bmax > 0) XGM_CUDA_TRY(ensure_bucket_index(g, s));
     XGM_CUDA_TRY(classify_heuristic(g, k, wmax, dmax, cmax, tb, s, smax, bmax, gmax));
   }
-  // the hub kernel counts up to 5-cliques; deeper plans split every hub
-  const int hub_max =
-      (!hub || k > 5 || sp.hub_max < 0) ? 0 : (sp.hub_max == 0 ? kHubCap : sp.hub_max);
+  // The hub kernel counts up to 5-cliques, by default up to 4-cliques: at 5 the split
+  // sub-tasks win (each works on the compressed rows of N+(v0) & N+(v1); R-MAT scale 23:
+  // split 6.47 s, whole hubs 7.37 s; 4-cliques 1.08 s -> 0.25 s with whole hubs).
+  const int hub_max = (!hub || k > 5 || sp.hub_max < 0 || (sp.hub_max == 0 && k > 4))
+                          ? 0
+                          : (sp.hub_max == 0 ? kHubCap : sp.hub_max);
   XGM_CUDA_TRY(build_lists(g, tb, order, s, hub_max));
   return XGM_OK;
 }

@@ -206,15 +206,32 @@ __global__ void k_compact_sizes(const int64_t* cnt, int64_t tiles, int64_t* n) {
   }
 }
 
-// Hub sub-task offsets in hub-list order; hubs the hub kernel runs whole
-// (kCtaCap < out-degree <= hub_max) have none.
-__global__ void k_hub_weights_list(const int32_t* hubs, const int64_t* n, const longlong2* dptr,
-                                   int hub_max, int64_t* w) {
+// Hubs the hub kernel could run whole (kCtaCap < out-degree <= hub_max) into n[8].
+__global__ void k_hub_eligible(const int32_t* hubs, int64_t* n, const longlong2* dptr,
+                               int hub_max) {
   const int64_t nh = n[3];
+  unsigned long long c = 0;
   GRID_STRIDE(h, nh) {
     const longlong2 d = dptr[hubs[h]];
     const int64_t s = d.y - d.x;
-    w[h] = (s > kCtaCap && s <= hub_max) ? 0 : s;
+    c += (s > kCtaCap && s <= hub_max) ? 1ull : 0ull;
+  }
+  if (c) atomicAdd((unsigned long long*)&n[8], c);
+}
+
+// Hub sub-task offsets in hub-list order.  Eligible hubs run whole (no sub-tasks) when
+// there are at least kHubMinWhole of them: the hub kernel runs after the main launch, so
+// a handful of whole hubs would be a tail of one CTA each (R-MAT scale 22: 4 hubs of
+// ~1030, +0.7 ms whole), while their sub-tasks run first inside the main launch.
+constexpr int64_t kHubMinWhole = 32;
+__global__ void k_hub_weights_list(const int32_t* hubs, const int64_t* n, const longlong2* dptr,
+                                   int hub_max, int64_t* w) {
+  const int64_t nh = n[3];
+  const bool whole = n[8] >= kHubMinWhole;
+  GRID_STRIDE(h, nh) {
+    const longlong2 d = dptr[hubs[h]];
+    const int64_t s = d.y - d.x;
+    w[h] = (whole && s > kCtaCap && s <= hub_max) ? 0 : s;
   }
 }
 
@@ -267,7 +284,7 @@ cudaError_t taskbuf_reserve(TaskBuf& tb, int64_t nv, cudaStream_t s) {
   TRY(dalloc(&tb.group, c, s));
   TRY(dalloc(&tb.split_v, c, s));
   TRY(dalloc(&tb.split_off, c + 1, s));
-  TRY(dalloc(&tb.n, 8, s));
+  TRY(dalloc(&tb.n, 9, s));
   TRY(dalloc(&tb.var, c, s));
   TRY(dalloc(&tb.w, c, s));
   TRY(dalloc(&tb.cost, c, s));
@@ -312,7 +329,7 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
   const int64_t nv = g.nv;
   tb.hub_max = hub_max > kHubCap ? kHubCap : (hub_max > kCtaCap ? hub_max : 0);
   hub_max = tb.hub_max;
-  TRY(cudaMemsetAsync(tb.n, 0, 8 * sizeof(int64_t), s));
+  TRY(cudaMemsetAsync(tb.n, 0, 9 * sizeof(int64_t), s));
   if (nv == 0) return cudaMemsetAsync(tb.split_off, 0, sizeof(int64_t), s);
   if (!order) {
     const int64_t tiles = (nv + kCompactTile - 1) / kCompactTile;
@@ -333,6 +350,8 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
     cudaFreeAsync(cnt, s);
     // hub offsets in hub-list order (at most nv hubs; the rest of w stays zero)
     TRY(cudaMemsetAsync(tb.w, 0, sizeof(int64_t) * nv, s));
+    if (hub_max > 0)
+      k_hub_eligible<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, hub_max);
     k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, hub_max,
                                                          tb.w);
     TRY(cudaGetLastError());
@@ -350,6 +369,8 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
     // hub offsets follow the ordered hub list (at most nv hubs; the unused tail of w
     // is zero so the scan total is the number of hub sub-tasks)
     TRY(cudaMemsetAsync(tb.w, 0, sizeof(int64_t) * nv, s));
+    if (hub_max > 0)
+      k_hub_eligible<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, hub_max);
     k_hub_weights_list<<<grid_for(nv), kThreads, 0, s>>>(tb.split_v, tb.n, g.dptr, hub_max,
                                                          tb.w);
     TRY(cudaGetLastError());

@@ -23,7 +23,7 @@ struct TaskBuf {
   int32_t* group = nullptr;
   int32_t* split_v = nullptr;
   int64_t* split_off = nullptr;
-  int64_t* n = nullptr;       // [8] see TaskLists
+  int64_t* n = nullptr;       // [9] see TaskLists; n[8] = hubs eligible to run whole
   uint8_t* var = nullptr;     // [cap_v] variant per vertex
   int64_t* w = nullptr;       // [cap_v] scratch
   float* cost = nullptr;      // [cap_v] predicted log-cost (learned policy)

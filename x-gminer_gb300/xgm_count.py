@@ -37,6 +37,8 @@ def main() -> None:
     src = ap.add_mutually_exclusive_group(required=True)
     src.add_argument("--graph", help="prefix of <prefix>.meta.txt / .vertex.bin / .edge.bin")
     src.add_argument("--rmat", type=int, metavar="SCALE", help="seeded R-MAT, edge factor 16")
+    src.add_argument("--er", type=int, nargs=2, metavar=("N", "M"),
+                     help="seeded Erdos-Renyi G(N, M) edge samples")
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--pattern", default="4-clique")
     ap.add_argument("--patternID", type=int,
@@ -44,6 +46,8 @@ def main() -> None:
                          "17-40 = GLUMIN P1-P24")
     ap.add_argument("--policy", choices=["heuristic", "learned"], default="heuristic")
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--hub-max", type=int, default=0,
+                    help="hub kernel bound (xgm_sched.hub_max; -1: split every hub)")
     args = ap.parse_args()
     if args.patternID and args.patternID not in PATTERN_IDS and args.patternID not in GRAPHPI_6:
         raise SystemExit(f"patternID {args.patternID} is not a supported plan "
@@ -59,22 +63,19 @@ def main() -> None:
     ctx = xgm.Context(0)
     if args.graph:
         g = ctx.load_graph(args.graph)
+    elif args.er:
+        nv, s, d = xgm.gen_er(args.er[0], args.er[1], seed=args.seed)
+        g = ctx.graph_from_edges(nv, s, d)
     else:
         nv, s, d = xgm.gen_rmat(args.rmat, 16, seed=args.seed)
         g = ctx.graph_from_edges(nv, s, d)
     kw = {}
     if args.policy == "learned":
-        spec = json.load(open(os.path.join(HERE, "costmodel.json")))
-        if spec.get("variants") != xgm.NUM_VARIANTS or spec.get("features") != xgm.MODEL_FEATURES:
-            raise SystemExit("costmodel.json was trained for another feature layout; retrain it "
-                             "with x-gminer_gb300/train_costmodel.py")
-        import numpy as np
-
-        m = xgm.Model(ctx)
-        m.set_params(np.asarray(spec["params"], dtype=np.float32))
-        kw = {"policy": xgm.SCHED_LEARNED, "model": m,
-              "order_by_cost": int(spec.get("order_by_cost", 1)),
-              "margin": float(spec.get("margin", 0.0))}
+        kw = xgm.trained_schedule(ctx)
+        if not kw:
+            raise SystemExit("costmodel.json is absent or was trained for another feature "
+                             "layout; retrain it with x-gminer_gb300/train_costmodel.py")
+    kw["hub_max"] = args.hub_max
     for _ in range(args.repeat):
         count, st = ctx.count(g, xgm.plan(pattern), with_stats=True, **kw)
         name = pattern if isinstance(pattern, str) else f"patternID {args.patternID}"
