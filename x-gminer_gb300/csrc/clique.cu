@@ -558,6 +558,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   constexpr bool MULTI = MODE == kModeMulti;  // Q == 3: also local edges + participation
   constexpr bool PART = MODE == kModePart || MULTI;
   constexpr bool WGT = MODE == kModeWeight;
+  constexpr bool kVec = !PART && !WGT;  // 128-bit loads of the lists (count modes)
   int32_t* S = (int32_t*)(sm + Sh::kOffS) + s_off;
   if (Q == 1) {
     if (!WGT) return (uint64_t)s;  // same value in every thread
@@ -603,8 +604,15 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
       if (hi - lo > kClipMin && ldg_i32(g.col + hi - 1) > smax0)
         hi = lower_pos(g.col, lo, hi, smax0 + 1);
     }
-    lb[i] = lo;
-    pre[i] = (int32_t)(hi - lo);
+    if constexpr (kVec) {  // 16-byte units from the aligned start; lb keeps the phase
+      const long long a = lo & ~3ll;
+      lb[i] = a | (lo - a);
+      cnt[i] = (uint32_t)(hi - lo);
+      pre[i] = hi > lo ? (int32_t)((hi - a + 3) >> 2) : 0;
+    } else {
+      lb[i] = lo;
+      pre[i] = (int32_t)(hi - lo);
+    }
   }
   __syncthreads();
   for (int i = tid; i < s; i += Sh::kThreads) {
@@ -621,6 +629,65 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   const int total = pre[s];
   const int32_t smax = S[s - 1];
   uint64_t acc = 0, q2 = 0;
+  // Count modes: flattened walk over 16-byte units of the rows' lists (pre[] counts
+  // units; lb[i] = the list's aligned start | its phase, cnt[i] = its length): warp
+  // chunks of 64 units, one 128-bit load per lane and unit, both loads of a lane in
+  // flight before use.  Elements of a unit outside the clipped list (the other rows'
+  // entries next to it) are masked by position.  Then the Bloom / hash test as below.
+  if constexpr (kVec) {
+    for (int c = warp; c * 64 < total; c += Sh::kWarps) {
+      const int kb = c * 64 + lane;
+      int i;
+      {  // segment of the chunk start, as in the scalar walk below
+        constexpr int kR1 = Sh::kCap <= 1024 ? 32 : 64;
+        constexpr int kR2 = kR1 / 32;
+        const int k0 = c * 64;
+        const int c1 = lane * kR1;
+        const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
+        const int r1 = 31 - __clz(b1);
+        const int c2 = r1 * kR1 + lane * kR2;
+        const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
+        i = r1 * kR1 + (31 - __clz(b2)) * kR2;
+        while (i + 1 < s && pre[i + 1] <= kb) ++i;
+      }
+      int4 v[2];
+      int iv[2], rel[2], len[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = kb + 32 * h;
+        iv[h] = i;
+        rel[h] = 0;
+        len[h] = 0;
+        v[h] = make_int4(0, 0, 0, 0);
+        if (k < total) {
+          while (k >= pre[i + 1]) ++i;
+          const long long L = lb[i];
+          const int u = k - pre[i];
+          iv[h] = i;
+          rel[h] = 4 * u - (int)(L & 3);  // element index of the unit's first word
+          len[h] = (int)cnt[i];
+          v[h] = __ldg((const int4*)(g.col + (L & ~3ll)) + u);
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int32_t xs4[4] = {v[h].x, v[h].y, v[h].z, v[h].w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int e = rel[h] + t;
+          const int32_t x = xs4[t];
+          if (e < 0 || e >= len[h] || x > smax) continue;
+          const uint32_t b = bloom_bit(x);
+          if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
+          const int j = hash_find<Sh>(hkey, hval, x);
+          if (j < 0) continue;
+          const int ii = iv[h];
+          if (Q == 2) acc += 1;
+          else atomicOr(&rows[roff[ii] + (j >> 5) - (ii >> 5)], 1u << (j & 31));
+        }
+      }
+    }
+  } else
   // Flattened walk over all (i, element) pairs: warp chunks of 256 consecutive
   // elements, lanes contiguous within a chunk so row reads are coalesced.  Each lane
   // keeps its segment's base in registers, issues four loads before using them, and
