@@ -1229,6 +1229,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
   constexpr bool MULTI = MODE == kModeMulti;
   constexpr bool PART = MODE == kModePart || MULTI;
   constexpr bool WGT = MODE == kModeWeight;
+  constexpr bool kVec = !PART && !WGT;  // 128-bit loads of the lists, as in cta_local
   const int lane = threadIdx.x & 31;
   const longlong2 d0 = ldg_ll2(g.dptr + v0);
   const int s = (int)(d0.y - d0.x);
@@ -1267,7 +1268,13 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
       len[t] = (int)(hi - lo);
     }
   }
-  const int mine = len[0] + len[1] + len[2] + len[3];
+  int units[4];  // kVec: 16-byte units of each list from its aligned start
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const long long a = lbv[t] & ~3ll;
+    units[t] = kVec ? (len[t] > 0 ? (int)((lbv[t] + len[t] - a + 3) >> 2) : 0) : len[t];
+  }
+  const int mine = units[0] + units[1] + units[2] + units[3];
   int inc = mine;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -1275,16 +1282,25 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
     if (lane >= o) inc += y;
   }
   int ex = inc - mine;
+  if (PART)
+    for (int x = lane; x < kWideCap; x += 32) w.cnt[x] = 0u;
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
     const int i = 4 * lane + t;
     if (i <= s) w.pre[i] = ex;  // pre[s] = total (items >= s have length 0)
-    if (i < s) w.lb[i] = lbv[t];
-    ex += len[t];
+    if (i < s) {
+      if (kVec) {  // aligned start | phase; the list's length in cnt
+        const long long a = lbv[t] & ~3ll;
+        w.lb[i] = a | (lbv[t] - a);
+        w.cnt[i] = (uint32_t)len[t];
+      } else {
+        w.lb[i] = lbv[t];
+      }
+    }
+    ex += units[t];
   }
   if (lane == 31) w.pre[kWideCap] = inc;  // total when s == kWideCap
   for (int x = lane; x < kWideCap * kWideWords; x += 32) w.rows[x] = 0u;
-  for (int x = lane; x < kWideCap; x += 32) w.cnt[x] = 0u;
   w.bloom[lane] = 0u;  // kWideBloomWords == 64
   w.bloom[lane + 32] = 0u;
   __syncwarp();
@@ -1298,6 +1314,46 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
   const int total = w.pre[s];
   uint64_t acc = 0, q2 = 0;
   int i = 0;
+  if constexpr (kVec) {  // two 16-byte units per lane in flight, then their 8 elements
+    for (int kb = lane; kb < total; kb += 64) {
+      int4 v[2];
+      int iv[2], rel[2], ln[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = kb + 32 * h;
+        iv[h] = i;
+        rel[h] = 0;
+        ln[h] = 0;
+        v[h] = make_int4(0, 0, 0, 0);
+        if (k < total) {
+          while (k >= w.pre[i + 1]) ++i;
+          const long long L = w.lb[i];
+          const int u = k - w.pre[i];
+          iv[h] = i;
+          rel[h] = 4 * u - (int)(L & 3);
+          ln[h] = (int)w.cnt[i];
+          v[h] = __ldg((const int4*)(g.col + (L & ~3ll)) + u);
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int32_t xs4[4] = {v[h].x, v[h].y, v[h].z, v[h].w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int e = rel[h] + t;
+          const int32_t x = xs4[t];
+          if (e < 0 || e >= ln[h] || x > smax) continue;
+          const uint32_t b = bloom_bit(x) >> 3;
+          if (!((w.bloom[b >> 5] >> (b & 31)) & 1u)) continue;
+          const int j = warp_bsearch(w.S, s, x);
+          if (j < 0) continue;
+          const int ii = iv[h];
+          if (Q == 2) acc += 1;
+          else atomicOr(&w.rows[ii * kWideWords + (j >> 5)], 1u << (j & 31));
+        }
+      }
+    }
+  } else {
   int seg_end = w.pre[1];
   long long seg_base = w.lb[0];
   for (int kb = lane; kb < total; kb += 128) {
@@ -1347,6 +1403,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
         }
       }
     }
+  }
   }
   if (MULTI) *q2out = q2;
   __syncwarp();
