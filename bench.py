@@ -75,7 +75,7 @@ def parse():
     p.add_argument("--no-clique5", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--workload", default="clique",
-                   choices=["clique", "batch", "motifs", "patterns5"],
+                   choices=["clique", "batch", "motifs", "patterns5", "ablation"],
                    help="clique: k-clique counting on R-MAT s22; batch: 4096 BA graphs; "
                         "motifs: edge-induced 4-vertex motifs on ER and Chung-Lu 2^21; "
                         "patterns5: GLUMIN's 5-vertex plans P6-P22 on R-MAT s12 and ER 2^16")
@@ -743,6 +743,83 @@ def patterns5_arm(args, dist: Dist) -> None:
     ctx.close()
 
 
+def ablation_arm(args, dist: Dist) -> None:
+    """What the learned schedule gains, and from what: on the same kernels, (1) the plain
+    degree-threshold heuristic (WARP <= 32 < WIDE <= 128 < CTA <= 1024 < split), (2) that
+    heuristic extended with the per-task variants by thresholds alone (GROUP <= 8 <
+    BUCKET <= 32), (3) the autotuned per-out-degree-bucket variant table (no model), (4)
+    the trained MLP's per-task choice.  4-clique on R-MAT scale 22 seed 2 (a training
+    scale, other seed) and on the held-out R-MAT scale 23 seed 99; the 4096-graph BA batch
+    (triangle + 4-clique + diamond).  Counts must agree across the arms."""
+    import numpy as np
+    import torch
+
+    xgm = load_engine()
+    torch.cuda.set_device(dist.local)
+    ctx = xgm.Context(dist.local)
+    learned = xgm.trained_schedule(ctx)
+    ext = {"group_max": 8, "bucket_max": 32}
+
+    def best_ms(fn, reps):
+        fn()
+        out, ms = None, []
+        for _ in range(reps):
+            out, t = fn()
+            ms.append(t)
+        return out, min(ms)
+
+    res = {}
+    clocks = ClockSampler(dist.local).start()
+    for scale, seed in ((22, 2), (23, 99)):
+        nv, src, dst = xgm.gen_rmat(scale, 16, seed=seed)
+        g = ctx.graph_from_edges(nv, src, dst)
+        del src, dst
+        tune = ctx.autotune(g, "4-clique", reps=2)
+        arms = {"heuristic": {}, "extended_heuristic": ext,
+                "autotuned": {"policy": xgm.SCHED_TUNED, "table": tune["table"]}}
+        if learned:
+            arms["learned"] = learned
+        row, want = {}, None
+        for name, kw in arms.items():
+            def run(kw=kw):
+                c, st = ctx.count(g, "4-clique", with_stats=True, **kw)
+                return c, st["kernel_ms"] + st["prep_ms"]
+            c, ms = best_ms(run, max(2, args.steps))
+            want = c if want is None else want
+            assert c == want, f"{name} changed the count"
+            row[name] = ms
+        row["count"] = want
+        res[f"4-clique rmat s{scale} seed {seed}"] = row
+        g.close()
+    vo, eo, src, dst = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=5)
+    b = ctx.batch_from_edges(vo, src, dst)
+    tune = ctx.autotune(b, BATCH_PATTERNS, reps=3)
+    arms = {"heuristic": {}, "extended_heuristic": ext,
+            "autotuned": {"policy": xgm.SCHED_TUNED, "table": tune["table"]}}
+    if learned:
+        arms["learned"] = learned
+    row, want = {}, None
+    for name, kw in arms.items():
+        def run(kw=kw):
+            out, st = ctx.count_batched(b, BATCH_PATTERNS, with_stats=True, **kw)
+            return out, st["kernel_ms"]
+        out, ms = best_ms(run, max(3, args.steps))
+        want = out if want is None else want
+        assert np.array_equal(out, want), f"{name} changed a count"
+        row[name] = ms
+    res["batch 4096 BA graphs, triangle + 4-clique + diamond"] = row
+    b.close()
+    clk = clocks.stop()
+    line = {"workload": "schedule ablation (ms per count, best of the steps)", "results": res,
+            "schedule_definitions": {"heuristic": "WARP <= 32 < WIDE <= 128 < CTA <= 1024 < split",
+                                     "extended_heuristic": "GROUP <= 8 < BUCKET <= 32 < WIDE <= 128 < CTA <= 1024 < split",
+                                     "autotuned": "per out-degree bucket variant table (xgm_autotune)",
+                                     "learned": "MLP per task (costmodel.json)"},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -755,6 +832,8 @@ def main():
             motifs_arm(args, dist)
         elif args.workload == "patterns5":
             patterns5_arm(args, dist)
+        elif args.workload == "ablation":
+            ablation_arm(args, dist)
         else:
             engine_arm(args, dist)
     finally:

@@ -356,7 +356,11 @@ xgm_status xgm_model_get_params(const xgm_model* m, float* params);
 /* Runs `plan` on g with every task forced to `variant` (tasks the variant cannot hold
  * fall back by capacity) and per-task timing on, and returns samples of the tasks that
  * ran with `variant`: features X[n][12], targets y[n] = log2(cycles * warps used), for
- * every `stride`-th such task, at most max_rows.  count_out (optional) gets the count. */
+ * every `stride`-th such task, at most max_rows.  count_out (optional) gets the count.
+ * With XGM_COLLECT_MULTI or-ed into `variant` (plan: triangle) the timed launch is the
+ * batched multi-pattern one (triangles + 4-cliques + triangle participation per task,
+ * xgm_count_batched), its tasks described as 4-clique tasks. */
+#define XGM_COLLECT_MULTI 0x100
 xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan, int variant,
                              int stride, float* X, float* y, int64_t max_rows, int64_t* n_rows,
                              uint64_t* count_out);

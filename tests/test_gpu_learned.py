@@ -64,3 +64,30 @@ def test_learned_schedule_in_batches(xgm, ctx):
     got = ctx.count_batched(b, ["triangle", "4-clique", "diamond"], policy=xgm.SCHED_LEARNED,
                             model=m)
     assert np.array_equal(base, got)
+
+
+def test_trained_model_gains_on_held_out_graph(xgm, ctx):
+    """The trained cost model (costmodel.json) against the plain degree-threshold
+    heuristic on a graph outside its training and validation sets (R-MAT scale 21, seed
+    77; training used seeds 10-14, validation seed 98, evaluation seed 99): same count,
+    and the learned schedule is not slower (best of 5 counts each; 3 % tolerance for
+    timing noise; it measured ~5 % faster at scale 22 and ~8 % at scale 23)."""
+    learned = xgm.trained_schedule(ctx)
+    if not learned:
+        pytest.skip("costmodel.json absent")
+    nv, s, d = xgm.gen_rmat(21, 16, seed=77)
+    g = ctx.graph_from_edges(nv, s, d)
+
+    def best(kw):
+        ctx.count(g, "4-clique", **kw)
+        ms, cnt = [], None
+        for _ in range(5):
+            cnt, st = ctx.count(g, "4-clique", with_stats=True, **kw)
+            ms.append(st["kernel_ms"] + st["prep_ms"])
+        return cnt, min(ms)
+
+    c_h, t_h = best({})
+    c_l, t_l = best(learned)
+    assert c_l == c_h
+    assert t_l <= 1.03 * t_h, f"learned {t_l:.2f} ms vs plain heuristic {t_h:.2f} ms"
+    g.close()

@@ -60,6 +60,7 @@ NUM_VARIANTS = 7
 ALL_VARIANTS = (VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH, VAR_BUCKET, VAR_GROUP)
 
 MODEL_FEATURES, MODEL_HIDDEN = 12, 32
+COLLECT_MULTI = 0x100  # xgm_model_collect: time the batched multi-pattern launch
 MODEL_PARAMS = MODEL_HIDDEN * MODEL_FEATURES + 2 * MODEL_HIDDEN + 1
 
 
@@ -339,11 +340,14 @@ class Context:
     def count_batched(self, batch: "Batch", patterns, policy: int = SCHED_HEURISTIC,
                       model: Optional["Model"] = None, table: Optional[TuneTable] = None,
                       use_graph: bool = True, order_by_cost: int = 1, margin: float = 0.0,
-                      with_stats: bool = False):
+                      group_max: int = 0, bucket_max: int = 0, search_max: int = 0,
+                      hub_max: int = 0, with_stats: bool = False):
         plans = [p if isinstance(p, Plan) else self.plan(p) for p in patterns]
         arr = (C.c_void_p * len(plans))(*[p._h.value for p in plans])
         sp = self._sched(policy, 0, model, 0, 0, order_by_cost, table,
-                         0 if use_graph else SCHED_NO_GRAPH, margin=margin)
+                         0 if use_graph else SCHED_NO_GRAPH, search_max=search_max,
+                         bucket_max=bucket_max, group_max=group_max, margin=margin,
+                         hub_max=hub_max)
         out = np.empty(batch.num_graphs * len(plans), dtype=np.uint64)
         st = Stats()
         _check(lib().xgm_count_batched(self._h, batch._h, C.cast(arr, C.c_void_p), len(plans),
@@ -542,8 +546,12 @@ class Model:
         _check(lib().xgm_model_set_params(self._h, _ptr(p)))
 
     def collect(self, graph: Graph, pattern, variant: int, stride: int = 1,
-                max_rows: int = 1 << 20):
+                max_rows: int = 1 << 20, multi: bool = False):
+        """Per-task features and log2 warp-cycles with every task forced to `variant`;
+        multi=True times the batched multi-pattern launch (pattern "triangle")."""
         plan = pattern if isinstance(pattern, Plan) else self.ctx.plan(pattern)
+        if multi:
+            variant |= COLLECT_MULTI
         X = np.empty((max_rows, MODEL_FEATURES), dtype=np.float32)
         y = np.empty(max_rows, dtype=np.float32)
         n = C.c_int64()

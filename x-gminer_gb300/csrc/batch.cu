@@ -235,9 +235,9 @@ xgm_status batch_sequence(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P,
       XGM_CUDA_TRY(cudaMemsetAsync(b->vpart, 0, sizeof(unsigned long long) * (g.nv > 0 ? g.nv : 1), s));
       XGM_CUDA_TRY(cudaMemsetAsync(b->epart, 0, sizeof(unsigned) * (g.ne > 0 ? g.ne : 1), s));
     }
-    // roots from out-degree 2 on (triangles); the launch does 4-clique work per task, so
-    // the learned model sees the tasks as 4-clique tasks
-    xgm_status r = schedule_into(b->tb, g, 3, sp, s, 4);
+    // roots from out-degree 2 on (triangles); the learned model describes the tasks as
+    // tasks of this multi-pattern launch (kFeatMulti)
+    xgm_status r = schedule_into(b->tb, g, 3, sp, s, kFeatMulti);
     if (r != XGM_OK) return r;
     // without a participation plan the counters go to a dummy-free path: the multi
     // kernel always credits participation, so give it real buffers

@@ -58,7 +58,7 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   f[1] = log2f(1.0f + (float)sum) / 24.0f;
   f[2] = log2f(1.0f + (float)maxd) / 11.0f;
   f[3] = (float)sum / ((float)s * (float)maxd + 1.0f);
-  f[4] = (float)(k - 3) * 0.5f;
+  f[4] = k == kFeatMulti ? 0.75f : (float)(k - 3) * 0.5f;
   for (int v = 0; v < XGM_NUM_VARIANTS; ++v) f[kShapeFeat + v] = 0.0f;
 }
 
@@ -435,12 +435,15 @@ xgm_status xgm_model_train(xgm_ctx* ctx, xgm_model* m, const float* X, const flo
 xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* plan, int variant,
                              int stride, float* X, float* y, int64_t max_rows, int64_t* n_rows,
                              uint64_t* count_out) {
+  const bool multi = (variant & XGM_COLLECT_MULTI) != 0;
+  variant &= ~XGM_COLLECT_MULTI;
   if (!ctx || !g || !plan || !X || !y || !n_rows || max_rows < 0 || stride <= 0 ||
       variant < 0 || variant >= XGM_NUM_VARIANTS)
     return XGM_ERR_INVALID;
   const int k = clique_k(plan->pattern);
-  if (!k) {
-    set_thread_error("timing collection covers the triangle / clique / participation plans");
+  if (!k || (multi && k != 3)) {
+    set_thread_error(multi ? "the multi-pattern timing runs with the triangle plan"
+                           : "timing collection covers the triangle / clique / participation plans");
     return finish_status(ctx, XGM_ERR_UNSUPPORTED);
   }
   cudaStream_t s = ctx->stream;
@@ -468,8 +471,20 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   XGM_CUDA_TRY(classify_heuristic(G, k, wmax, dmax, cmax, tb, s, smax, bmax, gmax));
   XGM_CUDA_TRY(build_lists(G, tb, false, s));
   XGM_CUDA_TRY(cudaMemsetAsync(ctx->d_sc, 0, sizeof(Scalars), s));
-  XGM_CUDA_TRY(launch_clique(k, G.view(), tb.lists(true), &ctx->d_sc->q, &ctx->d_sc->count,
-                             &ctx->d_sc->err, ctx->clique_grid > 0 ? ctx->clique_grid : 2 * ctx->num_sms, s));
+  const int grid = ctx->clique_grid > 0 ? ctx->clique_grid : 2 * ctx->num_sms;
+  unsigned long long* vpart = nullptr;
+  unsigned* epart = nullptr;
+  if (multi) {  // per-task triangles + 4-cliques + participation, as in the batched launch
+    XGM_CUDA_TRY(cudaMallocAsync(&vpart, sizeof(unsigned long long) * (G.nv > 0 ? G.nv : 1), s));
+    XGM_CUDA_TRY(cudaMallocAsync(&epart, sizeof(unsigned) * (G.ne > 0 ? G.ne : 1), s));
+    XGM_CUDA_TRY(cudaMemsetAsync(vpart, 0, sizeof(unsigned long long) * (G.nv > 0 ? G.nv : 1), s));
+    XGM_CUDA_TRY(cudaMemsetAsync(epart, 0, sizeof(unsigned) * (G.ne > 0 ? G.ne : 1), s));
+    XGM_CUDA_TRY(launch_multi(G.view(), tb.lists(true), &ctx->d_sc->q, vpart, epart,
+                              &ctx->d_sc->err, grid, s, GOut{}));
+  } else {
+    XGM_CUDA_TRY(launch_clique(k, G.view(), tb.lists(true), &ctx->d_sc->q, &ctx->d_sc->count,
+                               &ctx->d_sc->err, grid, s));
+  }
   float *dx = nullptr, *dy = nullptr;
   const int64_t cap = max_rows > 0 ? max_rows : 1;
   XGM_CUDA_TRY(cudaMallocAsync(&dx, sizeof(float) * cap * kFeat, s));
@@ -496,7 +511,7 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
                         : variant == XGM_VAR_BUCKET ? tl.log_bucket
                         : variant == XGM_VAR_GROUP  ? tl.log_group
                                                     : tl.log_split;
-  k_assemble<<<grid_for(G.nv), kThreads, 0, s>>>(G.view(), k, variant, list, tb.n, nidx, lg,
+  k_assemble<<<grid_for(G.nv), kThreads, 0, s>>>(G.view(), multi ? kFeatMulti : k, variant, list, tb.n, nidx, lg,
                                                  tb.split_off, stride, dx, dy, max_rows,
                                                  &ctx->d_sc->aux);
   XGM_CUDA_TRY(cudaGetLastError());
@@ -513,6 +528,8 @@ xgm_status xgm_model_collect(xgm_ctx* ctx, const xgm_graph* g, const xgm_plan* p
   }
   cudaFreeAsync(dx, s);
   cudaFreeAsync(dy, s);
+  if (vpart) cudaFreeAsync(vpart, s);
+  if (epart) cudaFreeAsync(epart, s);
   XGM_CUDA_TRY(cudaStreamSynchronize(s));
   return finish_status(ctx, r);
 }

@@ -11,6 +11,11 @@ enum : uint8_t {
   VAR_GROUP = 6, VAR_SKIP = 7
 };
 constexpr int kNumVar = 7;
+// k_feat code of the batched multi-pattern launch (triangles + 4-cliques + triangle
+// participation per task): the learned model's depth feature is 0.75 for it, between
+// the 4-clique (0.5) and 5-clique (1.0) tasks, so its timings do not collide with the
+// 4-clique count's.
+constexpr int kFeatMulti = 16;
 
 // Device buffers of one schedule; sized for a graph's vertex count and reused.
 struct TaskBuf {

@@ -75,16 +75,19 @@ def main():
     # (disjoint components; seed 6, not the benchmark's batch)
     vo, eo, s, d = xgm.gen_ba_batch(4096, 100, 5000, 3, 8, seed=6)
     g = ctx.graph_from_edges(int(vo[-1]), s, d)
-    for pat in ["triangle", "4-clique", "diamond"]:
+    # the batched launch itself: triangles + 4-cliques + participation per task
+    for pat, multi in (("triangle", False), ("4-clique", False), ("diamond", False),
+                       ("triangle", True)):
         for var in xgm.ALL_VARIANTS:
-            X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64)
+            X, y, _ = model.collect(g, pat, var, stride=1, max_rows=args.rows * 64, multi=multi)
             if len(y) > args.rows:
                 idx = np.random.default_rng(17 + var).choice(len(y), args.rows, replace=False)
                 X, y = X[idx], y[idx]
             Xs.append(X)
             ys.append(y)
-            meta.append({"graph": "ba x4096 seed 6", "pattern": pat, "variant": var,
-                         "rows": len(y)})
+            meta.append({"graph": "ba x4096 seed 6",
+                         "pattern": "multi (triangle + 4-clique)" if multi else pat,
+                         "variant": var, "rows": len(y)})
     g.close()
     X = np.concatenate(Xs)
     y = np.concatenate(ys)
