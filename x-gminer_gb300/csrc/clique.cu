@@ -28,6 +28,7 @@
 // eight-lane group tasks (s <= 8, four per warp), bucket-filtered search tasks, and
 // streaming warp tasks (s <= 32).
 #include <atomic>
+#include <type_traits>
 #include "clique.cuh"
 
 namespace xgm {
@@ -37,7 +38,11 @@ namespace {
 // ---------------------------------------------------------------- CTA shapes
 // A CTA task holds its local set S in shared memory.  Layout (bytes):
 //   lb[cap] i64 | S[cap + 4] i32 | pre[cap + 8] i32 | hkey[hash] i32 | hval[hash] u16 |
-//   cnt[cap] u32 | rows[tri_words(cap)] u32 | bloom[512] u32 | roff[cap] i32 | misc[32] i64
+//   [cnt[cap] u32] | rows[tri_words(cap)] u32 | bloom[512] u32 | misc[32] i64
+// cnt (per-member participation counters) exists in the participation and multi modes
+// only; the count modes keep each list's length in lb's top bits instead, so two main
+// CTAs of a count mode fit the 196 KB shared-memory configuration (60 KB of L1 left).
+// A row's word offset is computed (tri_row_off), not stored.
 // S has four words of slack: a bulk copy lands a list at its own 16-byte phase.
 // CtaMain is the persistent counting kernel's CTA (512 threads, 2 CTAs per SM, local
 // sets of up to 1024); CtaHub is the hub kernel's (1024 threads, 1 CTA per SM, up to
@@ -45,7 +50,7 @@ namespace {
 constexpr int tri_words_c(int s) {
   return s * ((s + 31) >> 5) - (16 * (s >> 5) * ((s >> 5) - 1) + (s & 31) * (s >> 5));
 }
-template <int NT, int CAP, int HBITS>
+template <int NT, int CAP, int HBITS, bool CNT = false>
 struct CtaShape {
   static constexpr int kThreads = NT, kWarps = NT / 32, kCap = CAP;
   static constexpr int kHashBits = HBITS, kHash = 1 << HBITS;
@@ -57,10 +62,9 @@ struct CtaShape {
   static constexpr int kOffHkey = kOffPre + 4 * (CAP + 8);
   static constexpr int kOffHval = kOffHkey + 4 * kHash;
   static constexpr int kOffCnt = kOffHval + 2 * kHash;
-  static constexpr int kOffRows = kOffCnt + 4 * CAP;
+  static constexpr int kOffRows = kOffCnt + (CNT ? 4 * CAP : 0);
   static constexpr int kOffBloom = kOffRows + 4 * kRowsWords;
-  static constexpr int kOffRowOff = kOffBloom + 4 * kBloomWords;  // int32[cap] row offsets
-  static constexpr int kOffMisc = kOffRowOff + 4 * CAP;
+  static constexpr int kOffMisc = kOffBloom + 4 * kBloomWords;
   static constexpr int kOffBar = kOffMisc + 8 * 31;  // mbarrier of the bulk copies
   static constexpr int kSmem = kOffMisc + 8 * 32;
   static_assert(2 * NT >= CAP, "the length scan gives each thread two members");
@@ -68,12 +72,16 @@ struct CtaShape {
   static_assert(kOffS % 16 == 0 && kOffMisc % 8 == 0 && 4 * kWarps <= 8 * 31,
                 "aligned regions; warp totals below the barrier");
 };
-using CtaMain = CtaShape<kCtaThreads, kCtaCap, 11>;
+using CtaMain = CtaShape<kCtaThreads, kCtaCap, 11>;           // count modes
+using CtaMainCnt = CtaShape<kCtaThreads, kCtaCap, 11, true>;  // participation / multi
 using CtaHub = CtaShape<kHubThreads, kHubCap, 12>;
 static_assert(CtaMain::kRowsWords == 16896 && CtaMain::kHash == kHashSize, "main CTA shape");
+static_assert(2 * (CtaMain::kSmem + 1024) <= 196 * 1024, "count-mode CTAs leave 60 KB of L1");
+static_assert(CtaMain::kOffS == CtaMainCnt::kOffS && CtaMain::kOffMisc + 4096 == CtaMainCnt::kOffMisc,
+              "the shapes differ only by cnt");
 constexpr int kOffS = CtaMain::kOffS;
-constexpr int kOffMisc = CtaMain::kOffMisc;
 constexpr int kCtaSmem = CtaMain::kSmem;
+constexpr int kCtaSmemCnt = CtaMainCnt::kSmem;
 constexpr int kHubSmem = CtaHub::kSmem;
 static_assert(kHubSmem <= 227 * 1024, "hub CTA fits one SM's shared memory");
 constexpr int kClipMin = 96;    // lists longer than this are clipped at max(S)
@@ -191,14 +199,14 @@ enum { kModeCount = 0, kModePart = 1, kModeWeight = 2, kModeMulti = 3 };
 // the word's popcounts in 32 bits.
 template <int Q, bool WGT, class Sh = CtaMain>
 __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, const int32_t* pre,
-                                                   const int32_t* roff, int W = 0) {
+                                                   int W = 0) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = n;
   if (W == 0) W = (n + 31) >> 5;
   uint64_t acc = 0;
   for (int i = warp; i < s; i += Sh::kWarps) {
     const int qi = i >> 5, nwi = W - qi;
-    const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
+    const uint32_t wi = lane < nwi ? rows[tri_row_off(i, W) + lane] : 0u;
     const int w = qi + lane;
     unsigned nz = __ballot_sync(kFull, wi != 0u);
     while (nz) {
@@ -264,8 +272,7 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
 // Row offsets of the members of one word come from one base pointer, as in
 // cta_count_rows.
 template <int Q, int G, class Sh = CtaMain>
-__device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff, int W,
-                                       int row_lo, int row_hi) {
+__device__ uint64_t count_rows_grouped(const uint32_t* rows, int W, int row_lo, int row_hi) {
   static_assert(Q == 3 || Q == 4, "grouped rows cover the 4- and 5-clique count phases");
   constexpr unsigned kGMask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
   constexpr int kGroups = 32 / G;
@@ -276,7 +283,7 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff
     const int i = i0 + lane / G;
     const bool live = i < row_hi;
     const int qi = live ? (i >> 5) : 0, nwi = W - qi;
-    const uint32_t wi = (live && sub < nwi) ? rows[roff[i] + sub] : 0u;
+    const uint32_t wi = (live && sub < nwi) ? rows[tri_row_off(i, W) + sub] : 0u;
     const int w = qi + sub;
     unsigned nz = (__ballot_sync(kFull, wi != 0u) >> gbase) & kGMask;
     while (__any_sync(kFull, nz != 0u)) {
@@ -328,14 +335,15 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, const int32_t* roff
 // above 1024, the hub CTA): lane holds words qi + lane and qi + lane + 32 of row i, and
 // each enumeration runs over the two halves in turn.
 template <int Q, class Sh>
-__device__ uint64_t cta_count_rows2(const uint32_t* rows, int nrows, const int32_t* roff, int W) {
+__device__ uint64_t cta_count_rows2(const uint32_t* rows, int nrows, int W) {
   static_assert(Q == 3 || Q == 4, "two-word rows cover the 4- and 5-clique count phases");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t acc = 0;
   for (int i = warp; i < nrows; i += Sh::kWarps) {
     const int qi = i >> 5, nwi = W - qi;
-    const uint32_t wa = lane < nwi ? rows[roff[i] + lane] : 0u;
-    const uint32_t wb = lane + 32 < nwi ? rows[roff[i] + lane + 32] : 0u;
+    const int ri = tri_row_off(i, W);
+    const uint32_t wa = lane < nwi ? rows[ri + lane] : 0u;
+    const uint32_t wb = lane + 32 < nwi ? rows[ri + lane + 32] : 0u;
     const int wA = qi + lane, wB = wA + 32;
 #pragma unroll 1
     for (int half = 0; half < 2; ++half) {
@@ -390,21 +398,20 @@ __device__ uint64_t cta_count_rows2(const uint32_t* rows, int nrows, const int32
 // keep the full-warp walk of cta_count_rows, the others run 2, 4 or 8 to a warp
 // (count_rows_grouped) so no lane idles on words past its row's end.
 template <int Q, class Sh = CtaMain>
-__device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int32_t* pre,
-                                          const int32_t* roff) {
+__device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int32_t* pre) {
   const int W = (s + 31) >> 5;
   // first row spanning at most t words: 32 * (W - t), clamped to [0, s]
   auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
   const int r16 = first(16), r8 = first(8), r4 = first(4);
   uint64_t acc = 0;
   if constexpr (Sh::kCap > 1024) {  // rows may span more than 32 words
-    if (r16 > 0) acc += cta_count_rows2<Q, Sh>(rows, r16, roff, W);
+    if (r16 > 0) acc += cta_count_rows2<Q, Sh>(rows, r16, W);
   } else {
-    if (r16 > 0) acc += cta_count_rows<Q, false, Sh>(rows, r16, pre, roff, W);
+    if (r16 > 0) acc += cta_count_rows<Q, false, Sh>(rows, r16, pre, W);
   }
-  acc += count_rows_grouped<Q, 16, Sh>(rows, roff, W, r16, r8);
-  acc += count_rows_grouped<Q, 8, Sh>(rows, roff, W, r8, r4);
-  acc += count_rows_grouped<Q, 4, Sh>(rows, roff, W, r4, s);
+  acc += count_rows_grouped<Q, 16, Sh>(rows, W, r16, r8);
+  acc += count_rows_grouped<Q, 8, Sh>(rows, W, r8, r4);
+  acc += count_rows_grouped<Q, 4, Sh>(rows, W, r4, s);
   return acc;
 }
 
@@ -413,7 +420,7 @@ __device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int
 // every candidate l > i, so the walk of cta_count_rows carries over level by level:
 // the next level's set is this level's set & R_l.
 template <int D>
-__device__ uint64_t rows_deep(const uint32_t* rows, const int32_t* roff, uint32_t m, int w, int qi) {
+__device__ uint64_t rows_deep(const uint32_t* rows, int W, uint32_t m, int w, int qi) {
   if constexpr (D == 1) {
     return (uint64_t)__popc(m);
   } else {
@@ -423,12 +430,15 @@ __device__ uint64_t rows_deep(const uint32_t* rows, const int32_t* roff, uint32_
       const int src = __ffs(nz) - 1;
       nz &= nz - 1;
       uint32_t bits = __shfl_sync(kFull, m, src);
+      const int ql = qi + src;  // block of every l of this word: row l = base + b (W - ql)
+      const bool on = m != 0u && w >= ql;
+      const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
+      const int sl = W - ql;
       while (bits) {
-        const int l = ((qi + src) << 5) + __ffs(bits) - 1;
+        const int b = __ffs(bits) - 1;
         bits &= bits - 1;
-        const int ql = l >> 5;
-        const uint32_t m2 = (m && w >= ql) ? (m & rows[roff[l] + (w - ql)]) : 0u;
-        acc += rows_deep<D - 1>(rows, roff, m2, w, qi);
+        const uint32_t m2 = on ? (m & Bl[b * sl]) : 0u;
+        acc += rows_deep<D - 1>(rows, W, m2, w, qi);
       }
     }
     return acc;
@@ -438,8 +448,8 @@ __device__ uint64_t rows_deep(const uint32_t* rows, const int32_t* roff, uint32_
 // rows_deep with G lanes per candidate set (32 / G sets per warp, one per group): group
 // ballots and shuffles, loops while any group has work.
 template <int D, int G>
-__device__ uint64_t rows_deep_grouped(const uint32_t* rows, const int32_t* roff, uint32_t m, int w,
-                                      int qi, int gbase) {
+__device__ uint64_t rows_deep_grouped(const uint32_t* rows, int W, uint32_t m, int w, int qi,
+                                      int gbase) {
   if constexpr (D == 1) {
     return (uint64_t)__popc(m);
   } else {
@@ -452,13 +462,16 @@ __device__ uint64_t rows_deep_grouped(const uint32_t* rows, const int32_t* roff,
       if (had) nz &= nz - 1;
       uint32_t bits = __shfl_sync(kFull, m, gbase + src);
       if (!had) bits = 0u;
+      const int ql = qi + src;
+      const bool on = m != 0u && w >= ql;
+      const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
+      const int sl = W - ql;
       while (__any_sync(kFull, bits != 0u)) {
         const bool hb = bits != 0u;
-        const int l = hb ? ((qi + src) << 5) + __ffs(bits) - 1 : 0;
+        const int b = hb ? __ffs(bits) - 1 : 0;
         if (hb) bits &= bits - 1;
-        const int ql = l >> 5;
-        const uint32_t m2 = (hb && m && w >= ql) ? (m & rows[roff[l] + (w - ql)]) : 0u;
-        acc += rows_deep_grouped<D - 1, G>(rows, roff, m2, w, qi, gbase);
+        const uint32_t m2 = (hb && on) ? (m & Bl[b * sl]) : 0u;
+        acc += rows_deep_grouped<D - 1, G>(rows, W, m2, w, qi, gbase);
       }
     }
     return acc;
@@ -466,8 +479,7 @@ __device__ uint64_t rows_deep_grouped(const uint32_t* rows, const int32_t* roff,
 }
 
 template <int Q, int G, class Sh = CtaMain>
-__device__ uint64_t count_deep_grouped(const uint32_t* rows, const int32_t* roff, int W,
-                                       int row_lo, int row_hi) {
+__device__ uint64_t count_deep_grouped(const uint32_t* rows, int W, int row_lo, int row_hi) {
   constexpr int kGroups = 32 / G;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane % G, gbase = lane - sub;
@@ -476,15 +488,15 @@ __device__ uint64_t count_deep_grouped(const uint32_t* rows, const int32_t* roff
     const int i = i0 + lane / G;
     const bool live = i < row_hi;
     const int qi = live ? (i >> 5) : 0, nwi = W - qi;
-    const uint32_t wi = (live && sub < nwi) ? rows[roff[i] + sub] : 0u;
-    acc += rows_deep_grouped<Q - 1, G>(rows, roff, wi, qi + sub, qi, gbase);
+    const uint32_t wi = (live && sub < nwi) ? rows[tri_row_off(i, W) + sub] : 0u;
+    acc += rows_deep_grouped<Q - 1, G>(rows, W, wi, qi + sub, qi, gbase);
   }
   return acc;
 }
 
 // Q-cliques for Q >= 5, rows tiered by the words they span as in cta_count_rows_tiered.
 template <int Q, class Sh = CtaMain>
-__device__ uint64_t cta_count_deep(const uint32_t* rows, int s, const int32_t* roff) {
+__device__ uint64_t cta_count_deep(const uint32_t* rows, int s) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int W = (s + 31) >> 5;
   auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
@@ -492,12 +504,12 @@ __device__ uint64_t cta_count_deep(const uint32_t* rows, int s, const int32_t* r
   uint64_t acc = 0;
   for (int i = warp; i < r16; i += Sh::kWarps) {
     const int qi = i >> 5, nwi = W - qi;
-    const uint32_t wi = lane < nwi ? rows[roff[i] + lane] : 0u;
-    acc += rows_deep<Q - 1>(rows, roff, wi, qi + lane, qi);
+    const uint32_t wi = lane < nwi ? rows[tri_row_off(i, W) + lane] : 0u;
+    acc += rows_deep<Q - 1>(rows, W, wi, qi + lane, qi);
   }
-  acc += count_deep_grouped<Q, 16, Sh>(rows, roff, W, r16, r8);
-  acc += count_deep_grouped<Q, 8, Sh>(rows, roff, W, r8, r4);
-  acc += count_deep_grouped<Q, 4, Sh>(rows, roff, W, r4, s);
+  acc += count_deep_grouped<Q, 16, Sh>(rows, W, r16, r8);
+  acc += count_deep_grouped<Q, 8, Sh>(rows, W, r8, r4);
+  acc += count_deep_grouped<Q, 4, Sh>(rows, W, r4, s);
   return acc;
 }
 
@@ -573,16 +585,14 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   int32_t* pre = (int32_t*)(sm + Sh::kOffPre);
   int32_t* hkey = (int32_t*)(sm + Sh::kOffHkey);
   uint16_t* hval = (uint16_t*)(sm + Sh::kOffHval);
-  uint32_t* cnt = (uint32_t*)(sm + Sh::kOffCnt);
+  uint32_t* cnt = (uint32_t*)(sm + Sh::kOffCnt);  // participation / multi shapes only
+  static_assert(!PART || Sh::kOffRows > Sh::kOffCnt, "participation needs the cnt region");
   uint32_t* rows = (uint32_t*)(sm + Sh::kOffRows);
   int32_t* wtot = (int32_t*)(sm + Sh::kOffMisc);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = (s + 31) >> 5;
 
   uint32_t* bloom = (uint32_t*)(sm + Sh::kOffBloom);
-  int32_t* roff = (int32_t*)(sm + Sh::kOffRowOff);  // word offset of row i (triangular layout)
-  if (Q >= 3)
-    for (int i = tid; i < s; i += Sh::kThreads) roff[i] = tri_row_off(i, W);
   for (int h = tid; h < Sh::kHash; h += Sh::kThreads) hkey[h] = -1;
   for (int h = tid; h < Sh::kBloomWords; h += Sh::kThreads) bloom[h] = 0u;
   if (Q >= 3)
@@ -604,10 +614,11 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
       if (hi - lo > kClipMin && ldg_i32(g.col + hi - 1) > smax0)
         hi = lower_pos(g.col, lo, hi, smax0 + 1);
     }
-    if constexpr (kVec) {  // 16-byte units from the aligned start; lb keeps the phase
+    if constexpr (kVec) {  // 16-byte units from the aligned start
+      // lb = aligned start (bits 0-39) | phase (40-41) | length (42-63): graphs hold
+      // fewer than 2^40 entries and a degree-oriented out-list fewer than sqrt(2E) < 2^21
       const long long a = lo & ~3ll;
-      lb[i] = a | (lo - a);
-      cnt[i] = (uint32_t)(hi - lo);
+      lb[i] = a | ((lo - a) << 40) | ((hi - lo) << 42);
       pre[i] = hi > lo ? (int32_t)((hi - a + 3) >> 2) : 0;
     } else {
       lb[i] = lo;
@@ -661,12 +672,12 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
         v[h] = make_int4(0, 0, 0, 0);
         if (k < total) {
           while (k >= pre[i + 1]) ++i;
-          const long long L = lb[i];
+          const unsigned long long L = (unsigned long long)lb[i];
           const int u = k - pre[i];
           iv[h] = i;
-          rel[h] = 4 * u - (int)(L & 3);  // element index of the unit's first word
-          len[h] = (int)cnt[i];
-          v[h] = __ldg((const int4*)(g.col + (L & ~3ll)) + u);
+          rel[h] = 4 * u - (int)((L >> 40) & 3);  // element index of the unit's first word
+          len[h] = (int)(L >> 42);
+          v[h] = __ldg((const int4*)(g.col + (long long)(L & ((1ull << 40) - 1))) + u);
         }
       }
 #pragma unroll
@@ -683,7 +694,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
           if (j < 0) continue;
           const int ii = iv[h];
           if (Q == 2) acc += 1;
-          else atomicOr(&rows[roff[ii] + (j >> 5) - (ii >> 5)], 1u << (j & 31));
+          else atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
         }
       }
     }
@@ -751,7 +762,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
             atomicAdd(&part.e[pv[t]], 1u);
           }
         } else {
-          atomicOr(&rows[roff[ii] + (j >> 5) - (ii >> 5)], 1u << (j & 31));
+          atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
           if (MULTI) {
             q2 += 1;
             atomicAdd(&cnt[ii], 1u);
@@ -771,10 +782,10 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
         atomicAdd(&part.e[sbase + i], cnt[i]);
       }
   }
-  if (Q == 3) acc = WGT ? cta_count_rows<3, true, Sh>(rows, s, pre, roff)
-                        : cta_count_rows_tiered<3, Sh>(rows, s, pre, roff);
-  if (Q == 4) acc = cta_count_rows_tiered<4, Sh>(rows, s, pre, roff);
-  if constexpr (Q >= 5) acc = cta_count_deep<Q, Sh>(rows, s, roff);
+  if (Q == 3) acc = WGT ? cta_count_rows<3, true, Sh>(rows, s, pre)
+                        : cta_count_rows_tiered<3, Sh>(rows, s, pre);
+  if (Q == 4) acc = cta_count_rows_tiered<4, Sh>(rows, s, pre);
+  if constexpr (Q >= 5) acc = cta_count_deep<Q, Sh>(rows, s);
   return acc;
 }
 
@@ -783,11 +794,11 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
 // PART credits the triangles (v0, v1, w): edges (v1, w) and (v0, w) and vertex w.
 // Without STORE only the size is produced (no capacity limit); WSUM adds d+(w) of every
 // member to *wsum (per thread).
-template <bool PART, bool STORE, bool WSUM = false>
+template <bool PART, bool STORE, bool WSUM = false, class Sh = CtaMain>
 __device__ int cta_intersect_into_S(const GView& g, char* sm, int32_t v0, int32_t v1, Part part,
                                     uint64_t* wsum = nullptr) {
   int32_t* S = (int32_t*)(sm + kOffS);
-  int32_t* wtot = (int32_t*)(sm + kOffMisc);
+  int32_t* wtot = (int32_t*)(sm + Sh::kOffMisc);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const longlong2 a = ldg_ll2(g.dptr + v0), b = ldg_ll2(g.dptr + v1);
   int n = 0;
@@ -1498,6 +1509,10 @@ __device__ __forceinline__ void emit(const GOut& o, int32_t v0, uint64_t r, uint
 // `part` instead of counting; kModeWeight (K <= 4) weights each clique by the out-degree
 // of its highest-ranked vertex; kModeMulti (K == 4) emits triangles to o.slot and
 // 4-cliques to o.slot2 and credits participation.
+// CTA shape of a kernel mode: the participation and multi modes keep per-member counters.
+template <int MODE>
+using CtaShapeOf = std::conditional_t<MODE == kModePart || MODE == kModeMulti, CtaMainCnt, CtaMain>;
+
 template <int K, int MODE>
 __global__ void __launch_bounds__(kCtaThreads, 2)
     k_clique(GView g, TaskLists t, QueueHeads* q, unsigned long long* count, uint32_t* err,
@@ -1506,6 +1521,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
   constexpr bool PART = MODE == kModePart || MULTI;
   constexpr int kMinS = MULTI ? 2 : K - 1;  // smallest out-degree that can contribute
   static_assert(!MULTI || K == 4, "multi mode runs the 4-clique machinery");
+  using ShK = CtaShapeOf<MODE>;
   extern __shared__ __align__(16) char sm[];
   __shared__ long long task_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1534,7 +1550,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
     constexpr bool kStore = MULTI || (MODE != kModePart && K - 2 >= 2);
     constexpr bool kWsum = MODE == kModeWeight && K == 3;
     uint64_t wsum = 0;
-    const int n = cta_intersect_into_S<PART, kStore, kWsum>(g, sm, v0, v1, part, &wsum);
+    const int n = cta_intersect_into_S<PART, kStore, kWsum, ShK>(g, sm, v0, v1, part, &wsum);
     if (n < 0) {
       if (tid == 0) atomicOr(err, ERR_CAPACITY);
     } else {
@@ -1545,12 +1561,12 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
         atomicAdd(&part.e[e01], (unsigned)n);
       }
       if (MULTI) {
-        const uint64_t k4 = n >= 2 ? cta_local<2, kModeCount>(g, sm, n, part, -1) : 0;
+        const uint64_t k4 = n >= 2 ? cta_local<2, kModeCount, ShK>(g, sm, n, part, -1) : 0;
         emit(o, v0, tid == 0 ? (uint64_t)n : 0, k4, acc);
       } else if (!PART && n > 0) {
         uint64_t r;
         if (K - 2 == 1) r = kWsum ? wsum : (tid == 0 ? (uint64_t)n : 0);  // |L| once per CTA
-        else r = cta_local<K - 2, MODE>(g, sm, n, part, -1);
+        else r = cta_local<K - 2, MODE, ShK>(g, sm, n, part, -1);
         if (MODE == kModeWeight) acc += r; else emit(o, v0, r, 0, acc);
       }
     }
@@ -1575,7 +1591,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
       for (int i = tid; i < s; i += kCtaThreads) S[i] = ldg_i32(g.col + d0.x + i);
       __syncthreads();
       uint64_t q2 = 0;
-      const uint64_t r = cta_local<K - 1, MODE>(g, sm, s, part, d0.x, &q2);
+      const uint64_t r = cta_local<K - 1, MODE, ShK>(g, sm, s, part, d0.x, &q2);
       if (PART) {
         // every local edge is a triangle containing v0
         const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
@@ -1847,7 +1863,8 @@ __global__ void __launch_bounds__(kHubThreads, 1)
 // Sets the dynamic shared-memory opt-in of `fn` once per device (bit d of `mask`;
 // devices >= 64 set it on every launch).
 template <class F>
-cudaError_t smem_optin(F fn, int bytes, std::atomic<unsigned long long>& mask) {
+cudaError_t smem_optin(F fn, int bytes, std::atomic<unsigned long long>& mask,
+                       int carveout_pct = -1) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -1855,6 +1872,10 @@ cudaError_t smem_optin(F fn, int bytes, std::atomic<unsigned long long>& mask) {
   if (!bit || !(mask.load(std::memory_order_acquire) & bit)) {
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
+    if (carveout_pct >= 0) {  // preferred shared-memory share of the unified L1
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carveout_pct);
+      if (e != cudaSuccess) return e;
+    }
     mask.fetch_or(bit, std::memory_order_acq_rel);
   }
   return cudaSuccess;
@@ -1879,9 +1900,13 @@ cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned
                      uint32_t* err, Part part, int grid, cudaStream_t s, GOut o = GOut{}) {
   // The shared-memory opt-in is a per-device function attribute.
   static std::atomic<unsigned long long> attr_devices{0};
-  cudaError_t e = smem_optin(k_clique<K, MODE>, kCtaSmem, attr_devices);
+  // count modes: two CTAs fit the 196 KB configuration (85 % of 228 KB), leaving 60 KB
+  // of L1 for the streamed lists
+  constexpr int kSmem = CtaShapeOf<MODE>::kSmem;
+  cudaError_t e = smem_optin(k_clique<K, MODE>, kSmem, attr_devices,
+                             kSmem == kCtaSmem ? 85 : -1);
   if (e != cudaSuccess) return e;
-  k_clique<K, MODE><<<grid, kCtaThreads, kCtaSmem, s>>>(g, t, q, count, err, part, o);
+  k_clique<K, MODE><<<grid, kCtaThreads, kSmem, s>>>(g, t, q, count, err, part, o);
   return cudaGetLastError();
 }
 

@@ -415,6 +415,8 @@ cudaError_t finish_graph(DevGraph& g, const int32_t* group, int num_groups, cuda
   const int db = bits_for(g.max_deg + 1);
   const int gb = group ? bits_for(num_groups) : 0;
   if (vb + db + gb > 64) return cudaErrorInvalidValue;
+  // the counting kernels pack a list position into 40 bits (clique.cu, count modes)
+  if (ne >= (int64_t(1) << 40)) return cudaErrorInvalidValue;
 
   uint64_t *keys = nullptr, *tmp = nullptr;
   const int64_t nk = std::max(nv, ne);
