@@ -219,10 +219,16 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
       const int sj = W - qj;
       if constexpr (Q == 3 && !WGT) {
         uint32_t part = 0;
-        while (bits) {
+        while (bits) {  // two members per pass: two independent load / AND / popc chains
           const int b = __ffs(bits) - 1;
           bits &= bits - 1;
-          if (on) part += __popc(wi & Bj[b * sj]);
+          const bool two = bits != 0u;
+          const int c = two ? __ffs(bits) - 1 : b;
+          bits &= bits - 1;
+          if (on) {
+            const uint32_t x = Bj[b * sj], y = Bj[c * sj];
+            part += __popc(wi & x) + (two ? __popc(wi & y) : 0);
+          }
         }
         acc += part;
       } else if constexpr (Q == 3) {
@@ -251,10 +257,16 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
             const bool on2 = m != 0u && w >= ql;
             const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
             const int sl = W - ql;
-            while (bits2) {
+            while (bits2) {  // two members per pass
               const int b2 = __ffs(bits2) - 1;
               bits2 &= bits2 - 1;
-              if (on2) part += __popc(m & Bl[b2 * sl]);
+              const bool two = bits2 != 0u;
+              const int c2 = two ? __ffs(bits2) - 1 : b2;
+              bits2 &= bits2 - 1;
+              if (on2) {
+                const uint32_t x = Bl[b2 * sl], y = Bl[c2 * sl];
+                part += __popc(m & x) + (two ? __popc(m & y) : 0);
+              }
             }
           }
           acc += part;
@@ -297,6 +309,22 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, int W, int row_lo, 
       const uint32_t* Bj = rows + tri_row_off(qj << 5, W) + (w - qj);
       const int sj = W - qj;
       uint32_t part = 0;
+      if constexpr (Q == 3) {
+        while (__any_sync(kFull, bits != 0u)) {  // two members per pass
+          const bool hb = bits != 0u;
+          const int b = hb ? __ffs(bits) - 1 : 0;
+          bits &= bits - 1;
+          const bool hc = bits != 0u;
+          const int c = hc ? __ffs(bits) - 1 : b;
+          bits &= bits - 1;
+          if (hb && on) {
+            const uint32_t x = Bj[b * sj], y = Bj[c * sj];
+            part += __popc(wi & x) + (hc ? __popc(wi & y) : 0);
+          }
+        }
+        acc += part;
+        continue;
+      }
       while (__any_sync(kFull, bits != 0u)) {
         const bool hb = bits != 0u;
         const int b = hb ? __ffs(bits) - 1 : 0;
@@ -316,11 +344,17 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, int W, int row_lo, 
             const bool on2 = m != 0u && w >= ql;
             const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
             const int sl = W - ql;
-            while (__any_sync(kFull, bits2 != 0u)) {
+            while (__any_sync(kFull, bits2 != 0u)) {  // two members per pass
               const bool hb2 = bits2 != 0u;
               const int b2 = hb2 ? __ffs(bits2) - 1 : 0;
-              if (hb2) bits2 &= bits2 - 1;
-              if (hb2 && on2) part += __popc(m & Bl[b2 * sl]);
+              bits2 &= bits2 - 1;
+              const bool hb3 = bits2 != 0u;
+              const int c2 = hb3 ? __ffs(bits2) - 1 : b2;
+              bits2 &= bits2 - 1;
+              if (hb2 && on2) {
+                const uint32_t x = Bl[b2 * sl], y = Bl[c2 * sl];
+                part += __popc(m & x) + (hb3 ? __popc(m & y) : 0);
+              }
             }
           }
         }
