@@ -219,15 +219,21 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
       const int sj = W - qj;
       if constexpr (Q == 3 && !WGT) {
         uint32_t part = 0;
-        while (bits) {  // two members per pass: two independent load / AND / popc chains
-          const int b = __ffs(bits) - 1;
-          bits &= bits - 1;
-          const bool two = bits != 0u;
-          const int c = two ? __ffs(bits) - 1 : b;
-          bits &= bits - 1;
+        while (bits) {  // four members per pass: independent load / AND / popc chains
+          int b[4];
+          bool h[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            h[u] = bits != 0u;
+            b[u] = h[u] ? __ffs(bits) - 1 : 0;
+            bits &= bits - 1;
+          }
           if (on) {
-            const uint32_t x = Bj[b * sj], y = Bj[c * sj];
-            part += __popc(wi & x) + (two ? __popc(wi & y) : 0);
+            uint32_t x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) x[u] = Bj[b[u] * sj];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) part += h[u] ? __popc(wi & x[u]) : 0u;
           }
         }
         acc += part;
@@ -257,15 +263,21 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
             const bool on2 = m != 0u && w >= ql;
             const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
             const int sl = W - ql;
-            while (bits2) {  // two members per pass
-              const int b2 = __ffs(bits2) - 1;
-              bits2 &= bits2 - 1;
-              const bool two = bits2 != 0u;
-              const int c2 = two ? __ffs(bits2) - 1 : b2;
-              bits2 &= bits2 - 1;
+            while (bits2) {  // four members per pass
+              int b[4];
+              bool h[4];
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                h[u] = bits2 != 0u;
+                b[u] = h[u] ? __ffs(bits2) - 1 : 0;
+                bits2 &= bits2 - 1;
+              }
               if (on2) {
-                const uint32_t x = Bl[b2 * sl], y = Bl[c2 * sl];
-                part += __popc(m & x) + (two ? __popc(m & y) : 0);
+                uint32_t x[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) x[u] = Bl[b[u] * sl];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) part += h[u] ? __popc(m & x[u]) : 0u;
               }
             }
           }
@@ -310,16 +322,21 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, int W, int row_lo, 
       const int sj = W - qj;
       uint32_t part = 0;
       if constexpr (Q == 3) {
-        while (__any_sync(kFull, bits != 0u)) {  // two members per pass
-          const bool hb = bits != 0u;
-          const int b = hb ? __ffs(bits) - 1 : 0;
-          bits &= bits - 1;
-          const bool hc = bits != 0u;
-          const int c = hc ? __ffs(bits) - 1 : b;
-          bits &= bits - 1;
-          if (hb && on) {
-            const uint32_t x = Bj[b * sj], y = Bj[c * sj];
-            part += __popc(wi & x) + (hc ? __popc(wi & y) : 0);
+        while (__any_sync(kFull, bits != 0u)) {  // four members per pass
+          int b[4];
+          bool h[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            h[u] = bits != 0u;
+            b[u] = h[u] ? __ffs(bits) - 1 : 0;
+            bits &= bits - 1;
+          }
+          if (h[0] && on) {
+            uint32_t x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) x[u] = Bj[b[u] * sj];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) part += h[u] ? __popc(wi & x[u]) : 0u;
           }
         }
         acc += part;
@@ -344,16 +361,21 @@ __device__ uint64_t count_rows_grouped(const uint32_t* rows, int W, int row_lo, 
             const bool on2 = m != 0u && w >= ql;
             const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
             const int sl = W - ql;
-            while (__any_sync(kFull, bits2 != 0u)) {  // two members per pass
-              const bool hb2 = bits2 != 0u;
-              const int b2 = hb2 ? __ffs(bits2) - 1 : 0;
-              bits2 &= bits2 - 1;
-              const bool hb3 = bits2 != 0u;
-              const int c2 = hb3 ? __ffs(bits2) - 1 : b2;
-              bits2 &= bits2 - 1;
-              if (hb2 && on2) {
-                const uint32_t x = Bl[b2 * sl], y = Bl[c2 * sl];
-                part += __popc(m & x) + (hb3 ? __popc(m & y) : 0);
+            while (__any_sync(kFull, bits2 != 0u)) {  // four members per pass
+              int b[4];
+              bool h[4];
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                h[u] = bits2 != 0u;
+                b[u] = h[u] ? __ffs(bits2) - 1 : 0;
+                bits2 &= bits2 - 1;
+              }
+              if (h[0] && on2) {
+                uint32_t x[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) x[u] = Bl[b[u] * sl];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) part += h[u] ? __popc(m & x[u]) : 0u;
               }
             }
           }
