@@ -40,9 +40,11 @@ namespace {
 //   lb[cap] i64 | S[cap + 4] i32 | pre[cap + 8] i32 | hkey[hash] i32 | hval[hash] u16 |
 //   [cnt[cap] u32] | rows[tri_words(cap)] u32 | bloom[512] u32 | misc[32] i64
 // cnt (per-member participation counters) exists in the participation and multi modes
-// only; the count modes keep each list's length in lb's top bits instead, so two main
-// CTAs of a count mode fit the 196 KB shared-memory configuration (60 KB of L1 left).
-// A row's word offset is computed (tri_row_off), not stored.
+// only; the count modes keep each list's length in lb's top bits instead.  A row's word
+// offset is computed (tri_row_off), not stored.  (Without cnt and the offsets two
+// count-mode CTAs fit the 196 KB shared-memory configuration, 60 KB of L1: measured no
+// faster, the launch is issue-bound; the space went to a 4096-slot hash instead, load
+// factor <= 1/4: R-MAT s22 4-clique 84.5 -> 83.1 ms.)
 // S has four words of slack: a bulk copy lands a list at its own 16-byte phase.
 // CtaMain is the persistent counting kernel's CTA (512 threads, 2 CTAs per SM, local
 // sets of up to 1024); CtaHub is the hub kernel's (1024 threads, 1 CTA per SM, up to
@@ -72,11 +74,11 @@ struct CtaShape {
   static_assert(kOffS % 16 == 0 && kOffMisc % 8 == 0 && 4 * kWarps <= 8 * 31,
                 "aligned regions; warp totals below the barrier");
 };
-using CtaMain = CtaShape<kCtaThreads, kCtaCap, 11>;           // count modes
-using CtaMainCnt = CtaShape<kCtaThreads, kCtaCap, 11, true>;  // participation / multi
+using CtaMain = CtaShape<kCtaThreads, kCtaCap, 12>;           // count modes
+using CtaMainCnt = CtaShape<kCtaThreads, kCtaCap, 12, true>;  // participation / multi
 using CtaHub = CtaShape<kHubThreads, kHubCap, 12>;
-static_assert(CtaMain::kRowsWords == 16896 && CtaMain::kHash == kHashSize, "main CTA shape");
-static_assert(2 * (CtaMain::kSmem + 1024) <= 196 * 1024, "count-mode CTAs leave 60 KB of L1");
+static_assert(CtaMain::kRowsWords == 16896, "main CTA shape");
+static_assert(2 * (CtaMain::kSmem + 1024) <= 228 * 1024, "two count-mode CTAs per SM");
 static_assert(CtaMain::kOffS == CtaMainCnt::kOffS && CtaMain::kOffMisc + 4096 == CtaMainCnt::kOffMisc,
               "the shapes differ only by cnt");
 constexpr int kOffS = CtaMain::kOffS;
@@ -1956,11 +1958,9 @@ cudaError_t launch_k(const GView& g, const TaskLists& t, QueueHeads* q, unsigned
                      uint32_t* err, Part part, int grid, cudaStream_t s, GOut o = GOut{}) {
   // The shared-memory opt-in is a per-device function attribute.
   static std::atomic<unsigned long long> attr_devices{0};
-  // count modes: two CTAs fit the 196 KB configuration (85 % of 228 KB), leaving 60 KB
-  // of L1 for the streamed lists
   constexpr int kSmem = CtaShapeOf<MODE>::kSmem;
   cudaError_t e = smem_optin(k_clique<K, MODE>, kSmem, attr_devices,
-                             kSmem == kCtaSmem ? 85 : -1);
+                             -1);
   if (e != cudaSuccess) return e;
   k_clique<K, MODE><<<grid, kCtaThreads, kSmem, s>>>(g, t, q, count, err, part, o);
   return cudaGetLastError();

@@ -7,7 +7,7 @@ namespace xgm {
 constexpr int kCtaThreads = 512;            // threads of the persistent counting CTA
 constexpr int kCtaWarps = kCtaThreads / 32;
 constexpr int kCtaCap = 1024;               // largest local set a CTA task holds
-constexpr int kHashSize = 2048;             // open-addressing table for the local set
+constexpr int kHashSize = 4096;             // open-addressing table for the local set
 constexpr int kWarpCap = 32;                // largest local set a warp task holds
 constexpr int kWideCap = 128;               // largest local set a wide-warp task holds
 constexpr int kWideWords = 4;               // bitmap words per row of a wide-warp task
