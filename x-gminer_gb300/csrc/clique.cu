@@ -28,6 +28,7 @@
 // eight-lane group tasks (s <= 8, four per warp), bucket-filtered search tasks, and
 // streaming warp tasks (s <= 32).
 #include <atomic>
+#include <cstddef>
 #include <type_traits>
 #include "clique.cuh"
 
@@ -113,6 +114,8 @@ struct WideSmem {
   uint32_t rows[kWideCap * kWideWords];  // full rows, word w of row i at [i*4 + w]
   uint32_t cnt[kWideCap];
 };
+static_assert(offsetof(WideSmem, rows) % 16 == 0 && sizeof(WideSmem) % 16 == 0,
+              "wide rows are read as uint4");
 constexpr int kOffWarpRegion = kCtaWarps * (int)sizeof(WideSmem);
 
 // Warp region: one per warp (s <= 32, one-word rows).
@@ -1482,7 +1485,45 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
         atomicAdd(&part.v[w.S[r]], (unsigned long long)w.cnt[r]);
         atomicAdd(&part.e[d0.x + r], w.cnt[r]);
       }
-  if (Q >= 3 && Q <= 4) {
+  if constexpr ((Q == 3 && !WGT) || Q == 4) {
+    // lane per row, its four words in registers; a member's row is one 128-bit load
+    // (rows are 16-byte aligned; words below a member's block are zero, so the full
+    // four-word AND needs no per-word branch)
+    static_assert(kWideWords == 4, "wide rows are one uint4");
+    const uint4* R4 = reinterpret_cast<const uint4*>(w.rows);
+    for (int r = lane; r < s; r += 32) {
+      const uint4 rr = R4[r];
+      const uint32_t rw[4] = {rr.x, rr.y, rr.z, rr.w};
+#pragma unroll
+      for (int wj = 0; wj < 4; ++wj) {
+        uint32_t bits = rw[wj];
+        while (bits) {
+          const int j = (wj << 5) + __ffs(bits) - 1;
+          bits &= bits - 1;
+          const uint4 rj = R4[j];
+          const uint32_t m0 = rr.x & rj.x, m1 = rr.y & rj.y, m2 = rr.z & rj.z, m3 = rr.w & rj.w;
+          if constexpr (Q == 3) {
+            acc += (uint32_t)(__popc(m0) + __popc(m1) + __popc(m2) + __popc(m3));
+          } else {
+            const uint32_t mw[4] = {m0, m1, m2, m3};
+            uint32_t part = 0;
+#pragma unroll
+            for (int wl = 0; wl < 4; ++wl) {
+              uint32_t b3 = mw[wl];
+              while (b3) {
+                const int l = (wl << 5) + __ffs(b3) - 1;
+                b3 &= b3 - 1;
+                const uint4 rl = R4[l];
+                part += __popc(m0 & rl.x) + __popc(m1 & rl.y) + __popc(m2 & rl.z) +
+                        __popc(m3 & rl.w);
+              }
+            }
+            acc += part;
+          }
+        }
+      }
+    }
+  } else if (Q == 3) {  // weighted: each clique by d+ of its top member
     for (int r = lane; r < s; r += 32) {
       const uint32_t* Rr = w.rows + r * kWideWords;
       for (int wj = r >> 5; wj < kWideWords; ++wj) {
