@@ -654,16 +654,29 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   const int W = (s + 31) >> 5;
 
   uint32_t* bloom = (uint32_t*)(sm + Sh::kOffBloom);
-  for (int h = tid; h < Sh::kHash; h += Sh::kThreads) hkey[h] = -1;
-  for (int h = tid; h < Sh::kBloomWords; h += Sh::kThreads) bloom[h] = 0u;
+  // Dense span: S is sorted, so when max(S) - S[0] < 32 * kHash (R-MAT's CTA tasks: their
+  // members are the top-ranked vertices) membership is a bitmap over [S[0], max(S)] in
+  // the hash-key region and a member's index is the per-word prefix (in the hash-value
+  // region) plus a popcount: no Bloom filter, no probes.  Else the hash table.
+  const int32_t sb0 = S[0];
+  const uint32_t span = (uint32_t)(S[s - 1] - sb0) + 1u;
+  const bool dense = span <= 32u * (uint32_t)Sh::kHash;  // same in every thread
+  uint32_t* bm = (uint32_t*)hkey;
+  uint16_t* bpre = hval;
+  if (dense) {
+    for (int h = tid; h < (int)((span + 31) >> 5); h += Sh::kThreads) bm[h] = 0u;
+  } else {
+    for (int h = tid; h < Sh::kHash; h += Sh::kThreads) hkey[h] = -1;
+    for (int h = tid; h < Sh::kBloomWords; h += Sh::kThreads) bloom[h] = 0u;
+  }
   if (Q >= 3)
     for (int x = tid; x < tri_words(s); x += Sh::kThreads) rows[x] = 0u;
   if (PART)
     for (int i = tid; i < s; i += Sh::kThreads) cnt[i] = 0u;
   // Only members S[i+1] .. max(S) can hit in row i: each list starts at the first
   // element >= S[i+1] and long lists end at max(S) (binary searches in the sorted global
-  // row), so the walk streams no element that cannot match.  At R-MAT scale 22 the
-  // start clip removes ~58 % of the CTA tasks' elements, the end clip ~0.4 %.
+  // row), so the walk streams no element that cannot match.  (At R-MAT scale 22 the two
+  // clips remove 1.2 % of the CTA tasks' 16.8 G elements: the lists sit above S[i+1].)
   const int32_t smax0 = S[s - 1];
   for (int i = tid; i < s; i += Sh::kThreads) {
     const longlong2 d = ldg_ll2(g.dptr + S[i]);
@@ -689,6 +702,15 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   __syncthreads();
   for (int i = tid; i < s; i += Sh::kThreads) {
     const int32_t x = S[i];
+    if (dense) {
+      // bit of x, and bpre[w] = members in words below w for the words since the
+      // previous member's (the last member's word is the last one queried)
+      const uint32_t off = (uint32_t)(x - sb0);
+      atomicOr(&bm[off >> 5], 1u << (off & 31));
+      const int w0 = i == 0 ? 0 : (int)(((uint32_t)(S[i - 1] - sb0) >> 5) + 1);
+      for (int w = w0; w <= (int)(off >> 5); ++w) bpre[w] = (uint16_t)i;
+      continue;
+    }
     uint32_t slot = hash_slot<Sh>(x);
     // s <= Sh::kCap < Sh::kHash members: an empty slot always exists
     for (int probe = 0; probe < Sh::kHash && atomicCAS(&hkey[slot], -1, x) != -1; ++probe)
@@ -707,132 +729,164 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   // flight before use.  Elements of a unit outside the clipped list (the other rows'
   // entries next to it) are masked by position.  Then the Bloom / hash test as below.
   if constexpr (kVec) {
-    for (int c = warp; c * 64 < total; c += Sh::kWarps) {
-      const int kb = c * 64 + lane;
-      int i;
-      {  // segment of the chunk start, as in the scalar walk below
-        constexpr int kR1 = Sh::kCap <= 1024 ? 32 : 64;
-        constexpr int kR2 = kR1 / 32;
-        const int k0 = c * 64;
-        const int c1 = lane * kR1;
-        const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
-        const int r1 = 31 - __clz(b1);
-        const int c2 = r1 * kR1 + lane * kR2;
-        const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
-        i = r1 * kR1 + (31 - __clz(b2)) * kR2;
-        while (i + 1 < s && pre[i + 1] <= kb) ++i;
-      }
-      int4 v[2];
-      int iv[2], rel[2], len[2];
+    // the membership test is chosen once per task (DENSE: span bitmap, else Bloom + hash)
+    auto walk = [&](auto dense_c) {
+      constexpr bool DENSE = decltype(dense_c)::value;
+      for (int c = warp; c * 64 < total; c += Sh::kWarps) {
+        const int kb = c * 64 + lane;
+        int i;
+        {  // segment of the chunk start, as in the scalar walk below
+          constexpr int kR1 = Sh::kCap <= 1024 ? 32 : 64;
+          constexpr int kR2 = kR1 / 32;
+          const int k0 = c * 64;
+          const int c1 = lane * kR1;
+          const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
+          const int r1 = 31 - __clz(b1);
+          const int c2 = r1 * kR1 + lane * kR2;
+          const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
+          i = r1 * kR1 + (31 - __clz(b2)) * kR2;
+          while (i + 1 < s && pre[i + 1] <= kb) ++i;
+        }
+        int4 v[2];
+        int iv[2], rel[2], len[2];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int k = kb + 32 * h;
-        iv[h] = i;
-        rel[h] = 0;
-        len[h] = 0;
-        v[h] = make_int4(0, 0, 0, 0);
-        if (k < total) {
-          while (k >= pre[i + 1]) ++i;
-          const unsigned long long L = (unsigned long long)lb[i];
-          const int u = k - pre[i];
+        for (int h = 0; h < 2; ++h) {
+          const int k = kb + 32 * h;
           iv[h] = i;
-          rel[h] = 4 * u - (int)((L >> 40) & 3);  // element index of the unit's first word
-          len[h] = (int)(L >> 42);
-          v[h] = __ldg((const int4*)(g.col + (long long)(L & ((1ull << 40) - 1))) + u);
-        }
-      }
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int32_t xs4[4] = {v[h].x, v[h].y, v[h].z, v[h].w};
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const int e = rel[h] + t;
-          const int32_t x = xs4[t];
-          if (e < 0 || e >= len[h] || x > smax) continue;
-          const uint32_t b = bloom_bit(x);
-          if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
-          const int j = hash_find<Sh>(hkey, hval, x);
-          if (j < 0) continue;
-          const int ii = iv[h];
-          if (Q == 2) acc += 1;
-          else atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
-        }
-      }
-    }
-  } else
-  // Flattened walk over all (i, element) pairs: warp chunks of 256 consecutive
-  // elements, lanes contiguous within a chunk so row reads are coalesced.  Each lane
-  // keeps its segment's base in registers, issues four loads before using them, and
-  // rejects most non-members with one Bloom-filter probe before the hash lookup.
-  for (int c = warp; c * 256 < total; c += Sh::kWarps) {
-    const int kb = c * 256 + lane;
-    int i;
-    {  // segment of the chunk start (largest i < s with pre[i] <= c * 256): a two-round
-       // 32-way search by the warp (strides kR1 then kR1 / 32), then each lane steps to
-       // its own segment
-      constexpr int kR1 = Sh::kCap <= 1024 ? 32 : 64;
-      static_assert(32 * kR1 >= Sh::kCap, "two search rounds cover the local set");
-      constexpr int kR2 = kR1 / 32;
-      const int k0 = c * 256;
-      const int c1 = lane * kR1;
-      const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
-      const int r1 = 31 - __clz(b1);  // b1 has bit 0: pre[0] = 0 <= k0
-      const int c2 = r1 * kR1 + lane * kR2;
-      const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
-      i = r1 * kR1 + (31 - __clz(b2)) * kR2;
-      while (i + 1 < s && pre[i + 1] <= kb) ++i;  // stays below s past the end
-    }
-    int seg_end = pre[i + 1];
-    long long seg_base = lb[i] - pre[i];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      int32_t xv[4];
-      int iv[4];
-      long long pv[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int k = kb + 32 * (4 * h + t);
-        xv[t] = 0x7FFFFFFF;  // above every id: rejected below
-        iv[t] = i;
-        pv[t] = 0;
-        if (k < total) {
-          while (k >= seg_end) {
-            ++i;
-            seg_end = pre[i + 1];
-            seg_base = lb[i] - pre[i];
+          rel[h] = 0;
+          len[h] = 0;
+          v[h] = make_int4(0, 0, 0, 0);
+          if (k < total) {
+            while (k >= pre[i + 1]) ++i;
+            const unsigned long long L = (unsigned long long)lb[i];
+            const int u = k - pre[i];
+            iv[h] = i;
+            rel[h] = 4 * u - (int)((L >> 40) & 3);  // element index of the unit's first word
+            len[h] = (int)(L >> 42);
+            v[h] = __ldg((const int4*)(g.col + (long long)(L & ((1ull << 40) - 1))) + u);
           }
-          pv[t] = seg_base + k;
-          iv[t] = i;
-          xv[t] = ldg_i32(g.col + pv[t]);
         }
-      }
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int32_t x = xv[t];
-        if (x > smax) continue;
-        const uint32_t b = bloom_bit(x);
-        if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
-        const int j = hash_find<Sh>(hkey, hval, x);
-        if (j < 0) continue;
-        const int ii = iv[t];
-        if (Q == 2) {
-          acc += WGT ? (uint64_t)(pre[j + 1] - pre[j]) : 1;
-          if (PART) {
-            atomicAdd(&cnt[ii], 1u);
-            atomicAdd(&cnt[j], 1u);
-            atomicAdd(&part.e[pv[t]], 1u);
-          }
-        } else {
-          atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
-          if (MULTI) {
-            q2 += 1;
-            atomicAdd(&cnt[ii], 1u);
-            atomicAdd(&cnt[j], 1u);
-            atomicAdd(&part.e[pv[t]], 1u);
+        for (int h = 0; h < 2; ++h) {
+          const int32_t xs4[4] = {v[h].x, v[h].y, v[h].z, v[h].w};
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int e = rel[h] + t;
+            const int32_t x = xs4[t];
+            if ((unsigned)e >= (unsigned)len[h]) continue;
+            int j;
+            if constexpr (DENSE) {
+              const uint32_t off = (uint32_t)(x - sb0);
+              if (off >= span) continue;
+              const uint32_t wv = bm[off >> 5], bit = 1u << (off & 31);
+              if (!(wv & bit)) continue;
+              j = bpre[off >> 5] + __popc(wv & (bit - 1u));
+            } else {
+              if (x > smax) continue;
+              const uint32_t b = bloom_bit(x);
+              if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
+              j = hash_find<Sh>(hkey, hval, x);
+              if (j < 0) continue;
+            }
+            const int ii = iv[h];
+            if (Q == 2) acc += 1;
+            else atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
           }
         }
       }
-    }
+    };
+    if (dense) walk(std::true_type{});
+    else walk(std::false_type{});
+  } else {
+    // Flattened walk over all (i, element) pairs: warp chunks of 256 consecutive
+    // elements, lanes contiguous within a chunk so row reads are coalesced.  Each lane
+    // keeps its segment's base in registers, issues four loads before using them, and
+    // rejects most non-members with one membership probe (span bitmap, or Bloom filter
+    // before the hash lookup).
+    auto walk = [&](auto dense_c) {
+      constexpr bool DENSE = decltype(dense_c)::value;
+      for (int c = warp; c * 256 < total; c += Sh::kWarps) {
+        const int kb = c * 256 + lane;
+        int i;
+        {  // segment of the chunk start (largest i < s with pre[i] <= c * 256): a two-round
+           // 32-way search by the warp (strides kR1 then kR1 / 32), then each lane steps to
+           // its own segment
+          constexpr int kR1 = Sh::kCap <= 1024 ? 32 : 64;
+          static_assert(32 * kR1 >= Sh::kCap, "two search rounds cover the local set");
+          constexpr int kR2 = kR1 / 32;
+          const int k0 = c * 256;
+          const int c1 = lane * kR1;
+          const unsigned b1 = __ballot_sync(kFull, c1 < s && pre[c1] <= k0);
+          const int r1 = 31 - __clz(b1);  // b1 has bit 0: pre[0] = 0 <= k0
+          const int c2 = r1 * kR1 + lane * kR2;
+          const unsigned b2 = __ballot_sync(kFull, c2 < s && pre[c2] <= k0);
+          i = r1 * kR1 + (31 - __clz(b2)) * kR2;
+          while (i + 1 < s && pre[i + 1] <= kb) ++i;  // stays below s past the end
+        }
+        int seg_end = pre[i + 1];
+        long long seg_base = lb[i] - pre[i];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          int32_t xv[4];
+          int iv[4];
+          long long pv[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int k = kb + 32 * (4 * h + t);
+            xv[t] = 0x7FFFFFFF;  // above every id: rejected below
+            iv[t] = i;
+            pv[t] = 0;
+            if (k < total) {
+              while (k >= seg_end) {
+                ++i;
+                seg_end = pre[i + 1];
+                seg_base = lb[i] - pre[i];
+              }
+              pv[t] = seg_base + k;
+              iv[t] = i;
+              xv[t] = ldg_i32(g.col + pv[t]);
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int32_t x = xv[t];
+            int j;
+            if constexpr (DENSE) {
+              const uint32_t off = (uint32_t)(x - sb0);
+              if (off >= span) continue;
+              const uint32_t wv = bm[off >> 5], bit = 1u << (off & 31);
+              if (!(wv & bit)) continue;
+              j = bpre[off >> 5] + __popc(wv & (bit - 1u));
+            } else {
+              if (x > smax) continue;
+              const uint32_t b = bloom_bit(x);
+              if (!((bloom[b >> 5] >> (b & 31)) & 1u)) continue;
+              j = hash_find<Sh>(hkey, hval, x);
+              if (j < 0) continue;
+            }
+            const int ii = iv[t];
+            if (Q == 2) {
+              acc += WGT ? (uint64_t)(pre[j + 1] - pre[j]) : 1;
+              if (PART) {
+                atomicAdd(&cnt[ii], 1u);
+                atomicAdd(&cnt[j], 1u);
+                atomicAdd(&part.e[pv[t]], 1u);
+              }
+            } else {
+              atomicOr(&rows[tri_row_off(ii, W) + (j >> 5) - (ii >> 5)], 1u << (j & 31));
+              if (MULTI) {
+                q2 += 1;
+                atomicAdd(&cnt[ii], 1u);
+                atomicAdd(&cnt[j], 1u);
+                atomicAdd(&part.e[pv[t]], 1u);
+              }
+            }
+          }
+        }
+      }
+    };
+    if (dense) walk(std::true_type{});
+    else walk(std::false_type{});
   }
   if (MULTI) *q2out = q2;
   __syncthreads();
