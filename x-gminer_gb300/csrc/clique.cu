@@ -254,6 +254,10 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
           }
         }
       } else {
+        // Q == 4: m = R_i & R_j, lane w holding word w; each member l of m is a lane of
+        // its own: for every nonzero word ql of m, lane b takes l = 32 ql + b when bit b
+        // is set, and adds popc(m & R_l) over the nonzero words of m from ql on (m's bits
+        // cluster in a few words: at R-MAT scale 19, 36 members in 2.8 words per pair)
         while (bits) {
           const int b = __ffs(bits) - 1;
           bits &= bits - 1;
@@ -262,28 +266,18 @@ __device__ __forceinline__ uint64_t cta_count_rows(const uint32_t* rows, int n, 
           uint32_t part = 0;
           while (nz2) {
             const int src2 = __ffs(nz2) - 1;
-            nz2 &= nz2 - 1;
-            uint32_t bits2 = __shfl_sync(kFull, m, src2);
+            const uint32_t bq = __shfl_sync(kFull, m, src2);
             const int ql = qi + src2;
-            const bool on2 = m != 0u && w >= ql;
-            const uint32_t* Bl = rows + tri_row_off(ql << 5, W) + (w - ql);
-            const int sl = W - ql;
-            while (bits2) {  // four members per pass
-              int b[4];
-              bool h[4];
-#pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                h[u] = bits2 != 0u;
-                b[u] = h[u] ? __ffs(bits2) - 1 : 0;
-                bits2 &= bits2 - 1;
-              }
-              if (on2) {
-                uint32_t x[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) x[u] = Bl[b[u] * sl];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) part += h[u] ? __popc(m & x[u]) : 0u;
-              }
+            const bool act = (bq >> lane) & 1u;
+            // row l = 32 ql + lane, its word w2 at Rl[w2 - qi]
+            const uint32_t* Rl = rows + tri_row_off(ql << 5, W) + lane * (W - ql) + (qi - ql);
+            unsigned rest = nz2;
+            nz2 &= nz2 - 1;
+            while (rest) {
+              const int s3 = __ffs(rest) - 1;
+              rest &= rest - 1;
+              const uint32_t mw = __shfl_sync(kFull, m, s3);
+              if (act) part += __popc(mw & Rl[s3]);
             }
           }
           acc += part;
@@ -465,6 +459,10 @@ __device__ uint64_t cta_count_rows_tiered(const uint32_t* rows, int s, const int
   auto first = [&](int t) { const int r = 32 * (W - t); return r < 0 ? 0 : (r > s ? s : r); };
   const int r16 = first(16), r8 = first(8), r4 = first(4);
   uint64_t acc = 0;
+  if constexpr (Q == 4 && Sh::kCap <= 1024) {
+    // the 5-clique count runs lane per member of m (cta_count_rows): no word tiers
+    return cta_count_rows<4, false, Sh>(rows, s, pre, W);
+  }
   if constexpr (Sh::kCap > 1024) {  // rows may span more than 32 words
     if (r16 > 0) acc += cta_count_rows2<Q, Sh>(rows, r16, W);
   } else {
