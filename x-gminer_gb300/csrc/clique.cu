@@ -671,21 +671,17 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
     for (int x = tid; x < tri_words(s); x += Sh::kThreads) rows[x] = 0u;
   if (PART)
     for (int i = tid; i < s; i += Sh::kThreads) cnt[i] = 0u;
-  // Only members S[i+1] .. max(S) can hit in row i: each list starts at the first
-  // element >= S[i+1] and long lists end at max(S) (binary searches in the sorted global
-  // row), so the walk streams no element that cannot match.  (At R-MAT scale 22 the two
-  // clips remove 1.2 % of the CTA tasks' 16.8 G elements: the lists sit above S[i+1].)
-  const int32_t smax0 = S[s - 1];
+  // Row i's list is streamed whole: only members S[i+1] .. max(S) can hit, but clipping
+  // it to that range (two binary searches in the global row) removes 1.2 % of the CTA
+  // tasks' 16.8 G elements at R-MAT scale 22 and cost more in the setup than it saved
+  // (4-clique 73.2 -> 69.1 ms without it); the membership test rejects the rest.  The
+  // last member has no later member to hit (not in weighted mode: its weights are the
+  // full out-degrees pre[j+1] - pre[j]).
   for (int i = tid; i < s; i += Sh::kThreads) {
     const longlong2 d = ldg_ll2(g.dptr + S[i]);
-    long long lo = d.x, hi = d.y;
-    // (not in weighted mode: its weights are the full out-degrees pre[j+1] - pre[j])
-    if (!WGT) {
-      if (i + 1 == s) lo = hi;  // the last member has no later member to hit
-      else if (hi - lo > kClipLoMin) lo = lower_pos(g.col, lo, hi, S[i + 1]);
-      if (hi - lo > kClipMin && ldg_i32(g.col + hi - 1) > smax0)
-        hi = lower_pos(g.col, lo, hi, smax0 + 1);
-    }
+    long long lo = d.x;
+    const long long hi = d.y;
+    if (!WGT && i + 1 == s) lo = hi;
     if constexpr (kVec) {  // 16-byte units from the aligned start
       // lb = aligned start (bits 0-39) | phase (40-41) | length (42-63): graphs hold
       // fewer than 2^40 entries and a degree-oriented out-list fewer than sqrt(2E) < 2^21
