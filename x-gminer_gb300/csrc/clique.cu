@@ -88,6 +88,7 @@ constexpr int kCtaSmemCnt = CtaMainCnt::kSmem;
 constexpr int kHubSmem = CtaHub::kSmem;
 static_assert(kHubSmem <= 227 * 1024, "hub CTA fits one SM's shared memory");
 constexpr int kWalkUnits = 4;   // 16-byte units per lane in flight in the CTA walk
+constexpr int kWideUnits = 2;   // the same in the wide-warp walk
 constexpr int kClipMin = 96;    // lists longer than this are clipped at max(S)
 constexpr int kClipLoMin = 8;   // lists longer than this start at the next member of S
 
@@ -1451,12 +1452,13 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
   const int total = w.pre[s];
   uint64_t acc = 0, q2 = 0;
   int i = 0;
-  if constexpr (kVec) {  // two 16-byte units per lane in flight, then their 8 elements
-    for (int kb = lane; kb < total; kb += 64) {
-      int4 v[2];
-      int iv[2], rel[2], ln[2];
+  if constexpr (kVec) {  // kWideUnits 16-byte units per lane in flight, then their elements
+    constexpr int kNU = kWideUnits;
+    for (int kb = lane; kb < total; kb += 32 * kNU) {
+      int4 v[kNU];
+      int iv[kNU], rel[kNU], ln[kNU];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < kNU; ++h) {
         const int k = kb + 32 * h;
         iv[h] = i;
         rel[h] = 0;
@@ -1473,7 +1475,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
         }
       }
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < kNU; ++h) {
         const int32_t xs4[4] = {v[h].x, v[h].y, v[h].z, v[h].w};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
