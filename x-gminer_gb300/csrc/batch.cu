@@ -248,6 +248,9 @@ xgm_status batch_sequence(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P,
     GOut o{g.gid, b->d_out, P, sl.tri, sl.k4};
     XGM_CUDA_TRY(launch_multi(view, b->tb.lists(false), &b->d_sc->q, b->vpart, b->epart,
                               &b->d_sc->err, grid, s, o));
+    // the multi launch's task lists, for the stats
+    XGM_CUDA_TRY(cudaMemcpyAsync(b->d_sc->n, b->tb.n, sizeof(int64_t) * 8,
+                                 cudaMemcpyDeviceToDevice, s));
     if (part)
       XGM_CUDA_TRY(launch_part_reduce_graphs(view, g.gid, b->vpart, b->epart, b->d_out, P, sl.dia,
                                              sl.tail, s));
@@ -348,6 +351,17 @@ xgm_status count_batched_impl(xgm_ctx* ctx, xgm_batch* b, const xgm_plan* const*
   st.kernel_ms = ms;
   st.device_error = b->h_sc->err;
   st.tasks = b->graph.g.nv;
+  if (sl.tri >= 0 || sl.k4 >= 0 || sl.dia >= 0 || sl.tail >= 0) {
+    // vertex tasks per variant of the multi-pattern launch
+    const int64_t* n = b->h_sc->n;
+    st.variant_tasks[XGM_VAR_WARP] = n[2];
+    st.variant_tasks[XGM_VAR_CTA] = n[1];
+    st.variant_tasks[XGM_VAR_SPLIT] = n[0];
+    st.variant_tasks[XGM_VAR_WIDE] = n[4];
+    st.variant_tasks[XGM_VAR_SEARCH] = n[5];
+    st.variant_tasks[XGM_VAR_BUCKET] = n[6];
+    st.variant_tasks[XGM_VAR_GROUP] = n[7];
+  }
   r = check_device_flag(ctx, b->h_sc->err);
   if (r != XGM_OK) return r;
   std::memcpy(out, b->h_out, sizeof(uint64_t) * (size_t)b->num_graphs * P);
