@@ -215,6 +215,7 @@ xgm_status batch_prepare(xgm_ctx* ctx, xgm_batch* b, const Slots& sl, int P,
   }
   ensure_clique_grid(ctx);
   if (sched_may_bucket(sp)) XGM_CUDA_TRY(ensure_bucket_index(g, s));  // before any capture
+  if (sp.policy == XGM_SCHED_LEARNED) XGM_CUDA_TRY(ensure_task_stats(g, s));
   XGM_CUDA_TRY(cudaStreamSynchronize(s));
   return XGM_OK;
 }

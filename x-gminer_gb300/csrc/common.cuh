@@ -38,6 +38,8 @@ struct GView {
   const int32_t* bcol = nullptr;    // [E] bucket-grouped out-lists (same row positions)
   const uint32_t* boff = nullptr;   // [16 V] bucket starts within each out-list
   const uint16_t* bmask = nullptr;  // [V] non-empty buckets
+  const int64_t* tsum = nullptr;    // [V] sum of the out-neighbours' out-degrees
+  const int32_t* tmax = nullptr;    // [V] largest out-neighbour out-degree
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -72,6 +72,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
     }
     order = sp.order_by_cost != 0;
     XGM_CUDA_TRY(ensure_bucket_index(g, s));  // the model may pick BUCKET
+    XGM_CUDA_TRY(ensure_task_stats(g, s));
     XGM_CUDA_TRY(classify_learned(g, k, *sp.model, tb, order, sp.margin, s, k_feat));
   } else if (sp.policy == XGM_SCHED_TUNED) {
     if (!sp.table) {

@@ -330,7 +330,7 @@ cudaError_t dalloc(T** p, int64_t n, cudaStream_t s) {
 
 void free_graph(DevGraph& g, cudaStream_t s) {
   void* ps[] = {g.rowptr_o, g.col_o, g.rank, g.perm, g.rowptr, g.col, g.dptr, g.gid,
-                g.bcol, g.boff, g.bmask, g.lut_rows, g.lut_off};
+                g.bcol, g.boff, g.bmask, g.lut_rows, g.lut_off, g.tsum, g.tmax};
   for (void* p : ps)
     if (p) cudaFreeAsync(p, s);
   g = DevGraph{};

@@ -33,11 +33,19 @@ struct DevGraph {
   mutable uint32_t* lut_rows = nullptr;
   mutable int64_t* lut_off = nullptr;
   mutable int lut_state = 0;
+  // out-neighbour degree sums / maxima (the learned schedule's task features), built on
+  // first use by the learned schedule
+  mutable int64_t* tsum = nullptr;
+  mutable int32_t* tmax = nullptr;
 
-  GView view() const { return GView{col, rowptr, dptr, nv, bcol, boff, bmask}; }
+  GView view() const { return GView{col, rowptr, dptr, nv, bcol, boff, bmask, tsum, tmax}; }
 };
 
 void free_graph(DevGraph& g, cudaStream_t s);
+
+// Builds g's out-neighbour degree sums and maxima once (learned.cu); later calls return
+// at once.
+cudaError_t ensure_task_stats(const DevGraph& g, cudaStream_t s);
 
 // Builds g's bucket index once (bucket.cu); later calls return at once.
 cudaError_t ensure_bucket_index(const DevGraph& g, cudaStream_t s);

@@ -47,11 +47,16 @@ __device__ void task_features(const GView& g, int32_t r, int k, float* f) {
   const longlong2 d0 = g.dptr[r];
   const long long s = d0.y - d0.x;
   long long sum = 0, maxd = 0;
-  for (long long e = d0.x; e < d0.y; ++e) {
-    const longlong2 d = g.dptr[g.col[e]];
-    const long long l = d.y - d.x;
-    sum += l;
-    maxd = l > maxd ? l : maxd;
+  if (g.tsum) {  // precomputed (ensure_task_stats)
+    sum = g.tsum[r];
+    maxd = g.tmax[r];
+  } else {
+    for (long long e = d0.x; e < d0.y; ++e) {
+      const longlong2 d = g.dptr[g.col[e]];
+      const long long l = d.y - d.x;
+      sum += l;
+      maxd = l > maxd ? l : maxd;
+    }
   }
   // 0-3 task shape, 4 clique depth, 5-11 variant one-hot (caller)
   f[0] = log2f(1.0f + (float)s) / 11.0f;
@@ -121,7 +126,8 @@ __global__ void k_classify_learned(GView g, int k, int k_feat, const __half* wh,
       cand[v] = !(((v == XGM_VAR_WARP || v == XGM_VAR_SEARCH || v == XGM_VAR_BUCKET) &&
                    s > kWarpCap) ||
                   (v == XGM_VAR_GROUP && s > kGroupCap) ||
-                  (v == XGM_VAR_WIDE && s > kWideCap) || (v == XGM_VAR_CTA && s > kCtaCap) ||
+                  (v == XGM_VAR_WIDE && (s > kWideCap || s <= kWarpCap)) ||
+                  (v == XGM_VAR_CTA && s > kCtaCap) ||
                   (v == XGM_VAR_SPLIT && s <= kCtaCap));
       ncand += cand[v];
     }
@@ -267,6 +273,57 @@ int clique_k(int pattern) {
 }
 
 }  // namespace
+
+// Out-neighbour degree sum and maximum of every vertex, a warp per vertex (coalesced over
+// its out-list): the features task_features would otherwise gather serially per task.
+__global__ void k_task_stats(GView g, int64_t* tsum, int32_t* tmax) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < g.nv; r += warps) {
+    const longlong2 d0 = g.dptr[r];
+    long long sum = 0, maxd = 0;
+    for (long long e = d0.x + lane; e < d0.y; e += 32) {
+      const longlong2 d = g.dptr[g.col[e]];
+      const long long l = d.y - d.x;
+      sum += l;
+      maxd = l > maxd ? l : maxd;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sum += __shfl_xor_sync(kFull, sum, o);
+      const long long y = __shfl_xor_sync(kFull, maxd, o);
+      maxd = y > maxd ? y : maxd;
+    }
+    if (lane == 0) {
+      tsum[r] = sum;
+      tmax[r] = (int32_t)maxd;
+    }
+  }
+}
+
+cudaError_t ensure_task_stats(const DevGraph& g, cudaStream_t s) {
+  if (g.tsum || g.nv == 0) return cudaSuccess;
+  int64_t* tsum = nullptr;
+  int32_t* tmax = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&tsum, sizeof(int64_t) * (size_t)g.nv, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&tmax, sizeof(int32_t) * (size_t)g.nv, s);
+  if (e != cudaSuccess) {
+    if (tsum) cudaFreeAsync(tsum, s);
+    return e;
+  }
+  int64_t blocks = (g.nv + kThreads / 32 - 1) / (kThreads / 32);
+  if (blocks > 65536) blocks = 65536;
+  k_task_stats<<<(unsigned)blocks, kThreads, 0, s>>>(g.view(), tsum, tmax);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaFreeAsync(tsum, s);
+    cudaFreeAsync(tmax, s);
+    return e;
+  }
+  g.tsum = tsum;
+  g.tmax = tmax;
+  return cudaSuccess;
+}
 
 cudaError_t classify_learned(const DevGraph& g, int k, const xgm_model& m, TaskBuf& tb,
                              bool need_cost, float margin, cudaStream_t s, int k_feat) {
