@@ -230,7 +230,9 @@ typedef struct {
   int cta_max;            /* heuristic: out-degree <= cta_max -> CTA, else SPLIT (0: default 1024) */
   int order_by_cost;      /* learned: 1 = heaviest predicted tasks first */
   const xgm_tune_table* table; /* for XGM_SCHED_TUNED */
-  int flags;              /* XGM_SCHED_NO_GRAPH: batched calls launch directly, no CUDA graph */
+  int flags;              /* XGM_SCHED_NO_GRAPH: batched calls launch directly, no CUDA graph;
+                             XGM_SCHED_HASH_ONLY: CTA tasks test membership with the Bloom
+                             filter and hash even where the span bitmap fits (same counts) */
   int wide_max;           /* heuristic: out-degree <= wide_max -> WIDE (0: default 128; -1: none) */
   int search_max;         /* heuristic: out-degree <= search_max -> SEARCH (0: none) */
   int bucket_max;         /* heuristic: out-degree <= bucket_max -> BUCKET (0: none) */
@@ -245,7 +247,7 @@ typedef struct {
                              hub split) */
 } xgm_sched;
 
-enum { XGM_SCHED_NO_GRAPH = 1 };
+enum { XGM_SCHED_NO_GRAPH = 1, XGM_SCHED_HASH_ONLY = 2 };
 
 typedef struct {
   double kernel_ms;        /* device time of the counting launch(es) */

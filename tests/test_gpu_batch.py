@@ -39,6 +39,7 @@ def test_batched_counts_match_oracle(xgm, ctx, orc, ba_batch):
     # replay of the captured CUDA graph, direct launches and a subset of plans agree
     assert np.array_equal(ctx.count_batched(b, PATTERNS), got)
     assert np.array_equal(ctx.count_batched(b, PATTERNS, use_graph=False), got)
+    assert np.array_equal(ctx.count_batched(b, PATTERNS, hash_only=True), got)
     sub = ctx.count_batched(b, ["diamond", "triangle"])
     assert np.array_equal(sub[:, 0], got[:, 2]) and np.array_equal(sub[:, 1], got[:, 0])
 

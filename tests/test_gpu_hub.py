@@ -31,6 +31,8 @@ def test_hub_kernel_complete_graph(xgm, ctx):
             got, st = ctx.count(g, pat, with_stats=True, hub_max=1536)
             assert got == math.comb(n, k), pat
             assert st["launches"] == 2, "the hub kernel ran"
+            # the same with the Bloom filter + hash membership test in every CTA task
+            assert ctx.count(g, pat, hub_max=1536, hash_only=True) == math.comb(n, k), pat
         # split hubs: a triangle sub-task only counts its intersection ...
         assert ctx.count(g, "triangle", hub_max=-1) == math.comb(n, 3)
         assert ctx.count(g, "triangle", hub_max=1200) == math.comb(n, 3)

@@ -76,6 +76,29 @@ def test_schedules_never_change_counts(xgm, ctx):
             assert ctx.count(g, pat, group_max=gmax, bucket_max=bmax) == base, (pat, gmax)
 
 
+@pytest.mark.parametrize("gen", ["chung_lu", "rmat_dense", "ba"])
+def test_membership_paths_agree(xgm, ctx, orc, gen):
+    """CTA tasks test membership of a streamed element with a bitmap over the local
+    set's id span when it fits, else with a Bloom filter and a hash; XGM_SCHED_HASH_ONLY
+    forces the second path.  Every vertex task runs as a CTA task (SCHED_FIXED CTA), so
+    both paths see every task; counts equal the oracle's either way."""
+    if gen == "chung_lu":
+        nv, s, d = xgm.gen_chung_lu(1 << 13, 2.1, 1500.0, 24.0, seed=4)
+    elif gen == "rmat_dense":
+        nv, s, d = xgm.gen_rmat(11, 64, seed=5)
+    else:
+        nv, s, d = xgm.gen_ba(20000, 7, seed=7)
+    g = ctx.graph_from_edges(nv, s, d)
+    rowptr, col = orc.build_csr(nv, s, d)
+    want = oracle_counts(orc, rowptr, col)
+    for hash_only in (False, True):
+        got = {k: ctx.count(g, p, policy=xgm.SCHED_FIXED, variant=xgm.VAR_CTA,
+                            hash_only=hash_only) for k, p in KIND_TO_PATTERN.items()}
+        assert got == want, (gen, hash_only)
+        assert {k: ctx.count(g, p, hash_only=hash_only)
+                for k, p in KIND_TO_PATTERN.items()} == want, (gen, hash_only)
+
+
 def test_upload_paths_agree(xgm, ctx, orc):
     nv, s, d = xgm.gen_ba(5000, 6, seed=13)
     rowptr, col = orc.build_csr(nv, s, d)

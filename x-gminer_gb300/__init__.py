@@ -54,6 +54,7 @@ MOTIF4_NAMES = ["3-star", "4-path", "tailed-triangle", "4-cycle", "diamond", "4-
 
 SCHED_HEURISTIC, SCHED_LEARNED, SCHED_FIXED, SCHED_TUNED = 0, 1, 2, 3
 SCHED_NO_GRAPH = 1
+SCHED_HASH_ONLY = 2  # CTA tasks use the Bloom filter + hash, never the span bitmap
 TUNE_BUCKETS = 16
 VAR_WARP, VAR_CTA, VAR_SPLIT, VAR_WIDE, VAR_SEARCH, VAR_BUCKET, VAR_GROUP = 0, 1, 2, 3, 4, 5, 6
 NUM_VARIANTS = 7
@@ -282,10 +283,11 @@ class Context:
               order_by_cost: int = 1, table: Optional[TuneTable] = None,
               wide_max: int = 0, search_max: int = 0, bucket_max: int = 0,
               group_max: int = 0, margin: float = 0.0, hub_max: int = 0,
-              with_stats: bool = False):
+              hash_only: bool = False, with_stats: bool = False):
         plan = pattern if isinstance(pattern, Plan) else self.plan(pattern)
         sp = self._sched(policy, variant, model, warp_max, cta_max, order_by_cost, table,
-                         wide_max=wide_max, search_max=search_max, bucket_max=bucket_max,
+                         SCHED_HASH_ONLY if hash_only else 0, wide_max=wide_max,
+                         search_max=search_max, bucket_max=bucket_max,
                          group_max=group_max, margin=margin, hub_max=hub_max)
         out = C.c_uint64()
         st = Stats()
@@ -341,11 +343,12 @@ class Context:
                       model: Optional["Model"] = None, table: Optional[TuneTable] = None,
                       use_graph: bool = True, order_by_cost: int = 1, margin: float = 0.0,
                       group_max: int = 0, bucket_max: int = 0, search_max: int = 0,
-                      hub_max: int = 0, with_stats: bool = False):
+                      hub_max: int = 0, hash_only: bool = False, with_stats: bool = False):
         plans = [p if isinstance(p, Plan) else self.plan(p) for p in patterns]
         arr = (C.c_void_p * len(plans))(*[p._h.value for p in plans])
         sp = self._sched(policy, 0, model, 0, 0, order_by_cost, table,
-                         0 if use_graph else SCHED_NO_GRAPH, search_max=search_max,
+                         (0 if use_graph else SCHED_NO_GRAPH) |
+                         (SCHED_HASH_ONLY if hash_only else 0), search_max=search_max,
                          bucket_max=bucket_max, group_max=group_max, margin=margin,
                          hub_max=hub_max)
         out = np.empty(batch.num_graphs * len(plans), dtype=np.uint64)

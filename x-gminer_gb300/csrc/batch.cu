@@ -289,6 +289,8 @@ std::string sched_key(const Slots& sl, const xgm_sched& sp) {
   const int more[4] = {sp.wide_max, sp.search_max, sp.bucket_max, sp.group_max};
   k.append(reinterpret_cast<const char*>(more), sizeof(more));
   k.append(reinterpret_cast<const char*>(&sp.margin), sizeof(float));
+  const int hash_only = sp.flags & XGM_SCHED_HASH_ONLY;
+  k.append(reinterpret_cast<const char*>(&hash_only), sizeof(int));
   if (sp.table) k.append(reinterpret_cast<const char*>(sp.table), sizeof(xgm_tune_table));
   return k;
 }

@@ -627,7 +627,7 @@ struct Part {
 // credit is the returned count.
 template <int Q, int MODE, class Sh = CtaMain>
 __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long long sbase,
-                              uint64_t* q2out = nullptr, int s_off = 0) {
+                              uint64_t* q2out = nullptr, int s_off = 0, bool span_ok = true) {
   constexpr bool MULTI = MODE == kModeMulti;  // Q == 3: also local edges + participation
   constexpr bool PART = MODE == kModePart || MULTI;
   constexpr bool WGT = MODE == kModeWeight;
@@ -662,7 +662,7 @@ __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long l
   // region) plus a popcount: no Bloom filter, no probes.  Else the hash table.
   const int32_t sb0 = S[0];
   const uint32_t span = (uint32_t)(S[s - 1] - sb0) + 1u;
-  const bool dense = span <= 32u * (uint32_t)Sh::kHash;  // same in every thread
+  const bool dense = span_ok && span <= 32u * (uint32_t)Sh::kHash;  // same in every thread
   uint32_t* bm = (uint32_t*)hkey;
   uint16_t* bpre = hval;
   if (dense) {
@@ -1727,12 +1727,14 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
         atomicAdd(&part.e[e01], (unsigned)n);
       }
       if (MULTI) {
-        const uint64_t k4 = n >= 2 ? cta_local<2, kModeCount, ShK>(g, sm, n, part, -1) : 0;
+        const uint64_t k4 =
+            n >= 2 ? cta_local<2, kModeCount, ShK>(g, sm, n, part, -1, nullptr, 0, !t.hash_only)
+                   : 0;
         emit(o, v0, tid == 0 ? (uint64_t)n : 0, k4, acc);
       } else if (!PART && n > 0) {
         uint64_t r;
         if (K - 2 == 1) r = kWsum ? wsum : (tid == 0 ? (uint64_t)n : 0);  // |L| once per CTA
-        else r = cta_local<K - 2, MODE, ShK>(g, sm, n, part, -1);
+        else r = cta_local<K - 2, MODE, ShK>(g, sm, n, part, -1, nullptr, 0, !t.hash_only);
         if (MODE == kModeWeight) acc += r; else emit(o, v0, r, 0, acc);
       }
     }
@@ -1757,7 +1759,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2)
       for (int i = tid; i < s; i += kCtaThreads) S[i] = ldg_i32(g.col + d0.x + i);
       __syncthreads();
       uint64_t q2 = 0;
-      const uint64_t r = cta_local<K - 1, MODE, ShK>(g, sm, s, part, d0.x, &q2);
+      const uint64_t r = cta_local<K - 1, MODE, ShK>(g, sm, s, part, d0.x, &q2, 0, !t.hash_only);
       if (PART) {
         // every local edge is a triangle containing v0
         const uint64_t tot = warp_sum_u64(MULTI ? q2 : r);
@@ -2016,7 +2018,7 @@ __global__ void __launch_bounds__(kHubThreads, 1)
       break;
     }
     const uint64_t r = cta_local<K - 1, kModeCount, CtaHub>(g, sm, s, Part{nullptr, nullptr}, -1,
-                                                            nullptr, off);
+                                                            nullptr, off, !t.hash_only);
     emit(o, v0, r, 0, acc);
     __syncthreads();
   }

@@ -38,6 +38,9 @@ struct TaskLists {
   // those with no sub-tasks in split_off (split_off[h + 1] == split_off[h]) do (0: every
   // hub is split)
   int hub_max = 0;
+  // CTA tasks test membership with the Bloom filter and hash even where the span bitmap
+  // fits (xgm_sched XGM_SCHED_HASH_ONLY)
+  int hash_only = 0;
   long long* log_cta = nullptr;
   long long* log_warp = nullptr;
   long long* log_split = nullptr;

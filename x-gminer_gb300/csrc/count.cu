@@ -119,6 +119,7 @@ xgm_status schedule_into(TaskBuf& tb, const DevGraph& g, int k, const xgm_sched&
                           ? 0
                           : (sp.hub_max == 0 ? kHubCap : sp.hub_max);
   XGM_CUDA_TRY(build_lists(g, tb, order, s, hub_max));
+  tb.hash_only = (sp.flags & XGM_SCHED_HASH_ONLY) ? 1 : 0;
   return XGM_OK;
 }
 

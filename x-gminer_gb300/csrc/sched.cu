@@ -260,6 +260,7 @@ TaskLists TaskBuf::lists(bool with_log) const {
   t.split_off = split_off;
   t.n = n;
   t.hub_max = hub_max;
+  t.hash_only = hash_only;
   if (with_log && log) {
     t.log_cta = log;
     t.log_warp = log + cap_v;
@@ -328,6 +329,7 @@ cudaError_t build_lists(const DevGraph& g, TaskBuf& tb, bool order, cudaStream_t
                         int hub_max) {
   const int64_t nv = g.nv;
   tb.hub_max = hub_max > kHubCap ? kHubCap : (hub_max > kCtaCap ? hub_max : 0);
+  tb.hash_only = 0;
   hub_max = tb.hub_max;
   TRY(cudaMemsetAsync(tb.n, 0, 9 * sizeof(int64_t), s));
   if (nv == 0) return cudaMemsetAsync(tb.split_off, 0, sizeof(int64_t), s);

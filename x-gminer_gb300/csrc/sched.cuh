@@ -35,6 +35,7 @@ struct TaskBuf {
   long long* log = nullptr;   // [6 * cap_v + split cap] per-task timing log (optional)
   int64_t log_cap = 0;
   int hub_max = 0;            // hubs left whole for the hub kernel (TaskLists::hub_max)
+  int hash_only = 0;          // TaskLists::hash_only
 
   TaskLists lists(bool with_log) const;
 };
