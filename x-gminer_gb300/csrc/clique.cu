@@ -999,7 +999,8 @@ __device__ uint64_t warp_vertex_task(const GView& g, WarpSmem& w, int32_t v0, Pa
   }
   const int32_t smax = __shfl_sync(kFull, xs, s - 1);
   const int32_t next = __shfl_down_sync(kFull, xs, 1);
-  // clip row lane to [S[lane+1], max(S)] (other members cannot hit), as in cta_local
+  // clip row lane to [S[lane+1], max(S)] (other members cannot hit; the CTA tier streams
+  // whole lists, whose clipping cost more than it saved there)
   if (!WGT && lane < s) {
     long long lo = dx.x, hi = dx.y;
     if (lane + 1 == s) lo = hi;
@@ -1392,7 +1393,7 @@ __device__ uint64_t warp_wide_task(const GView& g, WideSmem& w, int32_t v0, Part
   __syncwarp();
   const int32_t smax = w.S[s - 1];
   const int32_t next0 = __shfl_down_sync(kFull, xs[0], 1);  // item 4 * lane + 4
-  if (!WGT) {  // clip row i to [S[i+1], max(S)] as in cta_local
+  if (!WGT) {  // clip row i to [S[i+1], max(S)] (neutral here, unlike the CTA tier)
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int i = 4 * lane + t;
