@@ -26,6 +26,21 @@ def test_exports_every_declared_symbol(xgm):
     assert sorted(xgm.EXPORTED) == names
 
 
+def test_python_constants_match_header(xgm):
+    """The Python mirror's constants (schedule policies and flags, variants, statuses,
+    build flags, ...) equal the enum values include/xgm.h declares."""
+    txt = open(os.path.join(ROOT, "include", "xgm.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    pairs = re.findall(r"\bXGM_(\w+)\s*=\s*(-?\d+|0x[0-9a-fA-F]+)", txt)
+    checked = 0
+    for name, val in pairs:
+        if hasattr(xgm, name):
+            assert getattr(xgm, name) == int(val, 0), name
+            checked += 1
+    assert checked >= 10
+    assert xgm.SCHED_HASH_ONLY == 2 and xgm.SCHED_NO_GRAPH == 1
+
+
 def test_generators_deterministic(xgm):
     a = xgm.gen_rmat(12, 8, seed=11)
     b = xgm.gen_rmat(12, 8, seed=11)
