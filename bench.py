@@ -287,6 +287,26 @@ def cpu_sample(orc, pattern: str, scale: int, drow, dcol, budget_s: float, total
     return c, times, desc
 
 
+def host_cpu() -> dict:
+    """The host CPU the baseline ran on: model string (from /proc/cpuinfo where the kernel
+    gives one) and the online core count."""
+    import platform
+    fields = {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if ":" in line:
+                    k, v = line.split(":", 1)
+                    fields.setdefault(k.strip().lower(), v.strip())
+    except OSError:
+        pass
+    model = fields.get("model name") or fields.get("hardware") or ""
+    if not model and "cpu part" in fields:  # Arm: implementer / part ids (0x41 / 0xd4f: Neoverse V2)
+        model = f"arm implementer {fields.get('cpu implementer', '?')} part {fields['cpu part']}"
+    return {"model": model or platform.machine(), "machine": platform.machine(),
+            "nproc": os.cpu_count()}
+
+
 def sample_text(desc: dict, scale: int, dt: float) -> str:
     share = desc.get("match_share")
     return (f"seeded uniform random sample of {desc['fraction']:.6g} of the top-level vertices "
@@ -528,7 +548,7 @@ def engine_arm(args, dist: Dist) -> None:
         line["cpu_baseline"] = {"value": c / times[0], "unit": "matches/s",
                                 "cores": oracle.threads(), "kind": "port",
                                 "sample": sample_text(desc, args.scale, times[0]),
-                                "sample_detail": desc}
+                                "sample_detail": desc, "host": host_cpu()}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     if g is not None:
@@ -620,7 +640,7 @@ def reference_arm(args, dist: Dist) -> None:
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "matches/s", "cores": cores, "kind": "port",
                              "sample": sample_text(desc, args.scale, ms / 1e3),
-                             "sample_detail": desc},
+                             "sample_detail": desc, "host": host_cpu()},
             "e2e": {"value": value, "unit": "matches/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -736,7 +756,7 @@ def patterns5_arm(args, dist: Dist) -> None:
         dt = time.perf_counter() - t0
         gpu_ms = sum(v["ms"] for k, v in per.items() if k.startswith("er_"))
         line["cpu_baseline"] = {"value": c / dt, "unit": "matches/s", "cores": cores,
-                                "kind": "port",
+                                "kind": "port", "host": host_cpu(),
                                 "sample": f"P6-P22 on the ER graph ({c} matches in {dt:.2f} s, "
                                           f"OpenMP oracle port; the GPU took {gpu_ms:.1f} ms)"}
     print(json.dumps(line), flush=True)
