@@ -624,7 +624,8 @@ struct Part {
 // DAG induced on S, Q = 1..6.  PART (Q == 2 only, S = N+(root) starting at col entry
 // sbase): every local edge (i, j) is the triangle (root, S[i], S[j]); it is credited to
 // vertices S[i], S[j] and edges (root,S[i]), (root,S[j]), (S[i],S[j]).  The root's own
-// credit is the returned count.
+// credit is the returned count.  span_ok = false keeps the Bloom filter + hash membership
+// test even where the span bitmap fits (XGM_SCHED_HASH_ONLY).
 template <int Q, int MODE, class Sh = CtaMain>
 __device__ uint64_t cta_local(const GView& g, char* sm, int s, Part part, long long sbase,
                               uint64_t* q2out = nullptr, int s_off = 0, bool span_ok = true) {
