@@ -301,8 +301,10 @@ def host_cpu() -> dict:
     except OSError:
         pass
     model = fields.get("model name") or fields.get("hardware") or ""
-    if not model and "cpu part" in fields:  # Arm: implementer / part ids (0x41 / 0xd4f: Neoverse V2)
-        model = f"arm implementer {fields.get('cpu implementer', '?')} part {fields['cpu part']}"
+    if not model and "cpu part" in fields:  # Arm: implementer / part ids
+        impl, part = fields.get("cpu implementer", "?"), fields["cpu part"]
+        known = {("0x41", "0xd4f"): "Arm Neoverse V2"}  # the Grace host CPU
+        model = known.get((impl, part), f"arm implementer {impl} part {part}")
     return {"model": model or platform.machine(), "machine": platform.machine(),
             "nproc": os.cpu_count()}
 
